@@ -1,0 +1,90 @@
+// One (Sz, kx, ky) sector resident on the GPU, plus the kernel launchers that
+// build and apply it.  Host-side only types live here next to the device view.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <complex>
+#include <string>
+#include <vector>
+
+#include "edg_core.cuh"
+
+namespace edg {
+
+// Device pointers of one sector, passed by value to every kernel.
+struct SectorView {
+  const SectorParams* params;
+  const uint64_t* reps;
+  const uint8_t* lid;
+  RankRec* recs;
+  const uint32_t* Ia;
+  const int64_t* Ib;
+  const TermGroup* groups;
+  const ChTerm* ch;
+  const Bowtie* bows;
+  const uint8_t* nk;       // torus: rotation minimum of each row value
+  const uint16_t* rots;    // torus: rotations reaching it
+  const uint64_t* perms;   // walk: 2 x n_chunks x 256 permutation chunk tables
+  const uint64_t* binom;   // (kMaxSites+1)^2 binomials
+  int n_chunks;
+  int row_bits;            // torus: Lx (table size 2^Lx)
+};
+
+// Shared-memory image a kernel stages per CTA (see stage_sector()).
+template <typename Real>
+struct SmemGroup {
+  uint64_t mask;
+  Real fac;
+  Real Bre[2], Bim[2];
+  int16_t a;
+  int16_t ch_begin, ch_end;
+};
+template <typename Real>
+struct SmemCh {
+  Real Are[2], Aim[2];
+  int z;
+};
+
+struct DeviceBuffer {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+};
+
+struct Sector {
+  int device = 0;
+  SectorParams P{};
+  SectorView V{};
+  // device allocations
+  SectorParams* dP = nullptr;
+  uint64_t* reps = nullptr;
+  uint8_t* lid = nullptr;
+  RankRec* recs = nullptr;
+  uint32_t* Ia = nullptr;
+  int64_t* Ib = nullptr;
+  TermGroup* groups = nullptr;
+  ChTerm* ch = nullptr;
+  Bowtie* bows = nullptr;
+  uint8_t* nk = nullptr;
+  uint16_t* rots = nullptr;
+  uint64_t* perms = nullptr;
+  uint64_t* binom = nullptr;
+  size_t device_bytes = 0;
+  // host copies used by the adapters
+  std::vector<int> T1, T2;
+  double lambda = 1, Ch = 0, ChCh = 0;
+  // scratch kept for host-buffer H*v calls
+  DeviceBuffer host_in, host_out;
+  cudaStream_t stream = nullptr;
+  // Lanczos work area (allocated on first use)
+  DeviceBuffer lz_work;
+};
+
+// basis.cu
+cudaError_t build_basis(Sector& S, std::string& err);
+cudaError_t export_walk_tables(const Sector& S, int64_t* rep_loc_dev, int32_t* g_dev, cudaStream_t st);
+// hv.cu
+cudaError_t launch_hv(const Sector& S, const void* v, void* w, bool fp64, cudaStream_t st);
+cudaError_t count_offdiag(const Sector& S, unsigned long long* nnz_dev, cudaStream_t st);
+int hv_grid_blocks(bool fp64, bool torus, bool chch);
+
+}  // namespace edg

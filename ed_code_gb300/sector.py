@@ -1,0 +1,136 @@
+"""Python side of the GPU sector: the reference's sector surface over the C ABI.
+
+``GpuSector(model)`` is what ``sector_lanczos`` (Lanczos_sector.cpp:15-198)
+builds before it diagonalises: the (Sz, kx, ky) momentum basis, here built
+and kept on the GPU.  ``sHv`` mirrors the reference's ``sHv`` (H_v.cpp:192;
+H_v.h:36-57): host vectors in, host vector out.  ``hv`` applies H to CUDA
+tensors already on the device.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional, Tuple
+
+import numpy as np
+
+from . import _native as N
+from .lattice import Model
+
+
+def _model_struct(model: Model):
+    """edg_model for a lattice.Model; returns (struct, keep-alive list)."""
+    n = model.n_sites
+    T1 = (C.c_int * n)(*model.T1)
+    T2 = (C.c_int * n)(*model.T2)
+    bonds = (N.edg_bond * max(1, len(model.adj_list)))(
+        *[N.edg_bond(b.x, b.y, b.J, b.expphase.real, b.expphase.imag) for b in model.adj_list])
+    tris = (N.edg_triangle * max(1, len(model.ch_list)))(
+        *[N.edg_triangle(t.i, t.j, t.k, t.expphase.real, t.expphase.imag) for t in model.ch_list])
+    bows = (N.edg_bowtie * max(1, len(model.chch_list)))(
+        *[N.edg_bowtie(b.x, b.y, b.z, b.p, b.q, b.r) for b in model.chch_list])
+    m = N.edg_model(n, T1, T2, model.Jz, bonds, len(model.adj_list), model.Ch, tris, len(model.ch_list),
+                    model.ChCh, bows, len(model.chch_list))
+    return m, [T1, T2, bonds, tris, bows]
+
+
+class GpuSector:
+    """One (Sz, kx, ky) sector resident on the current CUDA device."""
+
+    def __init__(self, model: Model, n_ones: Optional[int] = None):
+        self.model = model
+        self.n_ones = model.n_ones if n_ones is None else int(n_ones)
+        m, self._keep = _model_struct(model)
+        h = C.c_void_p()
+        N.check(N.lib().edg_sector_create(C.byref(m), self.n_ones, int(model.kx), int(model.ky), C.byref(h)))
+        self._h = h
+        info = N.edg_sector_info()
+        N.check(N.lib().edg_sector_get_info(self._h, C.byref(info)))
+        self.info = {f: getattr(info, f) for f, _ in N.edg_sector_info._fields_}
+        self.n_p = int(info.n_p)
+
+    # -- basis tables ------------------------------------------------------
+    def basis(self) -> Tuple[np.ndarray, np.ndarray, np.ndarray]:
+        """(pblock_states, norm, norm_inv) as pConstruct_States returns them."""
+        st = np.empty(self.n_p, np.int64)
+        nr = np.empty(self.n_p, np.float64)
+        ni = np.empty(self.n_p, np.float64)
+        N.check(N.lib().edg_sector_copy_basis(self._h, st.ctypes.data, nr.ctypes.data, ni.ctypes.data))
+        return st, nr, ni
+
+    def lin_tables(self) -> Tuple[np.ndarray, np.ndarray, int]:
+        nh = 1 << (self.model.n_sites // 2)
+        Ia = np.empty(nh, np.int64)
+        Ib = np.empty(nh, np.int64)
+        br = C.c_int64()
+        N.check(N.lib().edg_sector_copy_lin_tables(self._h, Ia.ctypes.data, Ib.ctypes.data, C.byref(br)))
+        return Ia, Ib, int(br.value)
+
+    def config_tables(self, max_configs: int = 1 << 26):
+        """(rep_loc, state_ph, lxly) over all C(N, n_up) configurations."""
+        nc = int(self.info["n_configs"])
+        rl = np.empty(nc, np.int64)
+        ph = np.empty(nc, np.complex128)
+        lxly = np.empty((nc, 2), np.int32)
+        N.check(N.lib().edg_sector_copy_config_tables(self._h, int(max_configs), rl.ctypes.data, ph.ctypes.data,
+                                                      lxly.ctypes.data))
+        return rl, ph, lxly
+
+    # -- H*v -----------------------------------------------------------------
+    def sHv(self, v: np.ndarray, dtype=np.complex128) -> np.ndarray:
+        """w = H v with host arrays (copies in and out inside the call)."""
+        dt = np.dtype(dtype)
+        if dt not in (np.complex128, np.complex64):
+            raise TypeError("dtype must be complex128 or complex64")
+        v = np.ascontiguousarray(v, dtype=dt)
+        if v.shape != (self.n_p,):
+            raise ValueError(f"v must have shape ({self.n_p},)")
+        w = np.empty_like(v)
+        code = N.EDG_C128 if dt == np.complex128 else N.EDG_C64
+        N.check(N.lib().edg_hv_host(self._h, v.ctypes.data, w.ctypes.data, code))
+        return w
+
+    def hv(self, v, w, stream=None) -> None:
+        """w = H v on CUDA tensors (complex128 or complex64, n_p entries)."""
+        import torch
+
+        if v.dtype not in (torch.complex128, torch.complex64) or w.dtype != v.dtype:
+            raise TypeError("v and w must both be complex128 or both complex64")
+        if not (v.is_cuda and w.is_cuda and v.is_contiguous() and w.is_contiguous()):
+            raise ValueError("v and w must be contiguous CUDA tensors")
+        if v.numel() != self.n_p or w.numel() != self.n_p:
+            raise ValueError(f"v and w must have {self.n_p} entries")
+        code = N.EDG_C128 if v.dtype == torch.complex128 else N.EDG_C64
+        st = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        N.check(N.lib().edg_hv(self._h, C.c_void_p(v.data_ptr()), C.c_void_p(w.data_ptr()), code, C.c_void_p(st)))
+
+    def count_offdiag(self) -> int:
+        n = C.c_int64()
+        N.check(N.lib().edg_count_offdiag(self._h, C.byref(n)))
+        return int(n.value)
+
+    def algorithmic_bytes(self, elem_bytes: int, nnz_off: Optional[int] = None) -> int:
+        """Bytes one H*v must move at minimum: per row the representative (8),
+        the stabiliser byte (1), v_i and w_i; per off-diagonal target one v_j."""
+        if nnz_off is None:
+            nnz_off = self.count_offdiag()
+        return self.n_p * (8 + 1 + 2 * elem_bytes) + nnz_off * elem_bytes
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            N.lib().edg_sector_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def fill_random(t, seed: int, stream=None) -> None:
+    """Fill a complex CUDA tensor with the splitmix64 test vector for `seed`."""
+    import torch
+
+    code = N.EDG_C128 if t.dtype == torch.complex128 else N.EDG_C64
+    st = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    N.check(N.lib().edg_fill_random(C.c_void_p(t.data_ptr()), t.numel(), code, int(seed), C.c_void_p(st)))

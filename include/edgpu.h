@@ -1,0 +1,116 @@
+/* edgpu -- GB300 (sm_103a) momentum-sector exact diagonalisation, C ABI.
+ *
+ * Drop-in GPU replacement for the H*v hot path of hiteshjc/ED_Code and the
+ * solvers around it.  Every entry point below names the reference interface
+ * it replaces (paths are src/ files of the reference).  All pointers are
+ * plain host or device pointers; no C++ or framework types cross this
+ * boundary.  Every function returns EDG_OK (0) or an EDG_ERR_* code;
+ * edg_last_error() returns the message of the last failure on the calling
+ * thread.  Complex vectors are interleaved (re, im) arrays: EDG_C128 is
+ * double[2*n] (std::complex<double>), EDG_C64 is float[2*n].
+ */
+#ifndef EDGPU_H
+#define EDGPU_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EDGPU_ABI_VERSION 1
+
+enum {
+  EDG_OK = 0,
+  EDG_ERR_INVALID = 1,      /* malformed argument (bad permutation, odd N, n_ones out of range, ...) */
+  EDG_ERR_MOMENTUM = 2,     /* kx/ky outside [0,L1)x[0,L2): the reference's "Invalid kx or ky" */
+  EDG_ERR_EMPTY = 3,        /* the sector has no states: the reference's "No states in psector" */
+  EDG_ERR_CUDA = 4,         /* a CUDA call failed */
+  EDG_ERR_NOMEM = 5,        /* not enough device memory for the sector */
+  EDG_ERR_UNSUPPORTED = 6,  /* outside what this library implements (N > 40, too many terms) */
+  EDG_ERR_NOT_CONVERGED = 7 /* eigensolver stopped without meeting its tolerance */
+};
+
+enum { EDG_C128 = 0, EDG_C64 = 1 };
+
+/* Term-list entries, field for field the reference's structs (global.h:25-40).
+ * expphase is given as (re, im). */
+typedef struct { int x, y; double J, re, im; } edg_bond;          /* coordinates */
+typedef struct { int i, j, k; double re, im; } edg_triangle;      /* triangles   */
+typedef struct { int x, y, z, p, q, r; } edg_bowtie;              /* bowties     */
+
+/* The Hamiltonian: what ED_2D_Lattice_Geometry (read_input_file.cpp:110-430)
+ * hands to sector_lanczos.  lambda is Jz. */
+typedef struct {
+  int n_sites;
+  const int* T1;
+  const int* T2;
+  double lambda;
+  const edg_bond* bonds;
+  int n_bonds;
+  double Ch;
+  const edg_triangle* triangles;
+  int n_triangles;
+  double ChCh;
+  const edg_bowtie* bowties;
+  int n_bowties;
+} edg_model;
+
+typedef struct edg_sector edg_sector;
+
+typedef struct {
+  int n_sites, n_ones, L1, L2, kx, ky;
+  int torus;             /* 1: row-rotation orbit search, 0: the reference's walk */
+  int n_groups;          /* distinct flipped pairs after merging bond + chirality terms */
+  int64_t n_p;           /* sector dimension */
+  int64_t n_configs;     /* C(N, n_ones) */
+  int64_t device_bytes;  /* device memory held by the sector */
+} edg_sector_info;
+
+const char* edg_last_error(void);
+int edg_abi_version(void);
+
+/* Build the (n_ones, kx, ky) sector on the current CUDA device.
+ * Replaces: LxLy + pConstruct_States (Momentum_Basis.cpp:19-36, 645-778) and
+ * Lin_Tables (Lin_Tables.cpp:57-78) as called from sector_lanczos
+ * (Lanczos_sector.cpp:48-97).  Errors: EDG_ERR_MOMENTUM, EDG_ERR_EMPTY as the
+ * reference's exit(1) paths (Lanczos_sector.cpp:51-55, 93-97). */
+int edg_sector_create(const edg_model* model, int n_ones, int kx, int ky, edg_sector** out);
+int edg_sector_destroy(edg_sector* s);
+int edg_sector_get_info(const edg_sector* s, edg_sector_info* info);
+
+/* Host copies of pblock_states, norm and norm_inv (Momentum_Basis.cpp:756-770).
+ * Any pointer may be NULL. */
+int edg_sector_copy_basis(const edg_sector* s, int64_t* states, double* norm, double* norm_inv);
+
+/* Host copies of the Lin tables Ia, Ib (2^(N/2) entries each; Lin_Tables.cpp:57-78,
+ * Momentum_Basis.cpp:731-737) and bits_right. */
+int edg_sector_copy_lin_tables(const edg_sector* s, int64_t* Ia, int64_t* Ib, int64_t* bits_right);
+
+/* The reference's per-configuration tables rep_loc and state_ph
+ * (Momentum_Basis.cpp:750-777), computed with the reference's own orbit walk,
+ * for parity checks on sectors with at most max_configs configurations.
+ * state_ph is interleaved (re, im); lxly receives lx, ly pairs; any output may be NULL. */
+int edg_sector_copy_config_tables(const edg_sector* s, int64_t max_configs, int64_t* rep_loc, double* state_ph,
+                                  int32_t* lxly);
+
+/* w = H v on device pointers (n_p complex entries each, dtype EDG_C128 or
+ * EDG_C64), enqueued on `stream` (a cudaStream_t, NULL = the sector's stream).
+ * Replaces: sHv (H_v.cpp:192-357, declared H_v.h:36-57). */
+int edg_hv(edg_sector* s, const void* v, void* w, int dtype, void* stream);
+
+/* Same with host buffers: copies v in, applies H, copies w out, synchronises.
+ * This is the call the reference's sHv(v, w, ...) adapter makes. */
+int edg_hv_host(edg_sector* s, const void* v, void* w, int dtype);
+
+/* Number of nonzero off-diagonal bond/chirality targets summed over rows
+ * (the nnz_off of the algorithmic byte count). */
+int edg_count_offdiag(edg_sector* s, int64_t* nnz_off);
+
+/* Deterministic complex test vector (splitmix64, entries uniform in [-1,1)^2)
+ * written to device memory; the same generator as the test suite's. */
+int edg_fill_random(void* dst, int64_t n, int dtype, uint64_t seed, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

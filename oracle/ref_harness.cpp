@@ -1,0 +1,126 @@
+// Dump harness for the reference implementation (test infrastructure only).
+//
+// Links the reference's own objects (everything but ED.o), parses a reference
+// input file with the reference parser (read_input_file.cpp:110
+// ED_2D_Lattice_Geometry), builds the momentum basis with the reference
+// pConstruct_States (Momentum_Basis.cpp:645) and applies the reference sHv
+// (H_v.cpp:192) to caller-supplied vectors.  Everything is written as raw
+// little-endian arrays into an output directory:
+//
+//   meta.txt          n_sites n_ones L1 L2 kx ky n_p n_configs bits_right
+//   states.i64        pblock_states            (n_p)
+//   norm.f64          norm                     (n_p)
+//   rep_loc.i64       rep_loc                  (n_configs)      [tables mode]
+//   state_ph.c128     state_ph                 (n_configs)      [tables mode]
+//   Ia.i64, Ib.i64    Lin tables               (2^half)         [tables mode]
+//   w<k>.c128         sHv(v<k>)                                 [if v<k>.c128 given]
+//   terms.txt         adj_list / ch_list / chch_list / T1 / T2 as parsed
+//
+// usage: ref_harness <input-file> <out-dir> [tables|notables] [nvec] [reps]
+// The v<k>.c128 inputs are read from <out-dir>.  With reps > 1 each sHv call
+// is repeated and the mean wall time per call is written to hv_time.txt.
+#include <sys/stat.h>
+
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <string>
+#include <vector>
+
+#include "H_v.h"
+#include "Lanczos_sector.h"
+#include "Momentum_Basis.h"
+#include "read_input_file.h"
+
+template <class T>
+static void dump(const std::string& path, const std::vector<T>& a) {
+  FILE* f = std::fopen(path.c_str(), "wb");
+  if (!f) { std::perror(path.c_str()); std::exit(2); }
+  if (!a.empty()) std::fwrite(a.data(), sizeof(T), a.size(), f);
+  std::fclose(f);
+}
+
+static bool read_vec(const std::string& path, std::vector<std::complex<double>>& v, int64_t n) {
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) return false;
+  v.resize(n);
+  size_t got = std::fread(v.data(), sizeof(std::complex<double>), n, f);
+  std::fclose(f);
+  if ((int64_t)got != n) { std::fprintf(stderr, "short vector %s\n", path.c_str()); std::exit(2); }
+  return true;
+}
+
+int main(int argc, char** argv) {
+  if (argc < 3) { std::fprintf(stderr, "usage: %s input outdir [tables|notables] [nvec] [reps]\n", argv[0]); return 1; }
+  std::string in = argv[1], out = argv[2];
+  bool tables = argc < 4 || std::string(argv[3]) == "tables";
+  int nvec = argc > 4 ? std::atoi(argv[4]) : 0;
+  int reps = argc > 5 ? std::atoi(argv[5]) : 1;
+  mkdir(out.c_str(), 0755);
+  std::ofstream log((out + "/ref_log.txt").c_str());
+
+  double tol = 1e-11; bool use_arpack = false; int iters = 100, ncyc = 10;
+  routine_parameters(in, tol, use_arpack, iters, ncyc);
+  int n_spins = 0; double Jz = 1, J1 = 1, J2 = 0, Ch = 0, ChCh = 0;
+  std::vector<coordinates> adj; std::vector<triangles> chl; std::vector<bowties> chch;
+  std::vector<int> T1, T2, cut; double sSz = -1; int kx = -1, ky = -1;
+  bool all_s = false, psec = false, find_v = false, unwrap = true; double szs = -1;
+  int nev = 2; std::string vpath;
+  ED_2D_Lattice_Geometry(in, n_spins, Jz, J1, J2, adj, Ch, chl, ChCh, chch, T1, T2, cut, sSz, kx, ky, all_s, szs,
+                         psec, nev, find_v, unwrap, vpath, log);
+  // Same n_ones rule as Lanczos_sector.cpp:45-46.
+  int n_ones = int(sSz + n_spins / 2 + 1.0e-6);
+  int L1 = 0, L2 = 0;
+  LxLy(L1, L2, T1, T2);
+  double px = 2 * kx * M_PI / L1, py = 2 * ky * M_PI / L2;
+  std::vector<int64_t> states, rep_loc, Ia, Ib; std::vector<double> norm, norm_inv;
+  std::vector<std::complex<double>> state_ph; int64_t n_p = 0; int bits_right = 0;
+  double t0 = wall_clock();
+  pConstruct_States(states, norm, norm_inv, T1, T2, n_ones, px, py, n_p, rep_loc, state_ph, Ia, Ib, bits_right, log);
+  double t_basis = wall_clock() - t0;
+
+  FILE* m = std::fopen((out + "/meta.txt").c_str(), "w");
+  std::fprintf(m, "%d %d %d %d %d %d %lld %lld %d %.6f\n", n_spins, n_ones, L1, L2, kx, ky, (long long)n_p,
+               (long long)rep_loc.size(), bits_right, t_basis);
+  std::fclose(m);
+  {
+    // Term lists exactly as the reference parser produced them.
+    FILE* t = std::fopen((out + "/terms.txt").c_str(), "w");
+    std::fprintf(t, "lambda %.17g Ch %.17g ChCh %.17g J1 %.17g J2 %.17g\n", Jz, Ch, ChCh, J1, J2);
+    std::fprintf(t, "T1");
+    for (int v : T1) std::fprintf(t, " %d", v);
+    std::fprintf(t, "\nT2");
+    for (int v : T2) std::fprintf(t, " %d", v);
+    std::fprintf(t, "\n");
+    for (auto& b : adj) std::fprintf(t, "bond %d %d %.17g %.17g %.17g\n", b.x, b.y, b.J, b.expphase.real(), b.expphase.imag());
+    for (auto& c : chl) std::fprintf(t, "ch %d %d %d %.17g %.17g\n", c.i, c.j, c.k, c.expphase.real(), c.expphase.imag());
+    for (auto& c : chch) std::fprintf(t, "chch %d %d %d %d %d %d\n", c.x, c.y, c.z, c.p, c.q, c.r);
+    std::fclose(t);
+  }
+  dump(out + "/states.i64", states);
+  dump(out + "/norm.f64", norm);
+  if (tables) {
+    dump(out + "/rep_loc.i64", rep_loc);
+    dump(out + "/state_ph.c128", state_ph);
+    dump(out + "/Ia.i64", Ia);
+    dump(out + "/Ib.i64", Ib);
+  }
+  double t_hv = 0; int calls = 0;
+  for (int k = 0; k < nvec; ++k) {
+    std::vector<std::complex<double>> v, w(n_p);
+    if (!read_vec(out + "/v" + std::to_string(k) + ".c128", v, n_p)) break;
+    for (int r = 0; r < reps; ++r) {
+      double t1 = wall_clock();
+      sHv(v.data(), w.data(), states, norm, norm_inv, rep_loc, state_ph, Jz, adj, Ch, chl, ChCh, chch, n_spins, Ia,
+          Ib, bits_right, T1, T2, px, py, log);
+      t_hv += wall_clock() - t1; ++calls;
+    }
+    dump(out + "/w" + std::to_string(k) + ".c128", w);
+  }
+  if (calls) {
+    FILE* t = std::fopen((out + "/hv_time.txt").c_str(), "w");
+    std::fprintf(t, "%.9f %d\n", t_hv / calls, calls);
+    std::fclose(t);
+  }
+  return 0;
+}

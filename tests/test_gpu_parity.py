@@ -1,0 +1,175 @@
+"""GPU library against the reference (golden fixtures) and the oracle.
+
+Integer work (representatives, norms, Lin tables, rep_loc, phase indices) must
+be bit-exact.  H*v in FP64 must match the reference's sHv to 1e-13 relative to
+max|w|; H*v in FP32 to 2e-5 relative (single-precision accumulation over
+about 50 terms per row).
+"""
+import hashlib
+
+import numpy as np
+import pytest
+
+from conftest import all_golden_sectors, golden_arrays, golden_cases, golden_model
+
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-13
+FP32_TOL = 2e-5
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+@pytest.fixture(scope="module")
+def gpu(cuda_device):
+    from ed_code_gb300 import sector
+
+    return sector
+
+
+@pytest.mark.parametrize("name,idx", all_golden_sectors(max_configs=3_000_000))
+def test_basis_tables_bit_exact(gpu, name, idx):
+    meta = golden_cases()[name]["sectors"][idx]
+    sec = gpu.GpuSector(golden_model(name, idx))
+    assert sec.n_p == meta["n_p"]
+    states, norm, norm_inv = sec.basis()
+    assert sha(states) == meta["sha_states"]
+    assert sha(norm) == meta["sha_norm"]
+    Ia, Ib, bits_right = sec.lin_tables()
+    assert sha(Ia) == meta["sha_Ia"] and sha(Ib) == meta["sha_Ib"]
+    assert bits_right == meta["bits_right"]
+    rep_loc, state_ph, lxly = sec.config_tables()
+    assert sha(rep_loc) == meta["sha_rep_loc"]
+    g = golden_arrays(name)
+    tag = f"s{idx}"
+    if meta["full"]:
+        np.testing.assert_array_equal(state_ph, g[f"{tag}_state_ph"])
+        np.testing.assert_array_equal(states, g[f"{tag}_states"])
+    else:
+        cfg = g[f"{tag}_cfg"]
+        np.testing.assert_array_equal(state_ph[cfg], g[f"{tag}_state_ph_at_cfg"])
+
+
+@pytest.mark.parametrize("name,idx", all_golden_sectors(max_configs=3_000_000))
+@pytest.mark.parametrize("dtype", [np.complex128, np.complex64])
+def test_hv_matches_reference(gpu, name, idx, dtype):
+    meta = golden_cases()[name]["sectors"][idx]
+    sec = gpu.GpuSector(golden_model(name, idx))
+    g = golden_arrays(name)
+    tag = f"s{idx}"
+    tol = FP64_TOL if dtype == np.complex128 else FP32_TOL
+    for k, seed in enumerate(meta["vec_seeds"]):
+        v = O.splitmix_vector(sec.n_p, seed)
+        w = sec.sHv(v.astype(dtype), dtype=dtype).astype(np.complex128)
+        if meta["full"]:
+            ref = g[f"{tag}_w{k}"]
+            scale = max(1.0, np.abs(ref).max())
+            err = np.abs(w - ref).max() / scale
+            assert err <= tol, err
+        else:
+            rows = g[f"{tag}_rows"]
+            ref = g[f"{tag}_w{k}_at_rows"]
+            scale = max(1.0, np.abs(ref).max())
+            assert np.abs(w[rows] - ref).max() / scale <= tol
+            assert abs(np.vdot(w, w).real - g[f"{tag}_w{k}_norm2"][0]) <= 100 * tol * g[f"{tag}_w{k}_norm2"][0]
+
+
+def test_hv_device_equals_host(gpu):
+    import torch
+
+    sec = gpu.GpuSector(golden_model("tri4x3_chch", 0))
+    v = O.splitmix_vector(sec.n_p, 3)
+    w_host = sec.sHv(v)
+    vd = torch.from_numpy(v).cuda()
+    wd = torch.empty_like(vd)
+    sec.hv(vd, wd)
+    torch.cuda.synchronize()
+    assert np.array_equal(wd.cpu().numpy(), w_host)
+
+
+def test_fill_random_matches_host_generator(gpu):
+    import torch
+
+    t = torch.empty(1000, dtype=torch.complex128, device="cuda")
+    gpu.fill_random(t, 17)
+    torch.cuda.synchronize()
+    assert np.array_equal(t.cpu().numpy(), O.splitmix_vector(1000, 17))
+
+
+def test_errors_mirror_reference_exit_paths(gpu):
+    from ed_code_gb300 import lattice as L
+    from ed_code_gb300._native import EdgError
+
+    m = L.make_model(L.TorusSpec("square", 4, 4), 0, 4, 0)  # kx == L1: "Invalid kx or ky"
+    with pytest.raises(EdgError) as e:
+        gpu.GpuSector(m)
+    assert e.value.code == 2
+    m = L.make_model(L.TorusSpec("square", 4, 4), -8, 1, 0)  # only |0...0>, k != 0: empty sector
+    with pytest.raises(EdgError) as e:
+        gpu.GpuSector(m)
+    assert e.value.code == 3
+
+
+def test_nnz_offdiag_count_matches_oracle(gpu):
+    model = golden_model("tri4x3", 1)
+    sec = gpu.GpuSector(model)
+    osec = O.OracleSector(model)
+    # count targets with an allowed representative, one per anti-aligned bond pair
+    pairs = sorted({(min(b.x, b.y), max(b.x, b.y)) for b in model.adj_list} |
+                   {(min(t.i, t.j), max(t.i, t.j)) for t in model.ch_list})
+    n = 0
+    for s in osec.states:
+        for a, b in pairs:
+            if ((int(s) >> a) & 1) != ((int(s) >> b) & 1):
+                t = int(s) ^ (1 << a) ^ (1 << b)
+                left, right = t >> (model.n_sites // 2), t & osec.bits_right
+                loc = osec.Ia[right] + osec.Ib[left] - 1
+                n += osec.rep_loc[loc] >= 0
+    assert sec.count_offdiag() == n
+
+
+def large_sector_check(gpu, spec, Sz, kx, ky, n_rows=512, seed=9):
+    """Sectors beyond the reference's reach: properties plus row samples from the oracle."""
+    from ed_code_gb300 import lattice as L
+
+    model = L.make_model(spec, Sz, kx, ky)
+    sec = gpu.GpuSector(model)
+    assert sec.n_p == O.sector_dim(model)       # independent character count
+    states, norm, _ = sec.basis()
+    assert np.all(np.diff(states) > 0)          # strictly ascending like pblock_states
+    rng = np.random.default_rng(seed)
+    rows = np.sort(rng.choice(sec.n_p, size=min(n_rows, sec.n_p), replace=False))
+    lid = np.rint(model.n_sites / norm.astype(np.float64) ** 2).astype(np.int32)  # L1*L2/norm^2
+    for r in rows[:64]:
+        assert O.allowed_rep(model, int(states[r])) == lid[r]
+    v = O.splitmix_vector(sec.n_p, seed)
+    w = sec.sHv(v)
+    ref = O.hv_rows(model, states, lid, v, rows)
+    scale = max(1.0, np.abs(ref).max())
+    assert np.abs(w[rows] - ref).max() / scale <= FP64_TOL
+    w32 = sec.sHv(v.astype(np.complex64), dtype=np.complex64)
+    assert np.abs(w32[rows] - ref).max() / scale <= FP32_TOL
+    # Hermiticity as a size-independent property: <u|H v> = conj(<v|H u>)
+    u = O.splitmix_vector(sec.n_p, seed + 1)
+    hu = sec.sHv(u)
+    assert abs(np.vdot(u, w) - np.conj(np.vdot(v, hu))) <= 1e-11 * np.sqrt(sec.n_p) * scale
+    return sec
+
+
+def test_large_sector_6x5_triangular(gpu):
+    from ed_code_gb300 import lattice as L
+
+    large_sector_check(gpu, L.TorusSpec("triangular", 6, 5, Jz=0.8, Ch=0.2), 0, 2, 3)
+
+
+def test_large_sector_6x5_generic_walk(gpu):
+    """A relabelled torus forces the reference's walk instead of the row-rotation search."""
+    from ed_code_gb300 import lattice as L
+
+    perm = [int(x) for x in np.random.default_rng(4).permutation(20)]
+    sec = large_sector_check(gpu, L.TorusSpec("triangular", 5, 4, Jz=0.9, Ch=0.3, relabel=perm), 0, 1, 2)
+    assert sec.info["torus"] == 0
