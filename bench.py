@@ -1,0 +1,342 @@
+#!/usr/bin/env python
+"""Benchmark of the momentum-sector H*v (the hot path of ED_Code's sHv).
+
+Workload (default): triangular 6x6 torus, N=36, J1=1, Delta=1, Jchi=0.15,
+Sz=0, k=Gamma -- 252,091,362 basis states, FP32 complex vectors (2 GB each),
+synthetic seeded start vector.  One step is one full H*v.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME]
+  python bench.py --impl reference ...   # the reference algorithm on the host cores
+
+Timed region (device arm): K back-to-back H*v launches on the stream they are
+enqueued on, bracketed by a barrier and a synchronize, timed with CUDA events;
+inputs (2 GB vectors, 3.8 GB sector) are far larger than L2, so no flush is
+needed.  `e2e` repeats the measurement through the C ABI's host-buffer call
+(edg_hv_host): pinned host v in, host w out, copies inside the timed region.
+The CPU baseline runs the oracle's restatement of the reference's sHv row
+formula (orbit walk + binary search, as the reference's tables cannot exist at
+N=36) on a bounded sample of rows, on every host core.
+
+Multi-GPU: sectors are independent units, so N GPUs run N replicas with no
+data-path collective ("weak" scaling); value = all ranks' H*v / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "36-site H*v/s, GB/s; mixed-stream solves/s, p99 at |ΔE|≤1e-9 vs FP64 plain"
+UNIT = "H*v/s"
+
+WORKLOADS = {
+    # the large single sector: 6x6 triangular, Delta=1, Jchi=0.15, Sz=0, k=Gamma
+    "tri6x6_k00": dict(lattice="triangular", Lx=6, Ly=6, Jz=1.0, Ch=0.15, Sz=0, kx=0, ky=0),
+    # smaller cases of the same kernel (profiling, quick checks)
+    "tri8x4_k00": dict(lattice="triangular", Lx=8, Ly=4, Jz=1.0, Ch=0.15, Sz=0, kx=0, ky=0),
+    "tri6x5_k23": dict(lattice="triangular", Lx=6, Ly=5, Jz=0.8, Ch=0.2, Sz=0, kx=2, ky=3),
+}
+
+
+def measured_peak_hbm():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic(kernel_tag: str):
+    """DRAM bytes per launch recorded from an ncu capture in profiles/<tag>.md."""
+    path = os.path.join(ROOT, "profiles", f"{kernel_tag}.md")
+    try:
+        for line in open(path):
+            if line.strip().startswith("dram_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.idx = device_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax = float(p[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        sm.sort()
+        med = sm[len(sm) // 2] if sm else None
+        return {"sm_mhz": med, "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_model(name):
+    from ed_code_gb300 import lattice as L
+
+    w = dict(WORKLOADS[name])
+    spec = L.TorusSpec(w.pop("lattice"), w.pop("Lx"), w.pop("Ly"), Jz=w.pop("Jz"), Ch=w.pop("Ch"))
+    return L.make_model(spec, w["Sz"], w["kx"], w["ky"])
+
+
+def cpu_sample_rate(model, reps, lid, budget_s: float, threads: int, seed: int = 4):
+    """H*v per second of the oracle's row formula, from a timed sample of rows."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    n_p = len(reps)
+    rng = np.random.default_rng(seed)
+    v = O.splitmix_vector(n_p, seed)
+    n_rows = 256
+    while True:
+        rows = np.sort(rng.choice(n_p, size=min(n_rows, n_p), replace=False))
+        t0 = time.perf_counter()
+        O.hv_rows(model, reps, lid, v, rows, threads)
+        dt = time.perf_counter() - t0
+        if dt >= 0.25 * budget_s or n_rows >= n_p:
+            break
+        n_rows = int(min(n_p, n_rows * max(2.0, 0.5 * budget_s / max(dt, 1e-3))))
+    return len(rows) / dt / n_p, len(rows), dt
+
+
+def run_reference(args, world, rank):
+    """The reference's algorithm (CPU restatement; its own tables cannot exist at N=36)."""
+    if rank != 0:
+        return 0
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    model = build_model(args.workload)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    reps, lid = O.build_reps(model, threads)
+    t_basis = time.perf_counter() - t0
+    n_p = len(reps)
+    v = O.splitmix_vector(n_p, 4)
+    rng = np.random.default_rng(4)
+    # rows per step: about budget seconds of work each
+    rows = np.sort(rng.choice(n_p, size=min(2048, n_p), replace=False))
+    t1 = time.perf_counter()
+    O.hv_rows(model, reps, lid, v, rows, threads)
+    per_row = (time.perf_counter() - t1) / len(rows)
+    n_rows = int(min(n_p, max(256, args.ref_step_seconds / per_row)))
+    for _ in range(args.warmup):
+        r = np.sort(rng.choice(n_p, size=min(256, n_p), replace=False))
+        O.hv_rows(model, reps, lid, v, r, threads)
+    times = []
+    for _ in range(args.steps):
+        r = np.sort(rng.choice(n_p, size=n_rows, replace=False))
+        t = time.perf_counter()
+        O.hv_rows(model, reps, lid, v, r, threads)
+        times.append(time.perf_counter() - t)
+    sec_per_hv = sum(times) / len(times) * n_p / n_rows
+    value = 1.0 / sec_per_hv
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": sec_per_hv * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic", "impl": "reference",
+        "config": {"workload": args.workload, "n_p": n_p, "basis_seconds": round(t_basis, 2)},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{n_rows} random rows per step of the {n_p}-row sector, scaled to one H*v; "
+                                   "orbit walk + binary search per target (the reference's per-configuration "
+                                   "tables need ~400 GB at N=36)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def run_device(args, world, rank, local_rank):
+    import ctypes as C
+
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    from ed_code_gb300 import _native as N
+    from ed_code_gb300.sector import GpuSector, fill_random
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    model = build_model(args.workload)
+    t0 = time.perf_counter()
+    sec = GpuSector(model)
+    torch.cuda.synchronize()
+    t_basis = time.perf_counter() - t0
+    nnz = sec.count_offdiag()
+    fp64 = args.dtype == "c128"
+    ctype = torch.complex128 if fp64 else torch.complex64
+    elem = 16 if fp64 else 8
+    B = sec.algorithmic_bytes(elem, nnz)
+    v = torch.empty(sec.n_p, dtype=ctype, device=dev)
+    w = torch.empty_like(v)
+    stream = torch.cuda.Stream(device=dev)
+    with torch.cuda.stream(stream):
+        fill_random(v, 4, stream)
+        for _ in range(args.warmup):
+            sec.hv(v, w, stream)
+    stream.synchronize()
+
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    time.sleep(0.3)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        for _ in range(args.steps):
+            sec.hv(v, w, stream)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1)
+    t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = world * args.steps / (ms_max / 1e3)
+    ms_step = ms_max / args.steps
+
+    # e2e through the C ABI host-buffer call: pinned v in, w out, every step
+    e2e = None
+    if not args.no_e2e:
+        hv_in = torch.empty(sec.n_p, dtype=ctype, pin_memory=True)
+        hv_in.copy_(v.cpu())
+        hv_out = torch.empty(sec.n_p, dtype=ctype, pin_memory=True)
+        code = N.EDG_C128 if fp64 else N.EDG_C64
+        lib = N.lib()
+        N.check(lib.edg_hv_host(sec._h, C.c_void_p(hv_in.data_ptr()), C.c_void_p(hv_out.data_ptr()), code))
+        if world > 1:
+            dist.barrier()
+        te = time.perf_counter()
+        for _ in range(args.steps):
+            N.check(lib.edg_hv_host(sec._h, C.c_void_p(hv_in.data_ptr()), C.c_void_p(hv_out.data_ptr()), code))
+        dt = time.perf_counter() - te
+        tt = torch.tensor([dt], dtype=torch.float64, device=dev)
+        if world > 1:
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e = {"value": world * args.steps / float(tt.item()), "unit": UNIT,
+               "h2d_bytes_per_step": sec.n_p * elem, "d2h_bytes_per_step": sec.n_p * elem}
+        del hv_in, hv_out
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        states, norm, _ = sec.basis()
+        lid = np.rint(model.n_sites / norm.astype(np.float64) ** 2).astype(np.int32)
+        threads = os.cpu_count() or 1
+        rate, n_rows, dt = cpu_sample_rate(model, states, lid, args.cpu_seconds, threads)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{n_rows} random rows of the {sec.n_p}-row sector in {dt:.1f} s, scaled to one H*v "
+                         "(oracle row formula in FP64: orbit walk + binary search per target)"}
+
+    peak, peak_kind = measured_peak_hbm()
+    achieved = B / (ms_step / 1e3) / 1e9
+    traffic = profile_traffic(f"hv_{args.workload}_{args.dtype}")
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if fp64 else "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "n_p": sec.n_p, "nnz_off": nnz, "vector": args.dtype,
+                   "algorithmic_bytes_per_hv": B, "basis_seconds": round(t_basis, 3),
+                   "l2": "inputs larger than L2 (no flush needed)", "orbit_search": "torus" if sec.info["torus"] else "walk"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "traffic": traffic},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "clocks": clocks,
+        "gpu_launches": args.steps,
+    }
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="tri6x6_k00")
+    ap.add_argument("--dtype", choices=["c64", "c128"], default="c64")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--ref-step-seconds", type=float, default=4.0)
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, world, rank)
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    try:
+        return run_device(args, world, rank, local_rank)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -218,10 +218,26 @@ __global__ void __launch_bounds__(kBuildThreads) k_walk_tables(SectorView V, int
        i += (int64_t)gridDim.x * blockDim.x) {
     uint64_t t = unrank_config((uint64_t)i, P.n_sites, P.n_ones, V.binom);
     Orbit o = orbit_walk(t, P, T.p1, T.p2, V.n_chunks);
-    int64_t lin = lin_index(o.rep, P.half, P.right_mask, V.Ia, V.Ib);
-    RankRec rec = V.recs[lin / kRecBits];
-    rep_loc[i] = rank_lookup(lin, rec);
+    int bit;
+    const uint32_t q = vrec_of(o.rep, &bit);
+    rep_loc[i] = (int64_t)q < P.n_vrecs ? rank_lookup_bit(bit, V.vrecs[q]) : -1;
     gidx[i] = o.g;
+  }
+}
+
+// Value-indexed rank records: set the bit of every representative, then
+// count per record (the scan kernels turn counts into bases).
+__global__ void k_vrank_mark(const uint64_t* __restrict__ reps, int64_t n_p, RankRec* __restrict__ vrecs) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_p; i += (int64_t)gridDim.x * blockDim.x) {
+    int bit;
+    const uint32_t q = vrec_of(reps[i], &bit);
+    atomicOr(&vrecs[q].bits[bit >> 5], 1u << (bit & 31));
+  }
+}
+__global__ void k_vrank_count(const RankRec* __restrict__ vrecs, int64_t n, uint32_t* __restrict__ counts) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const RankRec r = vrecs[i];
+    counts[i] = (uint32_t)(__popc(r.bits[0]) + __popc(r.bits[1]) + __popc(r.bits[2]));
   }
 }
 
@@ -299,10 +315,50 @@ cudaError_t build_basis(Sector& S, std::string& err) {
     }
   }
   e = cudaStreamSynchronize(st);
+  // The Lin-indexed records are not needed past this point.
+  cudaFree(S.recs);
+  S.device_bytes -= sizeof(RankRec) * std::max<int64_t>(1, n_recs);
+  S.recs = nullptr;
+  S.V.recs = nullptr;
+  if (e == cudaSuccess && n_p > 0) {
+    uint64_t max_rep = 0;
+    e = cudaMemcpy(&max_rep, S.reps + (n_p - 1), sizeof(uint64_t), cudaMemcpyDeviceToHost);
+    const int64_t nv = (int64_t)(max_rep / kRecBits) + 1;
+    const int64_t nv_chunks = (nv + kScanChunk - 1) / kScanChunk;
+    S.P.n_vrecs = nv;
+    uint32_t* vcounts = nullptr;
+    uint32_t* vchunk = nullptr;
+    if (e == cudaSuccess) e = cudaMalloc(&S.vrecs, sizeof(RankRec) * nv);
+    if (e == cudaSuccess) e = cudaMalloc(&vcounts, sizeof(uint32_t) * nv);
+    if (e == cudaSuccess) e = cudaMalloc(&vchunk, sizeof(uint32_t) * nv_chunks);
+    if (e == cudaSuccess) {
+      S.device_bytes += sizeof(RankRec) * nv;
+      cudaMemsetAsync(S.vrecs, 0, sizeof(RankRec) * nv, st);
+      const int blocks = (int)std::min<int64_t>((n_p + 255) / 256, 152 * 64);
+      k_vrank_mark<<<blocks, 256, 0, st>>>(S.reps, (int64_t)n_p, S.vrecs);
+      const int cblocks = (int)std::min<int64_t>((nv + 255) / 256, 152 * 64);
+      k_vrank_count<<<cblocks, 256, 0, st>>>(S.vrecs, nv, vcounts);
+      k_scan_chunks<<<(unsigned)nv_chunks, kScanThreads, 0, st>>>(vcounts, nv, vchunk);
+      k_scan_sums<<<1, kScanThreads, 0, st>>>(vchunk, nv_chunks, total);
+      k_scan_apply<<<(unsigned)nv_chunks, kScanThreads, 0, st>>>(vcounts, nv, vchunk, S.vrecs);
+      unsigned long long check = 0;
+      e = cudaMemcpyAsync(&check, total, sizeof(check), cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      if (e == cudaSuccess && check != n_p) {
+        err = "basis build: value rank records disagree with the representative count";
+        e = cudaErrorUnknown;
+      }
+    } else if (err.empty()) {
+      err = "basis build: value rank records: out of device memory";
+    }
+    cudaFree(vcounts);
+    cudaFree(vchunk);
+    S.V.vrecs = S.vrecs;
+  }
   cudaFree(counts);
   cudaFree(chunk);
   cudaFree(total);
-  if (e != cudaSuccess) err = std::string("basis build: ") + cudaGetErrorString(e);
+  if (e != cudaSuccess && err.empty()) err = std::string("basis build: ") + cudaGetErrorString(e);
   return e;
 }
 

@@ -33,8 +33,9 @@ int cuda_fail(cudaError_t e, const char* what) {
 constexpr double kPi = 3.14159265358979323846;
 
 static void free_sector(Sector& S) {
-  void* ptrs[] = {S.dP, S.reps, S.lid, S.recs, S.Ia, S.Ib, S.groups, S.ch, S.bows, S.nk, S.rots, S.perms, S.binom,
-                  S.host_in.ptr, S.host_out.ptr, S.lz_work.ptr};
+  void* ptrs[] = {S.dP,   S.reps,    S.lid,         S.recs,         S.vrecs,       S.Ia,    S.Ib,
+                  S.groups, S.ch,   S.bows,    S.nk,          S.rots,         S.perms,       S.binom, S.host_in.ptr,
+                  S.host_out.ptr, S.lz_work.ptr, S.tplan, S.tgroups};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (S.stream) cudaStreamDestroy(S.stream);
@@ -229,7 +230,7 @@ static int create_sector(const edg_model* m, int n_ones, int kx, int ky, Sector&
   P.use_chch = (std::abs(m->ChCh) > 1e-16 && m->n_bowties > 0) ? 1 : 0;
   std::vector<Bowtie> bows;
   if (P.use_chch) {
-    if (m->n_bowties > kMaxBowties) return fail(EDG_ERR_UNSUPPORTED, "more than 4096 bowties");
+    if (m->n_bowties > kMaxBowties) return fail(EDG_ERR_UNSUPPORTED, "more than 65536 bowties");
     for (int k = 0; k < m->n_bowties; ++k) {
       const edg_bowtie& b = m->bowties[k];
       const int v[6] = {b.x, b.y, b.z, b.p, b.q, b.r};
@@ -239,6 +240,72 @@ static int create_sector(const edg_model* m, int n_ones, int kx, int ky, Sector&
     }
   }
   P.n_bowties = (int)bows.size();
+
+  // Torus plan: pairs filed by displacement class (see TorusPlan).
+  std::vector<TorusGroup> tgroups;
+  TorusPlan tplan;
+  std::memset(&tplan, 0, sizeof tplan);
+  bool torus_fast = P.torus && L1 <= 8 && L2 <= 8 && !P.use_chch && !groups.empty();
+  for (size_t g = 0; torus_fast && g < groups.size(); ++g)
+    if (group_ch[g].size() > 2) torus_fast = false;
+  if (torus_fast) {
+    const int Lx = L1, Ly = L2;
+    std::memset(tplan.gid, 0xFF, sizeof tplan.gid);
+    std::vector<std::pair<int, int>> cls;  // displacement (dx, dy) of each class
+    for (size_t g = 0; torus_fast && g < groups.size(); ++g) {
+      const int a = groups[g].a, b = groups[g].b;
+      const int dx = ((b % Lx) - (a % Lx) + Lx) % Lx, dy = ((b / Lx) - (a / Lx) + Ly) % Ly;
+      const int nx = (Lx - dx) % Lx, ny = (Ly - dy) % Ly;
+      int c = -1, site = a;
+      for (size_t k = 0; k < cls.size(); ++k) {
+        if (cls[k] == std::make_pair(dx, dy)) { c = (int)k; site = a; break; }
+        if (cls[k] == std::make_pair(nx, ny)) { c = (int)k; site = b; break; }
+      }
+      if (c < 0) {
+        if ((int)cls.size() == kMaxClasses) { torus_fast = false; break; }
+        cls.push_back({dx, dy});
+        c = (int)cls.size() - 1;
+        site = a;
+      }
+      if (tplan.gid[c][site] != 0xFFFF) { torus_fast = false; break; }
+      tplan.gid[c][site] = (uint16_t)g;
+      tplan.cls[c].classmask |= 1ull << site;
+    }
+    if (torus_fast) {
+      tplan.n_classes = (int)cls.size();
+      for (size_t k = 0; k < cls.size(); ++k) {
+        tplan.cls[k].rot_a = (Lx - cls[k].first) % Lx;   // T_{-d}: bit x+d lands on x
+        tplan.cls[k].rot_b = (Ly - cls[k].second) % Ly;
+      }
+      for (size_t g = 0; g < groups.size(); ++g) {
+        TorusGroup tg;
+        std::memset(&tg, 0, sizeof tg);
+        const TermGroup& gr = groups[g];
+        tg.mask = gr.mask;
+        tg.fac = gr.fac;
+        for (int cs = 0; cs < 2; ++cs) {
+          tg.B[2 * cs] = gr.Bre[cs];
+          tg.B[2 * cs + 1] = gr.Bim[cs];
+        }
+        const std::vector<ChTerm>& cv = group_ch[g];
+        if (cv.size() > 0) {
+          tg.z1 = (uint8_t)cv[0].z;
+          for (int cs = 0; cs < 2; ++cs) { tg.A1[2 * cs] = cv[0].Are[cs]; tg.A1[2 * cs + 1] = cv[0].Aim[cs]; }
+        }
+        if (cv.size() > 1) {
+          tg.z2 = (uint8_t)cv[1].z;
+          for (int cs = 0; cs < 2; ++cs) { tg.A2[2 * cs] = cv[1].Are[cs]; tg.A2[2 * cs + 1] = cv[1].Aim[cs]; }
+        }
+        tg.a = (uint8_t)gr.a;
+        tg.ya = (uint8_t)(gr.a / Lx);
+        tg.yb = (uint8_t)(gr.b / Lx);
+        tg.da = (uint8_t)(1u << (gr.a % Lx));
+        tg.db = (uint8_t)(1u << (gr.b % Lx));
+        tg.same_row = tg.ya == tg.yb;
+        tgroups.push_back(tg);
+      }
+    }
+  }
 
   // Lin tables (Lin_Tables.cpp:57-78; Ib as Momentum_Basis.cpp:731-737):
   // Ia = 1-based rank among half-words of equal popcount; Ib[l] = Lin index
@@ -315,6 +382,11 @@ static int create_sector(const edg_model* m, int n_ones, int kx, int ky, Sector&
   if ((e = upload(&S.rots, rots.data(), rots.size(), bytes)) != cudaSuccess) return cuda_fail(e, "rots");
   if ((e = upload(&S.perms, perms.data(), perms.size(), bytes)) != cudaSuccess) return cuda_fail(e, "perms");
   if ((e = upload(&S.binom, binom.data(), binom.size(), bytes)) != cudaSuccess) return cuda_fail(e, "binom");
+  if (torus_fast) {
+    if ((e = upload(&S.tplan, &tplan, 1, bytes)) != cudaSuccess) return cuda_fail(e, "torus plan");
+    if ((e = upload(&S.tgroups, tgroups.data(), tgroups.size(), bytes)) != cudaSuccess)
+      return cuda_fail(e, "torus groups");
+  }
   e = cudaMalloc(&S.recs, sizeof(RankRec) * std::max<int64_t>(1, P.n_recs));
   if (e != cudaSuccess) return fail(EDG_ERR_NOMEM, "rank records: out of device memory");
   bytes += sizeof(RankRec) * std::max<int64_t>(1, P.n_recs);
@@ -492,8 +564,7 @@ int edg_hv(edg_sector* s, const void* v, void* w, int dtype, void* stream) {
   if (!s || !v || !w) return fail(EDG_ERR_INVALID, "NULL argument");
   if (dtype != EDG_C128 && dtype != EDG_C64) return fail(EDG_ERR_INVALID, "dtype must be EDG_C128 or EDG_C64");
   if (v == w) return fail(EDG_ERR_INVALID, "v and w must not alias");
-  cudaStream_t st = stream ? (cudaStream_t)stream : s->s.stream;
-  cudaError_t e = launch_hv(s->s, v, w, dtype == EDG_C128, st);
+  cudaError_t e = launch_hv(s->s, v, w, dtype == EDG_C128, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "hv launch");
   return EDG_OK;
 }

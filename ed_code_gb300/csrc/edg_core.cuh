@@ -11,10 +11,12 @@
 //   reps[n_p]      u64   representatives in increasing order (pblock_states)
 //   lid[n_p]       u8    stabiliser count of each representative; the norms
 //                        sqrt(L1*L2/lid) come from a 65-entry table
-//   rank[n_rec]    16 B  {u32 base, u32 bits[3]}: one record per 96 consecutive
-//                        Lin indices; bit set <=> that configuration is an
+//   vrecs[n_vrec]  16 B  {u32 base, u32 bits[3]}: one record per 96 consecutive
+//                        values 0..max_rep; bit set <=> that value is an
 //                        allowed representative; base = allowed ones before it.
 //                        j(rep) = base + popcount of the bits below it.
+//                        (While the basis is built the same records are indexed
+//                        by Lin index over the C(N, n_up) configurations.)
 //   Ia[2^h], Ib[2^h]     Lin tables (Ia as u32, Ib as i64), Lin = Ia[r] + Ib[l] - 1
 //
 // The representative of a flipped state is found on the fly, so no per-
@@ -34,7 +36,7 @@ namespace edg {
 constexpr int kMaxSites = 40;      // Lin tables hold 2^(N/2) entries
 constexpr int kMaxGroups = 512;    // distinct flipped pairs
 constexpr int kMaxChTerms = 1024;  // chirality terms
-constexpr int kMaxBowties = 4096;
+constexpr int kMaxBowties = 65536;
 constexpr int kRecBits = 96;       // Lin indices per rank record
 constexpr int kMaxTorusRow = 10;   // row-rotation search tables hold 2^Lx entries
 
@@ -96,7 +98,8 @@ struct SectorParams {
   int n_groups, n_ch, n_bowties;
   int use_ch, use_chch;
   int pad0;
-  int64_t n_p, n_configs, n_recs;
+  int64_t n_p, n_configs, n_recs;   // n_recs: Lin-indexed records used while building
+  int64_t n_vrecs;                  // value-indexed rank records (see value_rank)
   uint64_t full_mask, right_mask;
   double total_fac;                 // sum over bonds of 0.25*lambda*J
   double ChCh;
@@ -114,6 +117,31 @@ struct SectorParams {
   int pad1;
 };
 
+// Torus plan: flip groups filed by displacement class.  Class c holds the
+// pairs (x, x+d_c); a state's anti-aligned pairs of class c are the set bits of
+// (s XOR T_{-d_c}(s)) & classmask, one 64-bit operation per class instead of
+// one test per pair.  Built only for row-major tori with Lx, Ly <= 8, at most
+// two chirality terms per pair and no ChCh terms.
+constexpr int kMaxClasses = 16;
+struct TorusClass {
+  uint64_t classmask;
+  int rot_a, rot_b;  // T_{-d}: rotate rows by rot_b, then within rows by rot_a
+};
+struct TorusGroup {
+  uint64_t mask;
+  double fac;
+  double B[4];   // bond coefficient: re/im for bit a of s = 0, then = 1
+  double A1[4];  // first chirality term (sign from bit z1 of s), same layout
+  double A2[4];  // second chirality term (bit z2)
+  uint8_t a, z1, z2, ya, yb, da, db, same_row;  // rows of the two sites and their bit in the row
+};
+struct TorusPlan {
+  int n_classes;
+  int pad[3];
+  TorusClass cls[kMaxClasses];
+  uint16_t gid[kMaxClasses][64];  // group of (class, site x), 0xFFFF when none
+};
+
 // --------------------------------------------------------------------------
 // Lin index and representative position
 // --------------------------------------------------------------------------
@@ -121,8 +149,36 @@ EDG_HD int64_t lin_index(uint64_t s, int half, uint64_t right_mask, const uint32
   return (int64_t)Ia[s & right_mask] + Ib[s >> half] - 1;
 }
 
+// Record holding Lin index `lin` and the bit inside it.  lin < 2^37 for
+// N <= 40, so lin/96 = (lin>>5)/3 runs in 32-bit arithmetic.
+EDG_HD uint32_t rec_of(int64_t lin, int* bit) {
+  const uint32_t q = (uint32_t)((uint64_t)lin >> 5) / 3u;
+  *bit = (int)(lin - (int64_t)q * kRecBits);
+  return q;
+}
+
 // Position of representative `rep` among the allowed representatives, -1 if
 // it is not one (the reference's rep_loc[...] < 0 case).
+EDG_HD int64_t rank_lookup_bit(int bit, const RankRec& rec) {
+  int w = bit >> 5, o = bit & 31;
+  uint32_t word = rec.bits[w];
+  if (!((word >> o) & 1u)) return -1;
+  int below = popc32(word & ((1u << o) - 1u));
+  if (w > 0) below += popc32(rec.bits[0]);
+  if (w > 1) below += popc32(rec.bits[1]);
+  return (int64_t)rec.base + below;
+}
+// Position of representative `rep` by its value: records cover the values
+// 0..max_rep in blocks of 96 (representatives are orbit minima, so max_rep is
+// far below 2^N and the table is about as small as a Lin-indexed one), and
+// the lookup needs no Lin index.  -1 when rep is not an allowed state.
+EDG_HD uint32_t vrec_of(uint64_t rep, int* bit) {
+  uint64_t q;
+  if ((rep >> 37) == 0) q = (uint32_t)(rep >> 5) / 3u;  // 32-bit division for rep < 2^37
+  else q = (rep >> 5) / 3u;
+  *bit = (int)(rep - q * kRecBits);
+  return (uint32_t)q;
+}
 EDG_HD int64_t rank_lookup(int64_t lin, const RankRec& rec) {
   int bit = (int)(lin % kRecBits);
   int w = bit >> 5, o = bit & 31;

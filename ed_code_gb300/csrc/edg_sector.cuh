@@ -16,7 +16,8 @@ struct SectorView {
   const SectorParams* params;
   const uint64_t* reps;
   const uint8_t* lid;
-  RankRec* recs;
+  RankRec* recs;         // Lin-indexed records, only while the basis is built
+  const RankRec* vrecs;  // value-indexed rank records
   const uint32_t* Ia;
   const int64_t* Ib;
   const TermGroup* groups;
@@ -38,6 +39,7 @@ struct SmemGroup {
   Real Bre[2], Bim[2];
   int16_t a;
   int16_t ch_begin, ch_end;
+  int8_t ya, yb;  // torus rows of the two flipped sites
 };
 template <typename Real>
 struct SmemCh {
@@ -59,6 +61,7 @@ struct Sector {
   uint64_t* reps = nullptr;
   uint8_t* lid = nullptr;
   RankRec* recs = nullptr;
+  RankRec* vrecs = nullptr;
   uint32_t* Ia = nullptr;
   int64_t* Ib = nullptr;
   TermGroup* groups = nullptr;
@@ -77,6 +80,9 @@ struct Sector {
   cudaStream_t stream = nullptr;
   // Lanczos work area (allocated on first use)
   DeviceBuffer lz_work;
+  // torus plan (null when the sector does not qualify)
+  TorusPlan* tplan = nullptr;
+  TorusGroup* tgroups = nullptr;
 };
 
 // basis.cu
@@ -84,6 +90,9 @@ cudaError_t build_basis(Sector& S, std::string& err);
 cudaError_t export_walk_tables(const Sector& S, int64_t* rep_loc_dev, int32_t* g_dev, cudaStream_t st);
 // hv.cu
 cudaError_t launch_hv(const Sector& S, const void* v, void* w, bool fp64, cudaStream_t st);
+cudaError_t launch_hv_generic(const Sector& S, const void* v, void* w, bool fp64, cudaStream_t st);
+// hv_torus.cu
+cudaError_t launch_hv_torus(const Sector& S, const void* v, void* w, bool fp64, cudaStream_t st);
 cudaError_t count_offdiag(const Sector& S, unsigned long long* nnz_dev, cudaStream_t st);
 int hv_grid_blocks(bool fp64, bool torus, bool chch);
 

@@ -6,8 +6,8 @@
 //     (groups merge every bond and chirality term that flips the same pair);
 //   * each one is flipped with one XOR, its representative and translation
 //     come from the orbit search (row-rotation candidates on row-major tori,
-//     the reference's walk otherwise), its position j from the Lin index and
-//     the rank records, its phase and norm ratio from shared-memory tables;
+//     the reference's walk otherwise), its position j from the value-indexed
+//     rank records, its phase and norm ratio from shared-memory tables;
 //   * w_i = sum_targets c(s)*phase*norm_i/norm_j*v_j + Ezz(s)*v_i, with
 //     Ezz(s) = sum_bonds lambda*J/4 - 2*sum_{anti-aligned} lambda*J/4.
 // ChCh bowtie terms (H_v.cpp:305-353) run as a separate per-row loop, only
@@ -87,6 +87,8 @@ __device__ HvSmem<Real> stage_hv(const SectorView& V, const SectorParams& P, uin
     d.a = (int16_t)src.a;
     d.ch_begin = (int16_t)src.ch_begin;
     d.ch_end = (int16_t)src.ch_end;
+    d.ya = (int8_t)(kTorus ? src.a / P.L1 : -1);
+    d.yb = (int8_t)(kTorus ? src.b / P.L1 : -1);
     H.groups[g] = d;
   }
   for (int m = threadIdx.x; m < P.n_ch; m += blockDim.x) {
@@ -133,29 +135,58 @@ __device__ __forceinline__ Orbit search(uint64_t t, const SectorParams& P, const
   return orbit_walk(t, P, H.p1, H.p2, n_chunks);
 }
 
-// Position of rep(t) and the data its term needs; j < 0 when the
-// representative is not an allowed state.
-template <typename Real, bool kTorus>
-__device__ __forceinline__ int64_t locate(uint64_t t, const SectorView& V, const SectorParams& P,
-                                          const HvSmem<Real>& H, Orbit& o) {
-  o = search<Real, kTorus>(t, P, H, V.n_chunks);
+// Position j of the representative o.rep; j < 0 when it is not an allowed
+// state (the reference's rep_loc < 0).
+__device__ __forceinline__ int64_t position(const Orbit& o, const SectorView& V, const SectorParams& P) {
   // A translate of t is an n_sites-bit word; anything else means the search
   // found no candidate, and is treated as "no allowed representative" rather
   // than used as a table index.
   if (o.rep & ~P.full_mask) return -1;
   if ((unsigned)o.g >= 64u || (unsigned)o.stab > 64u) return -1;
-  const int64_t lin = (int64_t)__ldg(V.Ia + (o.rep & P.right_mask)) + __ldg(V.Ib + (o.rep >> P.half)) - 1;
-  const uint4 raw = __ldg(reinterpret_cast<const uint4*>(V.recs) + lin / kRecBits);
+  int bit;
+  const uint32_t q = vrec_of(o.rep, &bit);
+  if ((int64_t)q >= P.n_vrecs) return -1;  // larger than every representative
+  const uint4 raw = __ldg(reinterpret_cast<const uint4*>(V.vrecs) + q);
   RankRec rec;
   rec.base = raw.x;
   rec.bits[0] = raw.y;
   rec.bits[1] = raw.z;
   rec.bits[2] = raw.w;
-  return rank_lookup(lin, rec);
+  return rank_lookup_bit(bit, rec);
+}
+
+template <typename Real, bool kTorus>
+__device__ __forceinline__ int64_t locate(uint64_t t, const SectorView& V, const SectorParams& P,
+                                          const HvSmem<Real>& H, Orbit& o) {
+  o = search<Real, kTorus>(t, P, H, V.n_chunks);
+  return position(o, V, P);
+}
+
+// Row-level facts for the torus fast path.  s is a representative, so its top
+// row is at its rotation minimum and no row has a smaller one.  When the top
+// row is the only row reaching that minimum and it is aperiodic, the identity
+// is the only candidate translation of s -- and of every flip of s that leaves
+// the top row alone and gives no other row a rotation minimum <= mstar.  Such
+// a flipped state is its own representative with stabiliser 1.
+struct RowInfo {
+  int mstar;
+  bool uniq;
+};
+template <typename Real>
+__device__ __forceinline__ RowInfo torus_row_info(uint64_t s, const SectorParams& P, const HvSmem<Real>& H) {
+  const int Lx = P.L1, Ly = P.L2;
+  const uint64_t rmask = (1ull << Lx) - 1ull;
+  const int rtop = (int)((s >> (Lx * (Ly - 1))) & rmask);
+  RowInfo r;
+  r.mstar = H.nk[rtop];
+  int cnt = 0;
+  for (int y = 0; y < Ly; ++y) cnt += (H.nk[(int)((s >> (Lx * y)) & rmask)] == r.mstar);
+  r.uniq = (cnt == 1) && (H.rots[rtop] == 1u);
+  return r;
 }
 
 template <typename Real, bool kTorus, bool kChCh>
-__global__ void __launch_bounds__(kHvThreads) k_hv(SectorView V, const typename C2<Real>::T* __restrict__ v,
+__global__ void __launch_bounds__(kHvThreads, 4) k_hv(SectorView V, const typename C2<Real>::T* __restrict__ v,
                                                    typename C2<Real>::T* __restrict__ w) {
   using CT = typename C2<Real>::T;
   __shared__ SectorParams P;
@@ -176,6 +207,10 @@ __global__ void __launch_bounds__(kHvThreads) k_hv(SectorView V, const typename 
     const CT vi = v[i];
     const Real norm_i = H.nrm[li];
     Real accr = 0, acci = 0, anti = 0;
+    RowInfo ri{0, false};
+    if (kTorus) ri = torus_row_info(s, P, H);
+    const int top = P.L2 - 1;
+    const uint64_t rmask = (1ull << P.L1) - 1ull;
     for (int g0 = 0; g0 < ng; g0 += 64) {
       const int gn = min(64, ng - g0);
       uint64_t am = 0;
@@ -198,8 +233,21 @@ __global__ void __launch_bounds__(kHvThreads) k_hv(SectorView V, const typename 
             ci += sg * c.Aim[cs];
           }
         }
+        const uint64_t t = s ^ gr.mask;
         Orbit o;
-        const int64_t j = locate<Real, kTorus>(s ^ gr.mask, V, P, H, o);
+        bool fast = false;
+        if (kTorus && ri.uniq && gr.ya != top && gr.yb != top) {
+          const int na = H.nk[(int)((t >> (P.L1 * gr.ya)) & rmask)];
+          const int nb = H.nk[(int)((t >> (P.L1 * gr.yb)) & rmask)];
+          if (na > ri.mstar && nb > ri.mstar) {
+            o.rep = t;
+            o.g = 0;
+            o.stab = 1;
+            fast = true;
+          }
+        }
+        if (!fast) o = search<Real, kTorus>(t, P, H, V.n_chunks);
+        const int64_t j = position(o, V, P);
         if (j >= 0) {
           const Real sc = norm_i * H.nrm_inv[o.stab];
           const Real pr = H.ph_re[o.g], pi = H.ph_im[o.g];
@@ -295,6 +343,11 @@ cudaError_t launch_t(const Sector& S, const void* v, void* w, cudaStream_t st) {
 }  // namespace
 
 cudaError_t launch_hv(const Sector& S, const void* v, void* w, bool fp64, cudaStream_t st) {
+  if (S.tplan) return launch_hv_torus(S, v, w, fp64, st);
+  return launch_hv_generic(S, v, w, fp64, st);
+}
+
+cudaError_t launch_hv_generic(const Sector& S, const void* v, void* w, bool fp64, cudaStream_t st) {
   const bool torus = S.P.torus != 0, chch = S.P.use_chch != 0;
   if (fp64) {
     if (torus) return chch ? launch_t<double, true, true>(S, v, w, st) : launch_t<double, true, false>(S, v, w, st);

@@ -94,7 +94,8 @@ int edg_sector_copy_config_tables(const edg_sector* s, int64_t max_configs, int6
                                   int32_t* lxly);
 
 /* w = H v on device pointers (n_p complex entries each, dtype EDG_C128 or
- * EDG_C64), enqueued on `stream` (a cudaStream_t, NULL = the sector's stream).
+ * EDG_C64), enqueued on `stream` (a cudaStream_t; NULL is the legacy default
+ * stream).  v and w must not overlap.
  * Replaces: sHv (H_v.cpp:192-357, declared H_v.h:36-57). */
 int edg_hv(edg_sector* s, const void* v, void* w, int dtype, void* stream);
 

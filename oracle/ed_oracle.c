@@ -398,3 +398,78 @@ int64_t or_sector_dim(int n_sites, int n_ones, const int *T1, const int *T2, int
   }
   return (int64_t)llroundl(total / (L1 * L2));
 }
+
+/* Unrank Lin index r (increasing-integer order of n_sites-bit words with
+ * n_ones bits) into the word. */
+static int64_t unrank_lin(int64_t r, int n_sites, int n_ones) {
+  int64_t t = 0;
+  int c = n_ones;
+  for (int p = n_sites - 1; p >= 0 && c > 0; --p) {
+    int64_t below = or_n_choose_k(p, c);
+    if (r >= below) { t |= (int64_t)1 << p; r -= below; --c; }
+  }
+  return t;
+}
+
+/* Any translate smaller than t?  (Early exit; order irrelevant.) */
+static int smaller_translate(int64_t t, const int *T1, const int *T2, int n, int L1, int L2) {
+  uint64_t row = (uint64_t)t;
+  for (int x = 0; x < L1; ++x) {
+    uint64_t tmp = row;
+    for (int y = 1; y < L2; ++y) {
+      tmp = or_translate(tmp, T2, n);
+      if ((int64_t)tmp < t) return 1;
+    }
+    row = or_translate(row, T1, n);
+    if (x + 1 < L1 && (int64_t)row < t) return 1;
+  }
+  return 0;
+}
+
+int64_t or_build_reps(int n_sites, int n_ones, const int *T1, const int *T2, int kx, int ky, int64_t **reps_out,
+                      int32_t **lid_out, int n_threads) {
+  int L1, L2;
+  or_LxLy(T1, T2, n_sites, &L1, &L2);
+  const double px = 2 * kx * OR_PI / L1, py = 2 * ky * OR_PI / L2;
+  const int64_t nc = or_n_choose_k(n_sites, n_ones);
+  const int64_t chunk = 1 << 16;
+  const int64_t nchunks = (nc + chunk - 1) / chunk;
+  int64_t *cnt = (int64_t *)calloc((size_t)nchunks + 1, sizeof(int64_t));
+#ifdef _OPENMP
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+#else
+  (void)n_threads;
+#endif
+  for (int pass = 0; pass < 2; ++pass) {
+    if (pass == 1) {
+      int64_t run = 0;
+      for (int64_t c = 0; c < nchunks; ++c) { int64_t k = cnt[c]; cnt[c] = run; run += k; }
+      cnt[nchunks] = run;
+      *reps_out = (int64_t *)malloc(sizeof(int64_t) * (run ? run : 1));
+      *lid_out = (int32_t *)malloc(sizeof(int32_t) * (run ? run : 1));
+    }
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t c = 0; c < nchunks; ++c) {
+      int64_t i0 = c * chunk, i1 = i0 + chunk < nc ? i0 + chunk : nc;
+      int64_t t = unrank_lin(i0, n_sites, n_ones);
+      int64_t k = pass ? cnt[c] : 0;
+      for (int64_t i = i0; i < i1; ++i) {
+        if (!smaller_translate(t, T1, T2, n_sites, L1, L2)) {
+          int lx, ly, lid, pid;
+          int64_t rep = or_representative(t, T1, T2, n_sites, L1, L2, px, py, &lx, &ly, &lid, &pid);
+          if (rep == t && pid) {
+            if (pass) { (*reps_out)[k] = t; (*lid_out)[k] = lid; }
+            ++k;
+          }
+        }
+        if (i + 1 < i1) t = next_same_popcount(t);
+      }
+      if (!pass) cnt[c] = k;
+    }
+  }
+  int64_t n = cnt[nchunks];
+  free(cnt);
+  return n;
+}
+
+void or_free(void *p) { free(p); }

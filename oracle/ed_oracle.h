@@ -61,6 +61,14 @@ void or_hv_rows(int n_sites, const int *T1, const int *T2, int kx, int ky, const
                 const or_bond *bonds, int nb, double Ch, const or_tri *tris, int nt, double ChCh,
                 const or_bowtie *bows, int nbw, int n_threads);
 
+/* Allowed representatives in increasing order with their stabiliser counts,
+ * without the per-configuration tables: the enumeration and acceptance rule of
+ * pConstruct_States (Momentum_Basis.cpp:724-770), run in parallel over chunks of
+ * the Lin order.  *reps and *lid are malloc'ed (free with or_free). */
+int64_t or_build_reps(int n_sites, int n_ones, const int *T1, const int *T2, int kx, int ky, int64_t **reps,
+                      int32_t **lid, int n_threads);
+void or_free(void *p);
+
 /* Is `state` an allowed representative (rep == state and p_id)?  Returns lid or 0. */
 int or_allowed_rep(int64_t state, const int *T1, const int *T2, int n_sites, int kx, int ky);
 

@@ -70,6 +70,10 @@ def lib() -> C.CDLL:
         L.or_allowed_rep.restype = C.c_int
         L.or_sector_dim.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int, C.c_int]
         L.or_sector_dim.restype = C.c_int64
+        L.or_build_reps.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int, C.c_int,
+                                    C.POINTER(C.POINTER(C.c_int64)), C.POINTER(C.POINTER(C.c_int32)), C.c_int]
+        L.or_build_reps.restype = C.c_int64
+        L.or_free.argtypes = [C.c_void_p]
         L.or_n_choose_k.argtypes = [C.c_int, C.c_int]
         L.or_n_choose_k.restype = C.c_int64
         _lib = L
@@ -164,6 +168,20 @@ def hv_rows(model, reps: np.ndarray, lid: np.ndarray, v: np.ndarray, rows: np.nd
                      v.ctypes.data, rows.ctypes.data, len(rows), out.ctypes.data, model.Jz, t.bonds, t.nb, model.Ch,
                      t.tris, t.nt, model.ChCh, t.bows, t.nbw, int(n_threads))
     return out
+
+
+def build_reps(model, n_threads: int = 0):
+    """(reps, lid) of the sector by parallel enumeration, without tables."""
+    t = TermLists(model)
+    rp = C.POINTER(C.c_int64)()
+    lp = C.POINTER(C.c_int32)()
+    n = lib().or_build_reps(model.n_sites, model.n_ones, t.T1, t.T2, model.kx, model.ky, C.byref(rp), C.byref(lp),
+                            int(n_threads))
+    reps = np.ctypeslib.as_array(rp, (max(n, 1),))[:n].copy()
+    lid = np.ctypeslib.as_array(lp, (max(n, 1),))[:n].copy()
+    lib().or_free(rp)
+    lib().or_free(lp)
+    return reps, lid
 
 
 def allowed_rep(model, state: int) -> int:
