@@ -57,18 +57,20 @@ class edg_sector_info(C.Structure):
     ]
 
 
-class edg_lanczos_opts(C.Structure):
+LOG_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_char_p)
+
+
+class edg_solver_opts(C.Structure):
     _fields_ = [
         ("n_ev", C.c_int), ("iterations", C.c_int), ("ncycles", C.c_int), ("tol", C.c_double),
-        ("seed", C.c_uint64), ("start_kind", C.c_int), ("want_vectors", C.c_int),
-        ("reorth_every", C.c_int), ("precision", C.c_int), ("verbose", C.c_int),
+        ("seed", C.c_uint64), ("dense_threshold", C.c_int64), ("log_fn", LOG_FN), ("log_ctx", C.c_void_p),
     ]
 
 
-class edg_lanczos_stats(C.Structure):
+class edg_solver_stats(C.Structure):
     _fields_ = [
-        ("hv_calls", C.c_int64), ("iterations_done", C.c_int64), ("hv_seconds", C.c_double),
-        ("ortho_seconds", C.c_double), ("total_seconds", C.c_double),
+        ("path", C.c_int), ("hv_calls", C.c_int64), ("hv_seconds", C.c_double), ("ortho_seconds", C.c_double),
+        ("total_seconds", C.c_double),
     ]
 
 
@@ -86,6 +88,8 @@ SIGNATURES = {
     "edg_hv_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
     "edg_count_offdiag": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
     "edg_fill_random": (C.c_int, [C.c_void_p, C.c_int64, C.c_int, C.c_uint64, C.c_void_p]),
+    "edg_solve_plain": (C.c_int, [C.c_void_p, C.POINTER(edg_solver_opts), C.c_void_p, C.c_int64,
+                                  C.POINTER(C.c_int64), C.c_void_p, C.c_int64, C.POINTER(edg_solver_stats)]),
 }
 
 _lib: Optional[C.CDLL] = None

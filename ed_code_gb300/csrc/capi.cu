@@ -5,6 +5,7 @@
 #include <cmath>
 #include <complex>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <string>
@@ -392,6 +393,7 @@ static int create_sector(const edg_model* m, int n_ones, int kx, int ky, Sector&
   bytes += sizeof(RankRec) * std::max<int64_t>(1, P.n_recs);
   if ((e = upload(&S.dP, &P, 1, bytes)) != cudaSuccess) return cuda_fail(e, "params");
   S.device_bytes = bytes;
+  if (const char* hv = std::getenv("EDG_HV_VARIANT")) S.hv_variant = (std::string(hv) == "torus") ? 1 : 0;
 
   SectorView& V = S.V;
   V.params = S.dP;
@@ -593,6 +595,13 @@ int edg_hv_host(edg_sector* s, const void* v, void* w, int dtype) {
   if (e == cudaSuccess) e = cudaStreamSynchronize(S.stream);
   if (e != cudaSuccess) return cuda_fail(e, "hv_host");
   return EDG_OK;
+}
+
+int edg_solve_plain(edg_sector* s, const edg_solver_opts* opts, double* eigs, int64_t eigs_capacity,
+                    int64_t* n_eigs, double* evecs, int64_t evecs_capacity, edg_solver_stats* stats) {
+  if (!s || !opts || !eigs || !n_eigs) return fail(EDG_ERR_INVALID, "NULL argument");
+  *n_eigs = 0;
+  return solve_plain(s->s, *opts, eigs, eigs_capacity, n_eigs, evecs, evecs_capacity, stats);
 }
 
 int edg_count_offdiag(edg_sector* s, int64_t* nnz_off) {

@@ -7,6 +7,7 @@
 #include <string>
 #include <vector>
 
+#include "../../include/edgpu.h"
 #include "edg_core.cuh"
 
 namespace edg {
@@ -83,6 +84,9 @@ struct Sector {
   // torus plan (null when the sector does not qualify)
   TorusPlan* tplan = nullptr;
   TorusGroup* tgroups = nullptr;
+  // H*v kernel: 0 = hv.cu (default), 1 = hv_torus.cu when the sector has a
+  // torus plan.  Chosen at sector creation from EDG_HV_VARIANT (for A/B timing).
+  int hv_variant = 0;
 };
 
 // basis.cu
@@ -91,6 +95,9 @@ cudaError_t export_walk_tables(const Sector& S, int64_t* rep_loc_dev, int32_t* g
 // hv.cu
 cudaError_t launch_hv(const Sector& S, const void* v, void* w, bool fp64, cudaStream_t st);
 cudaError_t launch_hv_generic(const Sector& S, const void* v, void* w, bool fp64, cudaStream_t st);
+// lanczos.cu
+int solve_plain(Sector& S, const edg_solver_opts& o, double* eigs, int64_t cap, int64_t* n_out, double* evecs,
+                int64_t evecs_cap, edg_solver_stats* stats);
 // hv_torus.cu
 cudaError_t launch_hv_torus(const Sector& S, const void* v, void* w, bool fp64, cudaStream_t st);
 cudaError_t count_offdiag(const Sector& S, unsigned long long* nnz_dev, cudaStream_t st);

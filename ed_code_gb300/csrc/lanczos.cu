@@ -1,0 +1,504 @@
+// Eigensolvers around the GPU H*v.
+//
+// solve_plain(): the reference's sector eigensolver in FP64 on the GPU --
+//   * n_p <= dense_threshold: exact_evecs (lanczos.cpp:81-131): the dense
+//     sector matrix (makeH, H_v.cpp:21-190, here assembled column by column
+//     from H*e_j) diagonalised by a dense Hermitian eigensolver, all
+//     eigenvalues returned;
+//   * otherwise lanczos_evecs (lanczos.cpp:133-349), step for step: one
+//     eigenvalue at a time with deflation against the earlier eigenvectors,
+//     `ncycles` restarts of `iterations` steps, three-term recurrence
+//     (alpha = <v|Hv>, beta = |w|), classical Gram-Schmidt against the
+//     earlier eigenvectors every step and against every stored Krylov vector
+//     in the last cycle, the lowest eigenvalue of T after every step and the
+//     convergence test |E0 - previous| < tol in the middle cycles, the Ritz
+//     vector rebuilt from the stored Krylov vectors at the end of each cycle.
+//   The vectors live in HBM; the scalars (alpha, beta, the T matrix) on the
+//   host, as in the reference.
+#include <cuda_runtime.h>
+#include <dlfcn.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdarg>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/edgpu.h"
+#include "blas1.cuh"
+#include "edg_sector.cuh"
+#include "tridiag.cuh"
+
+namespace edg {
+
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+namespace {
+
+using cplx = std::complex<double>;
+
+// ---------------------------------------------------------------- kernels ---
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) k_dotc_partial(const T* __restrict__ V, int64_t ld,
+                                                              const T* __restrict__ x, int64_t n,
+                                                              double* __restrict__ part) {
+  // part[(k*kRedBlocks + b)*2 + {0,1}] = partial sum of conj(V_k) x, k = blockIdx.y
+  const T* a = V + (int64_t)blockIdx.y * ld;
+  Acc sr, si;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const cd p = VecTraits<T>::load(a, i), q = VecTraits<T>::load(x, i);
+    sr.add(p.re * q.re + p.im * q.im);
+    si.add(p.re * q.im - p.im * q.re);
+  }
+  __shared__ double rr[kRedThreads], ri[kRedThreads];
+  rr[threadIdx.x] = sr.value();
+  ri[threadIdx.x] = si.value();
+  __syncthreads();
+  for (int h = kRedThreads / 2; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) {
+      rr[threadIdx.x] += rr[threadIdx.x + h];
+      ri[threadIdx.x] += ri[threadIdx.x + h];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const int64_t o = ((int64_t)blockIdx.y * gridDim.x + blockIdx.x) * 2;
+    part[o] = rr[0];
+    part[o + 1] = ri[0];
+  }
+}
+
+// One CTA per vector: sum its kRedBlocks partials in a fixed order.
+__global__ void __launch_bounds__(kRedThreads) k_dot_finish(const double* __restrict__ part, int nb,
+                                                            double* __restrict__ out) {
+  const double* p = part + (int64_t)blockIdx.x * nb * 2;
+  __shared__ double rr[kRedThreads], ri[kRedThreads];
+  double a = 0, b = 0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    a += p[2 * i];
+    b += p[2 * i + 1];
+  }
+  rr[threadIdx.x] = a;
+  ri[threadIdx.x] = b;
+  __syncthreads();
+  for (int h = kRedThreads / 2; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) {
+      rr[threadIdx.x] += rr[threadIdx.x + h];
+      ri[threadIdx.x] += ri[threadIdx.x + h];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[2 * blockIdx.x] = rr[0];
+    out[2 * blockIdx.x + 1] = ri[0];
+  }
+}
+
+// y = a*x + b*y  (complex scalars by value)
+template <typename T>
+__global__ void k_axpby(T* __restrict__ y, const T* __restrict__ x, cd a, cd b, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const cd xv = x ? VecTraits<T>::load(x, i) : cd{0, 0};
+    const cd yv = VecTraits<T>::load(y, i);
+    cd r;
+    r.re = a.re * xv.re - a.im * xv.im + b.re * yv.re - b.im * yv.im;
+    r.im = a.re * xv.im + a.im * xv.re + b.re * yv.im + b.im * yv.re;
+    VecTraits<T>::store(y, i, r);
+  }
+}
+
+// y -= sum_k q_k V_k  (q: K complex on device)
+template <typename T>
+__global__ void k_sub_multi(T* __restrict__ y, const T* __restrict__ V, int64_t ld, const double* __restrict__ q,
+                            int K, int64_t n) {
+  extern __shared__ double sq[];
+  for (int k = threadIdx.x; k < 2 * K; k += blockDim.x) sq[k] = q[k];
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    cd yv = VecTraits<T>::load(y, i);
+    for (int k = 0; k < K; ++k) {
+      const cd vv = VecTraits<T>::load(V + (int64_t)k * ld, i);
+      const double qr = sq[2 * k], qi = sq[2 * k + 1];
+      yv.re -= qr * vv.re - qi * vv.im;
+      yv.im -= qr * vv.im + qi * vv.re;
+    }
+    VecTraits<T>::store(y, i, yv);
+  }
+}
+
+// out = sum_k c_k V_k with real coefficients c (device)
+template <typename T>
+__global__ void k_combine(T* __restrict__ out, const T* __restrict__ V, int64_t ld, const double* __restrict__ c,
+                          int K, int64_t n) {
+  extern __shared__ double sc[];
+  for (int k = threadIdx.x; k < K; k += blockDim.x) sc[k] = c[k];
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    cd r{0, 0};
+    for (int k = 0; k < K; ++k) {
+      const cd vv = VecTraits<T>::load(V + (int64_t)k * ld, i);
+      r.re += sc[k] * vv.re;
+      r.im += sc[k] * vv.im;
+    }
+    VecTraits<T>::store(out, i, r);
+  }
+}
+
+__global__ void k_unit(double2* e, int64_t n, int64_t j) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    e[i] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+}
+
+int grid_of(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16)); }
+
+// ------------------------------------------------------------ vector ops ---
+struct Blas {
+  cudaStream_t st;
+  double* part = nullptr;  // partials for up to kMaxDots vectors
+  double* res = nullptr;   // finished dots (device)
+  double* coef = nullptr;  // coefficients for the multi-vector kernels (device)
+  static constexpr int kMaxDots = 1024;
+  cudaError_t init(cudaStream_t s) {
+    st = s;
+    cudaError_t e = cudaMalloc(&part, sizeof(double) * 2 * kRedBlocks * kMaxDots);
+    if (e == cudaSuccess) e = cudaMalloc(&res, sizeof(double) * 2 * kMaxDots);
+    if (e == cudaSuccess) e = cudaMalloc(&coef, sizeof(double) * 2 * kMaxDots);
+    return e;
+  }
+  ~Blas() {
+    cudaFree(part);
+    cudaFree(res);
+    cudaFree(coef);
+  }
+  // out[k] = <V_k | x> = sum conj(V_k) x, k < K
+  template <typename T>
+  cudaError_t dots(const T* V, int64_t ld, int K, const T* x, int64_t n, cplx* out) {
+    std::vector<double> h(2 * K);
+    for (int k0 = 0; k0 < K; k0 += kMaxDots) {
+      const int kk = std::min(kMaxDots, K - k0);
+      k_dotc_partial<T><<<dim3(kRedBlocks, kk), kRedThreads, 0, st>>>(V + (int64_t)k0 * ld, ld, x, n, part);
+      k_dot_finish<<<kk, kRedThreads, 0, st>>>(part, kRedBlocks, res);
+      cudaError_t e = cudaMemcpyAsync(h.data() + 2 * k0, res, sizeof(double) * 2 * kk, cudaMemcpyDeviceToHost, st);
+      if (e != cudaSuccess) return e;
+    }
+    cudaError_t e = cudaStreamSynchronize(st);
+    for (int k = 0; k < K; ++k) out[k] = cplx(h[2 * k], h[2 * k + 1]);
+    return e;
+  }
+  template <typename T>
+  cplx dot(const T* a, const T* b, int64_t n, cudaError_t& e) {
+    cplx r;
+    e = dots(a, 0, 1, b, n, &r);
+    return r;
+  }
+  template <typename T>
+  void axpby(T* y, const T* x, cplx a, cplx b, int64_t n) {
+    k_axpby<T><<<grid_of(n), 256, 0, st>>>(y, x, cd{a.real(), a.imag()}, cd{b.real(), b.imag()}, n);
+  }
+  // y -= sum_k q_k V_k
+  template <typename T>
+  cudaError_t sub_multi(T* y, const T* V, int64_t ld, const cplx* q, int K, int64_t n) {
+    for (int k0 = 0; k0 < K; k0 += kMaxDots) {
+      const int kk = std::min(kMaxDots, K - k0);
+      std::vector<double> h(2 * kk);
+      for (int k = 0; k < kk; ++k) {
+        h[2 * k] = q[k0 + k].real();
+        h[2 * k + 1] = q[k0 + k].imag();
+      }
+      cudaError_t e = cudaMemcpyAsync(coef, h.data(), sizeof(double) * 2 * kk, cudaMemcpyHostToDevice, st);
+      if (e != cudaSuccess) return e;
+      k_sub_multi<T><<<grid_of(n), 256, sizeof(double) * 2 * kk, st>>>(y, V + (int64_t)k0 * ld, ld, coef, kk, n);
+      e = cudaStreamSynchronize(st);  // h must outlive the copy
+      if (e != cudaSuccess) return e;
+    }
+    return cudaGetLastError();
+  }
+  template <typename T>
+  cudaError_t combine(T* out, const T* V, int64_t ld, const double* c, int K, int64_t n) {
+    cudaError_t e = cudaMemcpyAsync(coef, c, sizeof(double) * K, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return e;
+    k_combine<T><<<grid_of(n), 256, sizeof(double) * K, st>>>(out, V, ld, coef, K, n);
+    return cudaStreamSynchronize(st);
+  }
+};
+
+// orth_wrt_previous_evecs (lanczos.cpp:57-74): classical Gram-Schmidt, all
+// projections first, then one subtraction pass.
+cudaError_t orth(Blas& B, double2* v, const double2* V, int64_t ld, int K, int64_t n) {
+  if (K <= 0) return cudaSuccess;
+  std::vector<cplx> q(K);
+  cudaError_t e = B.dots(V, ld, K, v, n, q.data());  // <V_k|v>
+  if (e != cudaSuccess) return e;
+  return B.sub_multi(v, V, ld, q.data(), K, n);  // q = conj(zdotc(v, V_k)) = <V_k|v>
+}
+
+// normalize (lanczos.cpp:50-55)
+cudaError_t normalize(Blas& B, double2* v, int64_t n) {
+  cudaError_t e;
+  const cplx d = B.dot(v, v, n, e);
+  if (e != cudaSuccess) return e;
+  B.axpby(v, (const double2*)nullptr, cplx(0, 0), cplx(1.0 / std::sqrt(d.real()), 0), n);
+  return cudaGetLastError();
+}
+
+// -------------------------------------------------- dense eigensolver (lib) --
+// cuSOLVER is loaded on first use, so the library does not depend on it unless
+// the dense path runs.
+struct Cusolver {
+  void* lib = nullptr;
+  int (*create)(void**) = nullptr;
+  int (*destroy)(void*) = nullptr;
+  int (*set_stream)(void*, cudaStream_t) = nullptr;
+  int (*zheevd_bufsize)(void*, int, int, int, const void*, int, const double*, int*) = nullptr;
+  int (*zheevd)(void*, int, int, int, void*, int, double*, void*, int, int*) = nullptr;
+  bool load(std::string& err) {
+    if (lib) return true;
+    const char* names[] = {"libcusolver.so", "libcusolver.so.12", "libcusolver.so.11", "libcusolver.so.13"};
+    for (const char* nm : names)
+      if ((lib = dlopen(nm, RTLD_NOW | RTLD_LOCAL))) break;
+    if (!lib) {
+      err = "dense path: libcusolver could not be loaded";
+      return false;
+    }
+    create = (int (*)(void**))dlsym(lib, "cusolverDnCreate");
+    destroy = (int (*)(void*))dlsym(lib, "cusolverDnDestroy");
+    set_stream = (int (*)(void*, cudaStream_t))dlsym(lib, "cusolverDnSetStream");
+    zheevd_bufsize = (int (*)(void*, int, int, int, const void*, int, const double*, int*))dlsym(
+        lib, "cusolverDnZheevd_bufferSize");
+    zheevd = (int (*)(void*, int, int, int, void*, int, double*, void*, int, int*))dlsym(lib, "cusolverDnZheevd");
+    if (!create || !destroy || !set_stream || !zheevd_bufsize || !zheevd) {
+      err = "dense path: cusolverDn symbols missing";
+      return false;
+    }
+    return true;
+  }
+};
+Cusolver g_cusolver;
+
+constexpr int kEigModeNoVector = 0, kEigModeVector = 1, kFillUpper = 1;  // cusolverEigMode_t, cublasFillMode_t
+
+int solve_dense(Sector& S, const edg_solver_opts& o, double* eigs, int64_t cap, int64_t* n_out, double* evecs,
+                int64_t evecs_cap, edg_solver_stats* stats) {
+  const int64_t n = S.P.n_p;
+  if (cap < n) return fail(EDG_ERR_INVALID, "dense path returns all n_p eigenvalues: eigs_capacity too small");
+  std::string err;
+  if (!g_cusolver.load(err)) return fail(EDG_ERR_UNSUPPORTED, err);
+  cudaStream_t st = S.stream;
+  double2 *H = nullptr, *e = nullptr, *work = nullptr;
+  double* W = nullptr;
+  int* info = nullptr;
+  auto cleanup = [&]() {
+    cudaFree(H);
+    cudaFree(e);
+    cudaFree(work);
+    cudaFree(W);
+    cudaFree(info);
+  };
+  cudaError_t ce = cudaMalloc(&H, sizeof(double2) * n * n);
+  if (ce == cudaSuccess) ce = cudaMalloc(&e, sizeof(double2) * n);
+  if (ce == cudaSuccess) ce = cudaMalloc(&W, sizeof(double) * n);
+  if (ce == cudaSuccess) ce = cudaMalloc(&info, sizeof(int));
+  if (ce != cudaSuccess) {
+    cleanup();
+    return fail(EDG_ERR_NOMEM, "dense path: out of device memory");
+  }
+  const auto t0 = std::chrono::steady_clock::now();
+  // column j of H = H e_j (makeH writes the same matrix elements)
+  for (int64_t j = 0; j < n && ce == cudaSuccess; ++j) {
+    k_unit<<<grid_of(n), 256, 0, st>>>(e, n, j);
+    ce = launch_hv(S, e, H + j * n, true, st);
+  }
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+  const auto t1 = std::chrono::steady_clock::now();
+  if (ce != cudaSuccess) {
+    cleanup();
+    return cuda_fail(ce, "dense path: assembling H");
+  }
+  void* h = nullptr;
+  int lwork = 0, hinfo = 0;
+  const int jobz = (evecs && evecs_cap > 0) ? kEigModeVector : kEigModeNoVector;
+  int rc = g_cusolver.create(&h);
+  if (rc == 0) rc = g_cusolver.set_stream(h, st);
+  if (rc == 0) rc = g_cusolver.zheevd_bufsize(h, jobz, kFillUpper, (int)n, H, (int)n, W, &lwork);
+  if (rc == 0 && cudaMalloc(&work, sizeof(double2) * std::max(1, lwork)) != cudaSuccess) rc = -1;
+  if (rc == 0) rc = g_cusolver.zheevd(h, jobz, kFillUpper, (int)n, H, (int)n, W, work, lwork, info);
+  if (rc == 0) ce = cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (rc == 0 && ce == cudaSuccess) ce = cudaMemcpyAsync(eigs, W, sizeof(double) * n, cudaMemcpyDeviceToHost, st);
+  if (rc == 0 && ce == cudaSuccess && jobz == kEigModeVector) {
+    const int64_t nv = std::min<int64_t>(evecs_cap, n);
+    ce = cudaMemcpyAsync(evecs, H, sizeof(double2) * n * nv, cudaMemcpyDeviceToHost, st);
+  }
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+  if (h) g_cusolver.destroy(h);
+  cleanup();
+  if (rc != 0) return fail(EDG_ERR_CUDA, "dense path: cusolverDnZheevd failed (status " + std::to_string(rc) + ")");
+  if (ce != cudaSuccess) return cuda_fail(ce, "dense path");
+  if (hinfo != 0) return fail(EDG_ERR_NOT_CONVERGED, "dense path: zheevd info " + std::to_string(hinfo));
+  *n_out = n;
+  if (stats) {
+    stats->path = 1;
+    stats->hv_calls = n;
+    stats->hv_seconds = std::chrono::duration<double>(t1 - t0).count();
+    stats->total_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+  return EDG_OK;
+}
+
+void log_line(const edg_solver_opts& o, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
+void log_line(const edg_solver_opts& o, const char* fmt, ...) {
+  if (!o.log_fn) return;
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  o.log_fn(o.log_ctx, buf);
+}
+
+int solve_lanczos(Sector& S, const edg_solver_opts& o, double* eigs, int64_t cap, int64_t* n_out, double* evecs,
+                  int64_t evecs_cap, edg_solver_stats* stats) {
+  const int64_t n = S.P.n_p;
+  const int how_many = (int)std::min<int64_t>(o.n_ev, n);
+  if (how_many <= 0) return fail(EDG_ERR_INVALID, "n_ev must be positive");
+  if (cap < how_many) return fail(EDG_ERR_INVALID, "eigs_capacity < n_ev");
+  if (o.iterations <= 0 || o.ncycles <= 0) return fail(EDG_ERR_INVALID, "iterations and ncycles must be positive");
+  int iterations = o.iterations;
+  cudaStream_t st = S.stream;
+  Blas B;
+  cudaError_t ce = B.init(st);
+  if (ce != cudaSuccess) return fail(EDG_ERR_NOMEM, "Lanczos: scratch allocation");
+  // device storage: v_p, w, the Krylov vectors of a cycle, earlier eigenvectors
+  const int64_t max_it = std::min<int64_t>(iterations, n);
+  double2 *vp = nullptr, *w = nullptr, *vs = nullptr, *prev = nullptr;
+  auto cleanup = [&]() {
+    cudaFree(vp);
+    cudaFree(w);
+    cudaFree(vs);
+    cudaFree(prev);
+  };
+  ce = cudaMalloc(&vp, sizeof(double2) * n);
+  if (ce == cudaSuccess) ce = cudaMalloc(&w, sizeof(double2) * n);
+  if (ce == cudaSuccess) ce = cudaMalloc(&vs, sizeof(double2) * n * max_it);
+  if (ce == cudaSuccess) ce = cudaMalloc(&prev, sizeof(double2) * n * how_many);
+  if (ce != cudaSuccess) {
+    cleanup();
+    return fail(EDG_ERR_NOMEM, "Lanczos: the stored Krylov vectors do not fit in device memory");
+  }
+  using clk = std::chrono::steady_clock;
+  const auto t_start = clk::now();
+  double t_hv = 0, t_ortho = 0;
+  int64_t hv_calls = 0;
+  std::vector<double> all_eigs;
+  std::vector<double> alphas, betas, d, e, y, wk;
+  double eig0 = 0;
+  for (int num = 0; num < how_many; ++num) {
+    iterations = (int)std::min<int64_t>(iterations, n - num);  // lanczos.cpp:188
+    edg_fill_random(vp, n, EDG_C128, o.seed + (uint64_t)num, st);
+    double previous_eig = 1000.0;
+    for (int cycle = 0; cycle < o.ncycles; ++cycle) {
+      if ((ce = orth(B, vp, prev, n, num, n)) != cudaSuccess) break;
+      if ((ce = normalize(B, vp, n)) != cudaSuccess) break;
+      alphas.clear();
+      betas.assign(1, 0.0);
+      int n_vs = 0;
+      double beta = 0.0;
+      bool stop_cycle = false;
+      for (int it = 0; it < iterations && !stop_cycle; ++it) {
+        auto t0 = clk::now();
+        if ((ce = launch_hv(S, vp, w, true, st)) != cudaSuccess) break;
+        if ((ce = cudaStreamSynchronize(st)) != cudaSuccess) break;
+        t_hv += std::chrono::duration<double>(clk::now() - t0).count();
+        ++hv_calls;
+        if (it != 0) B.axpby(w, vs + (int64_t)(it - 1) * n, cplx(-beta, 0), cplx(1, 0), n);
+        const cplx alpha = std::conj(B.dot(w, vp, n, ce));  // conj(zdotc(w, v_p)), lanczos.cpp:238
+        if (ce != cudaSuccess) break;
+        alphas.push_back(alpha.real());
+        B.axpby(w, vp, -alpha, cplx(1, 0), n);
+        cudaMemcpyAsync(vs + (int64_t)n_vs * n, vp, sizeof(double2) * n, cudaMemcpyDeviceToDevice, st);
+        ++n_vs;
+        beta = std::sqrt(B.dot(w, w, n, ce).real());
+        if (ce != cudaSuccess) break;
+        // v_p = w / beta
+        B.axpby(vp, w, cplx(1.0 / beta, 0), cplx(0, 0), n);
+        betas.push_back(beta);
+        auto t1 = clk::now();
+        if ((ce = orth(B, vp, prev, n, num, n)) != cudaSuccess) break;
+        if (cycle == o.ncycles - 1 && (ce = orth(B, vp, vs, n, n_vs, n)) != cudaSuccess) break;
+        if ((ce = normalize(B, vp, n)) != cudaSuccess) break;
+        t_ortho += std::chrono::duration<double>(clk::now() - t1).count();
+        // lowest eigenvalue of T (diagonal Re(alpha), off-diagonal beta)
+        const int m = (int)alphas.size();
+        d.assign(alphas.begin(), alphas.end());
+        e.assign(m, 0.0);
+        for (int j = 1; j < m; ++j) e[j] = betas[j];
+        eig0 = tridiag_eigenvalue(d.data(), e.data(), m, 0);
+        if (cycle != 0 && cycle != o.ncycles - 1 && it > 1) {
+          log_line(o, "Eigs[0]      = %+.15f", eig0);
+          log_line(o, "Previous Eig = %+.15f", previous_eig);
+          if (std::fabs(eig0 - previous_eig) < o.tol) {
+            log_line(o, "Convergence, doing last cycle with orth !!");
+            stop_cycle = true;           // it = iterations  (lanczos.cpp:293)
+            cycle = o.ncycles - 2;       // next cycle is the last one
+          }
+          previous_eig = eig0;
+        } else if (cycle == o.ncycles - 1) {
+          log_line(o, "Final cycle, Eigs[0]      = %+.15f", eig0);
+        } else {
+          log_line(o, "Eigs[0]      = %+.15f", eig0);
+          log_line(o, "Previous Eig = %+.15f", previous_eig);
+          previous_eig = eig0;
+        }
+      }
+      if (ce != cudaSuccess) break;
+      // Ritz vector from the stored Krylov vectors (lanczos.cpp:311-320)
+      const int m = (int)alphas.size();
+      d.assign(alphas.begin(), alphas.end());
+      e.assign(m, 0.0);
+      for (int j = 1; j < m; ++j) e[j] = betas[j];
+      y.assign(m, 0.0);
+      wk.assign(5 * m, 0.0);
+      tridiag_eigenvector(d.data(), e.data(), m, tridiag_eigenvalue(d.data(), e.data(), m, 0), y.data(), wk.data());
+      if ((ce = B.combine(vp, vs, n, y.data(), n_vs, n)) != cudaSuccess) break;
+      if ((ce = orth(B, vp, prev, n, num, n)) != cudaSuccess) break;
+      if ((ce = normalize(B, vp, n)) != cudaSuccess) break;
+    }
+    if (ce != cudaSuccess) break;
+    cudaMemcpyAsync(prev + (int64_t)num * n, vp, sizeof(double2) * n, cudaMemcpyDeviceToDevice, st);
+    log_line(o, "Eigenvalue number %d = %+.15f", num, eig0);
+    all_eigs.push_back(eig0);
+  }
+  if (ce == cudaSuccess && evecs && evecs_cap > 0) {
+    const int64_t nv = std::min<int64_t>(evecs_cap, how_many);
+    ce = cudaMemcpyAsync(evecs, prev, sizeof(double2) * n * nv, cudaMemcpyDeviceToHost, st);
+  }
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+  cleanup();
+  if (ce != cudaSuccess) return cuda_fail(ce, "Lanczos");
+  for (size_t k = 0; k < all_eigs.size(); ++k) eigs[k] = all_eigs[k];
+  *n_out = (int64_t)all_eigs.size();
+  if (stats) {
+    stats->path = 0;
+    stats->hv_calls = hv_calls;
+    stats->hv_seconds = t_hv;
+    stats->ortho_seconds = t_ortho;
+    stats->total_seconds = std::chrono::duration<double>(clk::now() - t_start).count();
+  }
+  return EDG_OK;
+}
+
+}  // namespace
+
+int solve_plain(Sector& S, const edg_solver_opts& o, double* eigs, int64_t cap, int64_t* n_out, double* evecs,
+                int64_t evecs_cap, edg_solver_stats* stats) {
+  if (stats) std::memset(stats, 0, sizeof(*stats));
+  if (o.dense_threshold >= 0 && S.P.n_p <= o.dense_threshold)
+    return solve_dense(S, o, eigs, cap, n_out, evecs, evecs_cap, stats);
+  return solve_lanczos(S, o, eigs, cap, n_out, evecs, evecs_cap, stats);
+}
+
+}  // namespace edg

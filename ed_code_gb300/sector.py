@@ -103,6 +103,25 @@ class GpuSector:
         st = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
         N.check(N.lib().edg_hv(self._h, C.c_void_p(v.data_ptr()), C.c_void_p(w.data_ptr()), code, C.c_void_p(st)))
 
+    def solve_plain(self, n_ev: int = 2, iterations: int = 100, ncycles: int = 10, tol: float = 1e-11,
+                    seed: int = 0, dense_threshold: int = 10000, want_vectors: bool = False, log=None):
+        """The sector eigensolver of sector_lanczos in FP64 (lanczos_evecs, or
+        exact_evecs for n_p <= dense_threshold).  Returns (eigs, evecs, stats)."""
+        dense = dense_threshold >= 0 and self.n_p <= dense_threshold
+        cap = self.n_p if dense else min(n_ev, self.n_p)
+        eigs = np.empty(cap, np.float64)
+        nvec = (min(n_ev, self.n_p) if want_vectors else 0)
+        evecs = np.empty((nvec, self.n_p), np.complex128) if nvec else None
+        cb = N.LOG_FN(lambda ctx, line: log(line.decode())) if log else N.LOG_FN()
+        opts = N.edg_solver_opts(int(n_ev), int(iterations), int(ncycles), float(tol), int(seed),
+                                 int(dense_threshold), cb, None)
+        n_out = C.c_int64()
+        st = N.edg_solver_stats()
+        N.check(N.lib().edg_solve_plain(self._h, C.byref(opts), eigs.ctypes.data, cap, C.byref(n_out),
+                                        evecs.ctypes.data if nvec else None, nvec, C.byref(st)))
+        stats = {f: getattr(st, f) for f, _ in N.edg_solver_stats._fields_}
+        return eigs[: n_out.value], evecs, stats
+
     def count_offdiag(self) -> int:
         n = C.c_int64()
         N.check(N.lib().edg_count_offdiag(self._h, C.byref(n)))

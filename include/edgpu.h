@@ -107,6 +107,35 @@ int edg_hv_host(edg_sector* s, const void* v, void* w, int dtype);
  * (the nnz_off of the algorithmic byte count). */
 int edg_count_offdiag(edg_sector* s, int64_t* nnz_off);
 
+/* Options of the plain (FP64) sector eigensolver. */
+typedef struct {
+  int n_ev;                 /* eigenvalues wanted: Num_Eigenvalues */
+  int iterations;           /* Lanczos steps per cycle: Lanczos_iterations */
+  int ncycles;              /* restarts: Lanczos_ncycles */
+  double tol;               /* |E0 - E0_previous| < tol ends the middle cycles: tol */
+  uint64_t seed;            /* start vector of eigenvalue k: splitmix64 stream seed + k */
+  int64_t dense_threshold;  /* n_p <= this takes the dense path (the reference: 10000); -1: never */
+  void (*log_fn)(void* ctx, const char* line); /* optional: the reference's per-iteration log lines */
+  void* log_ctx;
+} edg_solver_opts;
+
+typedef struct {
+  int path;                 /* 0: Lanczos, 1: dense */
+  int64_t hv_calls;
+  double hv_seconds, ortho_seconds, total_seconds;
+} edg_solver_stats;
+
+/* The sector eigensolver of sector_lanczos in FP64 on the GPU.
+ * Replaces: lanczos_evecs (lanczos.cpp:133-349) and, for n_p <= dense_threshold,
+ * exact_evecs (lanczos.cpp:81-131), dispatched as Lanczos_sector.cpp:105-120.
+ * eigs receives *n_eigs values: min(n_ev, n_p) for Lanczos (one per deflation
+ * step, so degenerate levels repeat), all n_p for the dense path, ascending
+ * for the dense path and in deflation order for Lanczos, as the reference
+ * returns them.  evecs (NULL allowed) receives up to evecs_capacity
+ * eigenvectors of n_p complex128 entries each, in the same order. */
+int edg_solve_plain(edg_sector* s, const edg_solver_opts* opts, double* eigs, int64_t eigs_capacity,
+                    int64_t* n_eigs, double* evecs, int64_t evecs_capacity, edg_solver_stats* stats);
+
 /* Deterministic complex test vector (splitmix64, entries uniform in [-1,1)^2)
  * written to device memory; the same generator as the test suite's. */
 int edg_fill_random(void* dst, int64_t n, int dtype, uint64_t seed, void* stream);
