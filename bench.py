@@ -220,8 +220,37 @@ def run_device(args, world, rank, local_rank):
     v = torch.empty(sec.n_p, dtype=ctype, device=dev)
     w = torch.empty_like(v)
     stream = torch.cuda.Stream(device=dev)
+
+    def timed(steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for _ in range(steps):
+                sec.hv(v, w, stream)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
     with torch.cuda.stream(stream):
         fill_random(v, 4, stream)
+    # matrix-free H*v (orbit search on the fly), timed for the record
+    mf_steps = max(1, min(args.steps, 3))
+    with torch.cuda.stream(stream):
+        sec.hv(v, w, stream)
+    mf_ms = timed(mf_steps) / mf_steps
+    B_mf = sec.algorithmic_bytes(elem, nnz)
+    # stored targets: the search done once, its results streamed every H*v
+    mode = "matrix-free"
+    t_tgt = None
+    if not args.matrix_free:
+        t0 = time.perf_counter()
+        if sec.build_targets():
+            torch.cuda.synchronize()
+            t_tgt = time.perf_counter() - t0
+            mode = "stored-targets"
+            B = sec.algorithmic_bytes(elem, nnz)
+    with torch.cuda.stream(stream):
         for _ in range(args.warmup):
             sec.hv(v, w, stream)
     stream.synchronize()
@@ -285,20 +314,25 @@ def run_device(args, world, rank, local_rank):
 
     peak, peak_kind = measured_peak_hbm()
     achieved = B / (ms_step / 1e3) / 1e9
-    traffic = profile_traffic(f"hv_{args.workload}_{args.dtype}")
+    traffic = profile_traffic(f"hv_{mode}_{args.workload}_{args.dtype}")
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if fp64 else "f32", "data": "synthetic",
         "config": {"workload": args.workload, "n_p": sec.n_p, "nnz_off": nnz, "vector": args.dtype,
-                   "algorithmic_bytes_per_hv": B, "basis_seconds": round(t_basis, 3),
+                   "hv_mode": mode, "algorithmic_bytes_per_hv": B, "basis_seconds": round(t_basis, 3),
+                   "target_build_seconds": None if t_tgt is None else round(t_tgt, 3),
+                   "stored_target_bytes": 4 * sec.info.get("n_targets", 0),
+                   "matrix_free_ms_per_step": mf_ms,
+                   "matrix_free_GBps": B_mf / (mf_ms / 1e3) / 1e9,
                    "l2": "inputs larger than L2 (no flush needed)", "orbit_search": "torus" if sec.info["torus"] else "walk"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "traffic": traffic},
         "cpu_baseline": cpu,
         "e2e": e2e,
         "clocks": clocks,
-        "gpu_launches": args.steps,
+        # one H*v kernel per step; the stored-target path adds the u = v/norm pass
+        "gpu_launches": args.steps * (2 if mode == "stored-targets" else 1),
     }
     if rank == 0:
         print(json.dumps(out), flush=True)
@@ -314,6 +348,7 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="tri6x6_k00")
     ap.add_argument("--dtype", choices=["c64", "c128"], default="c64")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--matrix-free", action="store_true", help="do not store the searched targets")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-step-seconds", type=float, default=4.0)

@@ -53,7 +53,7 @@ class edg_sector_info(C.Structure):
     _fields_ = [
         ("n_sites", C.c_int), ("n_ones", C.c_int), ("L1", C.c_int), ("L2", C.c_int), ("kx", C.c_int),
         ("ky", C.c_int), ("torus", C.c_int), ("n_groups", C.c_int), ("n_p", C.c_int64), ("n_configs", C.c_int64),
-        ("device_bytes", C.c_int64),
+        ("device_bytes", C.c_int64), ("n_targets", C.c_int64),
     ]
 
 
@@ -74,6 +74,16 @@ class edg_solver_stats(C.Structure):
     ]
 
 
+class edg_mixed_opts(C.Structure):
+    _fields_ = [("n_ev", C.c_int), ("iterations", C.c_int), ("reorth_every", C.c_int), ("seed", C.c_uint64),
+                ("want_vectors", C.c_int)]
+
+
+class edg_mixed_stats(C.Structure):
+    _fields_ = [("hv_calls", C.c_int64), ("hv_seconds", C.c_double), ("total_seconds", C.c_double),
+                ("passes", C.c_int)]
+
+
 # name -> (restype, argtypes); every exported symbol of include/edgpu.h
 SIGNATURES = {
     "edg_last_error": (C.c_char_p, []),
@@ -88,8 +98,12 @@ SIGNATURES = {
     "edg_hv_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
     "edg_count_offdiag": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
     "edg_fill_random": (C.c_int, [C.c_void_p, C.c_int64, C.c_int, C.c_uint64, C.c_void_p]),
+    "edg_sector_build_targets": (C.c_int, [C.c_void_p, C.c_int64]),
+    "edg_sector_free_targets": (C.c_int, [C.c_void_p]),
     "edg_solve_plain": (C.c_int, [C.c_void_p, C.POINTER(edg_solver_opts), C.c_void_p, C.c_int64,
                                   C.POINTER(C.c_int64), C.c_void_p, C.c_int64, C.POINTER(edg_solver_stats)]),
+    "edg_solve_mixed": (C.c_int, [C.c_void_p, C.POINTER(edg_mixed_opts), C.c_void_p, C.c_void_p, C.c_void_p,
+                                  C.POINTER(C.c_int64), C.c_void_p, C.POINTER(edg_mixed_stats)]),
 }
 
 _lib: Optional[C.CDLL] = None

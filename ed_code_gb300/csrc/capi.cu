@@ -5,6 +5,7 @@
 #include <cmath>
 #include <complex>
 #include <cstdio>
+#include <cstdint>
 #include <cstdlib>
 #include <cstring>
 #include <map>
@@ -34,6 +35,7 @@ int cuda_fail(cudaError_t e, const char* what) {
 constexpr double kPi = 3.14159265358979323846;
 
 static void free_sector(Sector& S) {
+  free_targets(S);
   void* ptrs[] = {S.dP,   S.reps,    S.lid,         S.recs,         S.vrecs,       S.Ia,    S.Ib,
                   S.groups, S.ch,   S.bows,    S.nk,          S.rots,         S.perms,       S.binom, S.host_in.ptr,
                   S.host_out.ptr, S.lz_work.ptr, S.tplan, S.tgroups};
@@ -482,6 +484,7 @@ int edg_sector_get_info(const edg_sector* s, edg_sector_info* info) {
   info->n_p = P.n_p;
   info->n_configs = P.n_configs;
   info->device_bytes = (int64_t)s->s.device_bytes;
+  info->n_targets = P.n_targets;
   return EDG_OK;
 }
 
@@ -602,6 +605,32 @@ int edg_solve_plain(edg_sector* s, const edg_solver_opts* opts, double* eigs, in
   if (!s || !opts || !eigs || !n_eigs) return fail(EDG_ERR_INVALID, "NULL argument");
   *n_eigs = 0;
   return solve_plain(s->s, *opts, eigs, eigs_capacity, n_eigs, evecs, evecs_capacity, stats);
+}
+
+int edg_solve_mixed(edg_sector* s, const edg_mixed_opts* opts, double* eigs, double* ritz, double* residuals,
+                    int64_t* n_eigs, double* evecs, edg_mixed_stats* stats) {
+  if (!s || !opts || !eigs || !n_eigs) return fail(EDG_ERR_INVALID, "NULL argument");
+  if (opts->iterations > 2000) return fail(EDG_ERR_UNSUPPORTED, "at most 2000 iterations");
+  *n_eigs = 0;
+  if (stats) std::memset(stats, 0, sizeof(*stats));
+  return solve_mixed(s->s, *opts, eigs, ritz, residuals, n_eigs, opts->want_vectors ? evecs : nullptr, stats);
+}
+
+int edg_sector_build_targets(edg_sector* s, int64_t max_bytes) {
+  if (!s) return fail(EDG_ERR_INVALID, "NULL sector");
+  std::string err;
+  const int rc = build_targets(s->s, max_bytes > 0 ? max_bytes : INT64_MAX, err);
+  if (rc != EDG_OK) return fail(rc, err);
+  return EDG_OK;
+}
+
+int edg_sector_free_targets(edg_sector* s) {
+  if (!s) return fail(EDG_ERR_INVALID, "NULL sector");
+  const int64_t before = s->s.P.n_targets;
+  free_targets(s->s);
+  s->s.device_bytes -= 4 * before + 8 * s->s.P.n_p + 16 * s->s.P.n_p;
+  cudaMemcpy(s->s.dP, &s->s.P, sizeof(SectorParams), cudaMemcpyHostToDevice);
+  return EDG_OK;
 }
 
 int edg_count_offdiag(edg_sector* s, int64_t* nnz_off) {

@@ -87,6 +87,10 @@ struct Sector {
   // H*v kernel: 0 = hv.cu (default), 1 = hv_torus.cu when the sector has a
   // torus plan.  Chosen at sector creation from EDG_HV_VARIANT (for A/B timing).
   int hv_variant = 0;
+  // stored targets: one u32 per (row, anti-aligned pair), rows at row_ptr
+  uint32_t* tgt = nullptr;
+  uint64_t* row_ptr = nullptr;
+  DeviceBuffer ubuf;  // v_j / norm_j scratch for the stored-target H*v
 };
 
 // basis.cu
@@ -98,9 +102,14 @@ cudaError_t launch_hv_generic(const Sector& S, const void* v, void* w, bool fp64
 // lanczos.cu
 int solve_plain(Sector& S, const edg_solver_opts& o, double* eigs, int64_t cap, int64_t* n_out, double* evecs,
                 int64_t evecs_cap, edg_solver_stats* stats);
+int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, double* resid, int64_t* n_out,
+                double* evecs, edg_mixed_stats* stats);
 // hv_torus.cu
 cudaError_t launch_hv_torus(const Sector& S, const void* v, void* w, bool fp64, cudaStream_t st);
 cudaError_t count_offdiag(const Sector& S, unsigned long long* nnz_dev, cudaStream_t st);
+int build_targets(Sector& S, int64_t max_bytes, std::string& err);
+void free_targets(Sector& S);
+cudaError_t launch_hv_stored(const Sector& S, const void* v, void* w, bool fp64, cudaStream_t st);
 int hv_grid_blocks(bool fp64, bool torus, bool chch);
 
 }  // namespace edg

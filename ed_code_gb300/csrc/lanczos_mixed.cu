@@ -1,0 +1,442 @@
+// Mixed-precision Lanczos: Krylov vectors and H*v in FP32 complex, FP64 only
+// where stability needs it.
+//
+//  * one Lanczos run (no restarts, no deflation) of `iterations` steps from a
+//    seeded start vector; alpha_j = Re<v_j|Hv_j> and beta_{j+1} = |w| are
+//    reduced in FP64 with compensated (Neumaier) sums over the FP32 vectors,
+//    on the device, so a step needs no host round trip;
+//  * reorth_every > 0 keeps every Krylov vector (FP32) and, every
+//    reorth_every steps, orthogonalises the new vector against all of them
+//    twice (classical Gram-Schmidt with FP64 coefficients); reorth_every = 0
+//    keeps three vectors resident (the 36-site case: 2 GB each);
+//  * T's lowest eigenvalues by bisection and their eigenvectors by inverse
+//    iteration, in FP64 in one CTA on the GPU; Ritz values that T shares with
+//    T-without-its-first-row are copies produced by lost orthogonality and are
+//    dropped (Cullum and Willoughby's test);
+//  * Ritz vectors in FP64 -- from the stored vectors, or by re-running the
+//    recurrence with the same alpha/beta when only three vectors are kept;
+//  * one FP64 H*v per Ritz vector x: the reported eigenvalue is the Rayleigh
+//    quotient <x|Hx>/<x|x>, and |Hx - theta x|/|x| is its residual.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/edgpu.h"
+#include "blas1.cuh"
+#include "edg_sector.cuh"
+#include "tridiag.cuh"
+
+namespace edg {
+
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+namespace {
+
+constexpr int kMaxEv = 32;      // Ritz pairs returned
+constexpr int kCand = 2 * kMaxEv + 8;  // lowest eigenvalues of T examined for copies
+
+// partial sums of sum conj(a) b over FP32 vectors, FP64 compensated;
+// part[(k*gridDim.x + b)*2 + {0,1}], k = blockIdx.y selects a = V + k*ld
+__global__ void __launch_bounds__(kRedThreads) k_dot32(const float2* __restrict__ V, int64_t ld,
+                                                       const float2* __restrict__ x, int64_t n,
+                                                       double* __restrict__ part) {
+  const float2* a = V + (int64_t)blockIdx.y * ld;
+  Acc sr, si;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 p = a[i], q = x[i];
+    sr.add((double)p.x * q.x + (double)p.y * q.y);
+    si.add((double)p.x * q.y - (double)p.y * q.x);
+  }
+  __shared__ double rr[kRedThreads], ri[kRedThreads];
+  rr[threadIdx.x] = sr.value();
+  ri[threadIdx.x] = si.value();
+  __syncthreads();
+  for (int h = kRedThreads / 2; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) {
+      rr[threadIdx.x] += rr[threadIdx.x + h];
+      ri[threadIdx.x] += ri[threadIdx.x + h];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const int64_t o = ((int64_t)blockIdx.y * gridDim.x + blockIdx.x) * 2;
+    part[o] = rr[0];
+    part[o + 1] = ri[0];
+  }
+}
+
+// Sum the partials of vector k (one CTA per k); mode 0: complex result to
+// out[2k], mode 1: real part to out[0], mode 2: sqrt of the real part to out[0].
+__global__ void __launch_bounds__(kRedThreads) k_finish(const double* __restrict__ part, int nb, double* out,
+                                                        int mode) {
+  const double* p = part + (int64_t)blockIdx.x * nb * 2;
+  __shared__ double rr[kRedThreads], ri[kRedThreads];
+  double a = 0, b = 0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    a += p[2 * i];
+    b += p[2 * i + 1];
+  }
+  rr[threadIdx.x] = a;
+  ri[threadIdx.x] = b;
+  __syncthreads();
+  for (int h = kRedThreads / 2; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) {
+      rr[threadIdx.x] += rr[threadIdx.x + h];
+      ri[threadIdx.x] += ri[threadIdx.x + h];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    if (mode == 0) {
+      out[2 * blockIdx.x] = rr[0];
+      out[2 * blockIdx.x + 1] = ri[0];
+    } else if (mode == 1) {
+      out[0] = rr[0];
+    } else {
+      out[0] = sqrt(rr[0]);
+    }
+  }
+}
+
+// w = w - alpha v - beta vprev (FP64 arithmetic, FP32 storage), and partial
+// sums of |w|^2 of the stored values.
+__global__ void __launch_bounds__(kRedThreads) k_step(float2* __restrict__ w, const float2* __restrict__ v,
+                                                      const float2* __restrict__ vprev,
+                                                      const double* __restrict__ alpha,
+                                                      const double* __restrict__ beta, int64_t n,
+                                                      double* __restrict__ part) {
+  const double a = *alpha, b = vprev ? *beta : 0.0;
+  Acc s;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 wi = w[i], vi = v[i];
+    double re = (double)wi.x - a * vi.x, im = (double)wi.y - a * vi.y;
+    if (vprev) {
+      const float2 pi = vprev[i];
+      re -= b * pi.x;
+      im -= b * pi.y;
+    }
+    const float2 o = make_float2((float)re, (float)im);
+    w[i] = o;
+    s.add((double)o.x * o.x + (double)o.y * o.y);
+  }
+  __shared__ double rr[kRedThreads];
+  rr[threadIdx.x] = s.value();
+  __syncthreads();
+  for (int h = kRedThreads / 2; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) rr[threadIdx.x] += rr[threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = rr[0];
+    part[2 * blockIdx.x + 1] = 0.0;
+  }
+}
+
+// dst = src / beta
+__global__ void k_scale_inv(float2* __restrict__ dst, const float2* __restrict__ src, const double* __restrict__ beta,
+                            int64_t n) {
+  const double s = 1.0 / *beta;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 x = src[i];
+    dst[i] = make_float2((float)(x.x * s), (float)(x.y * s));
+  }
+}
+
+// y -= sum_k q_k V_k with q (complex, device) read into shared memory
+__global__ void k_sub32(float2* __restrict__ y, const float2* __restrict__ V, int64_t ld,
+                        const double* __restrict__ q, int K, int64_t n) {
+  extern __shared__ double sq[];
+  for (int k = threadIdx.x; k < 2 * K; k += blockDim.x) sq[k] = q[k];
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 y0 = y[i];
+    double re = y0.x, im = y0.y;
+    for (int k = 0; k < K; ++k) {
+      const float2 vv = V[(int64_t)k * ld + i];
+      re -= sq[2 * k] * vv.x - sq[2 * k + 1] * vv.y;
+      im -= sq[2 * k] * vv.y + sq[2 * k + 1] * vv.x;
+    }
+    y[i] = make_float2((float)re, (float)im);
+  }
+}
+
+// X_e += c[e][j] * v (FP64 accumulators, E Ritz vectors)
+__global__ void k_accumulate(double2* __restrict__ X, int64_t ldx, const float2* __restrict__ v,
+                             const double* __restrict__ c, int E, int64_t n) {
+  extern __shared__ double sc[];
+  for (int e = threadIdx.x; e < E; e += blockDim.x) sc[e] = c[e];
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 vv = v[i];
+    for (int e = 0; e < E; ++e) {
+      double2 x = X[(int64_t)e * ldx + i];
+      x.x += sc[e] * vv.x;
+      x.y += sc[e] * vv.y;
+      X[(int64_t)e * ldx + i] = x;
+    }
+  }
+}
+
+// FP64 sums over x, Hx: |x|^2, <x|Hx>, and after theta is known |Hx - theta x|^2.
+__global__ void __launch_bounds__(kRedThreads) k_rq_partial(const double2* __restrict__ x,
+                                                            const double2* __restrict__ hx, int64_t n,
+                                                            const double* __restrict__ theta,
+                                                            double* __restrict__ part) {
+  Acc nx, re, r2;
+  const double th = theta ? *theta : 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 a = x[i], b = hx[i];
+    nx.add(a.x * a.x + a.y * a.y);
+    re.add(a.x * b.x + a.y * b.y);
+    const double dr = b.x - th * a.x, di = b.y - th * a.y;
+    r2.add(dr * dr + di * di);
+  }
+  __shared__ double s0[kRedThreads], s1[kRedThreads], s2[kRedThreads];
+  s0[threadIdx.x] = nx.value();
+  s1[threadIdx.x] = re.value();
+  s2[threadIdx.x] = r2.value();
+  __syncthreads();
+  for (int h = kRedThreads / 2; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) {
+      s0[threadIdx.x] += s0[threadIdx.x + h];
+      s1[threadIdx.x] += s1[threadIdx.x + h];
+      s2[threadIdx.x] += s2[threadIdx.x + h];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    part[3 * blockIdx.x] = s0[0];
+    part[3 * blockIdx.x + 1] = s1[0];
+    part[3 * blockIdx.x + 2] = s2[0];
+  }
+}
+
+// Lowest eigenvalues of T (diag alpha[0..m-1], off-diag beta[1..m-1]) and of
+// T-hat (first row and column removed), then the Ritz vectors' coefficients
+// for the accepted ones.  One CTA; thread k bisects eigenvalue k.
+__global__ void k_tridiag(const double* __restrict__ alpha, const double* __restrict__ beta, int m, int want,
+                          double* __restrict__ theta, double* __restrict__ theta_hat, double* __restrict__ y,
+                          double* __restrict__ work, int* __restrict__ accepted, int* __restrict__ n_acc) {
+  extern __shared__ double sh[];
+  double* d = sh;          // m
+  double* e = sh + m;      // m (e[0] unused)
+  for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    d[i] = alpha[i];
+    e[i] = i > 0 ? beta[i] : 0.0;
+  }
+  __syncthreads();
+  const int nc = min(kCand, m);
+  for (int k = threadIdx.x; k < nc; k += blockDim.x) theta[k] = tridiag_eigenvalue(d, e, m, k);
+  for (int k = threadIdx.x; k < min(kCand, m - 1); k += blockDim.x)
+    theta_hat[k] = tridiag_eigenvalue(d + 1, e + 1, m - 1, k);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    // Cullum-Willoughby: a simple eigenvalue of T that T-hat also has is a copy.
+    double scale = 0;
+    for (int i = 0; i < m; ++i) scale = fmax(scale, fabs(d[i]) + fabs(e[i]) + (i + 1 < m ? fabs(e[i + 1]) : 0.0));
+    const double tol = 1e-10 * fmax(scale, 1.0);
+    int na = 0;
+    for (int k = 0; k < nc && na < want; ++k) {
+      const bool multiple = (k > 0 && fabs(theta[k] - theta[k - 1]) < tol) || (k + 1 < nc && fabs(theta[k + 1] - theta[k]) < tol);
+      bool in_hat = false;
+      for (int q = 0; q < min(kCand, m - 1); ++q)
+        if (fabs(theta_hat[q] - theta[k]) < tol) in_hat = true;
+      if (in_hat && !multiple) continue;                         // spurious copy
+      if (multiple && k > 0 && fabs(theta[k] - theta[k - 1]) < tol) continue;  // keep one per cluster
+      accepted[na++] = k;
+    }
+    *n_acc = na;
+  }
+  __syncthreads();
+  const int na = *n_acc;
+  for (int q = threadIdx.x; q < na; q += blockDim.x)
+    tridiag_eigenvector(d, e, m, theta[accepted[q]], y + (int64_t)q * m, work + (int64_t)q * 5 * m);
+}
+
+int grid_n(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16)); }
+
+struct Dev {
+  std::vector<void*> ptrs;
+  template <class T>
+  cudaError_t alloc(T** p, size_t n) {
+    cudaError_t e = cudaMalloc(p, sizeof(T) * std::max<size_t>(n, 1));
+    if (e == cudaSuccess) ptrs.push_back(*p);
+    return e;
+  }
+  ~Dev() {
+    for (void* p : ptrs) cudaFree(p);
+  }
+};
+
+}  // namespace
+
+int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, double* resid, int64_t* n_out,
+                double* evecs, edg_mixed_stats* stats) {
+  const int64_t n = S.P.n_p;
+  const int m = (int)std::min<int64_t>(o.iterations, n);
+  const int want = std::min(std::min(o.n_ev, kMaxEv), m);
+  if (want <= 0 || m < 2) return fail(EDG_ERR_INVALID, "need n_ev >= 1 and at least 2 iterations");
+  const bool store = o.reorth_every > 0;
+  cudaStream_t st = S.stream;
+  using clk = std::chrono::steady_clock;
+  const auto t_start = clk::now();
+  Dev D;
+  float2 *V = nullptr, *w = nullptr, *buf[3] = {nullptr, nullptr, nullptr};
+  double *alpha, *beta, *part, *scal, *theta, *theta_hat, *y, *work;
+  int *acc, *nacc;
+  cudaError_t e = cudaSuccess;
+  if (store) {
+    if ((e = D.alloc(&V, (size_t)n * (m + 1))) != cudaSuccess)
+      return fail(EDG_ERR_NOMEM, "mixed Lanczos: the stored FP32 Krylov vectors do not fit (use reorth_every=0)");
+  } else {
+    for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = D.alloc(&buf[k], (size_t)n);
+    if (e != cudaSuccess) return fail(EDG_ERR_NOMEM, "mixed Lanczos: vectors do not fit");
+  }
+  if ((e = D.alloc(&w, (size_t)n)) != cudaSuccess) return fail(EDG_ERR_NOMEM, "mixed Lanczos: w");
+  const int64_t kparts = (int64_t)std::max(m + 1, 4) * kRedBlocks * 2;
+  if ((e = D.alloc(&alpha, m + 1)) != cudaSuccess || (e = D.alloc(&beta, m + 2)) != cudaSuccess ||
+      (e = D.alloc(&part, kparts)) != cudaSuccess || (e = D.alloc(&scal, 2 * (m + 2))) != cudaSuccess ||
+      (e = D.alloc(&theta, kCand)) != cudaSuccess || (e = D.alloc(&theta_hat, kCand)) != cudaSuccess ||
+      (e = D.alloc(&y, (size_t)kMaxEv * m)) != cudaSuccess || (e = D.alloc(&work, (size_t)kMaxEv * 5 * m)) != cudaSuccess ||
+      (e = D.alloc(&acc, kMaxEv)) != cudaSuccess || (e = D.alloc(&nacc, 1)) != cudaSuccess)
+    return fail(EDG_ERR_NOMEM, "mixed Lanczos: scratch");
+  cudaMemsetAsync(beta, 0, sizeof(double) * (m + 2), st);
+
+  auto vec = [&](int j) -> float2* { return store ? V + (int64_t)j * n : buf[j % 3]; };
+  auto norm_into = [&](const float2* x, double* dst) {  // dst = |x| in FP64
+    k_dot32<<<dim3(kRedBlocks, 1), kRedThreads, 0, st>>>(x, 0, x, n, part);
+    k_finish<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, dst, 2);
+  };
+  double t_hv = 0;
+  int64_t hv_calls = 0;
+  // one Lanczos pass; with acc_X non-null the Ritz vectors are accumulated
+  // instead of alpha/beta being computed (second pass, same recurrence)
+  auto run = [&](bool second, double2* X, int E, const std::vector<double>& yh) -> cudaError_t {
+    cudaError_t ce = edg_fill_random(w, n, EDG_C64, o.seed, st) == EDG_OK ? cudaSuccess : cudaErrorUnknown;
+    if (ce != cudaSuccess) return ce;
+    norm_into(w, scal);                                     // |v0 unnormalised|
+    k_scale_inv<<<grid_n(n), 256, 0, st>>>(vec(0), w, scal, n);
+    for (int j = 0; j < m; ++j) {
+      if (second) {
+        std::vector<double> c(E);
+        for (int q = 0; q < E; ++q) c[q] = yh[(size_t)q * m + j];
+        cudaMemcpyAsync(scal, c.data(), sizeof(double) * E, cudaMemcpyHostToDevice, st);
+        k_accumulate<<<grid_n(n), 256, sizeof(double) * E, st>>>(X, n, vec(j), scal, E, n);
+        if ((ce = cudaStreamSynchronize(st)) != cudaSuccess) return ce;  // c must outlive the copy
+        if (j + 1 == m) break;
+      }
+      auto t0 = clk::now();
+      if ((ce = launch_hv(S, vec(j), w, false, st)) != cudaSuccess) return ce;
+      ++hv_calls;
+      if (!second) {
+        k_dot32<<<dim3(kRedBlocks, 1), kRedThreads, 0, st>>>(vec(j), 0, w, n, part);
+        k_finish<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, alpha + j, 1);
+      }
+      k_step<<<kRedBlocks, kRedThreads, 0, st>>>(w, vec(j), j > 0 ? vec(j - 1) : nullptr, alpha + j, beta + j, n, part);
+      if (!second && store && ((j + 1) % o.reorth_every == 0)) {
+        // periodic full reorthogonalisation of w against v_0..v_j, twice
+        for (int pass = 0; pass < 2; ++pass) {
+          const int K = j + 1;
+          for (int k0 = 0; k0 < K; k0 += 512) {
+            const int kk = std::min(512, K - k0);
+            k_dot32<<<dim3(kRedBlocks, kk), kRedThreads, 0, st>>>(V + (int64_t)k0 * n, n, w, n, part);
+            k_finish<<<kk, kRedThreads, 0, st>>>(part, kRedBlocks, scal, 0);
+            k_sub32<<<grid_n(n), 256, sizeof(double) * 2 * kk, st>>>(w, V + (int64_t)k0 * n, n, scal, kk, n);
+          }
+        }
+        norm_into(w, beta + j + 1);
+      } else if (!second) {
+        k_finish<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, beta + j + 1, 2);
+      }
+      if (j + 1 < m || second) k_scale_inv<<<grid_n(n), 256, 0, st>>>(vec(j + 1), w, beta + j + 1, n);
+      if ((ce = cudaGetLastError()) != cudaSuccess) return ce;
+      t_hv += std::chrono::duration<double>(clk::now() - t0).count();
+    }
+    return cudaStreamSynchronize(st);
+  };
+  if ((e = run(false, nullptr, 0, {})) != cudaSuccess) return cuda_fail(e, "mixed Lanczos");
+  // eigenvalues and Ritz coefficients of T on the device
+  const size_t tsh = sizeof(double) * 2 * m;
+  k_tridiag<<<1, 128, tsh, st>>>(alpha, beta, m, want, theta, theta_hat, y, work, acc, nacc);
+  int na = 0;
+  std::vector<int> acc_h(kMaxEv);
+  std::vector<double> th(kCand), yh;
+  if ((e = cudaMemcpyAsync(&na, nacc, sizeof(int), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(st)) != cudaSuccess)
+    return cuda_fail(e, "mixed Lanczos: T");
+  yh.resize((size_t)std::max(na, 1) * m);
+  cudaMemcpyAsync(acc_h.data(), acc, sizeof(int) * kMaxEv, cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(th.data(), theta, sizeof(double) * std::min(kCand, m), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(yh.data(), y, sizeof(double) * na * m, cudaMemcpyDeviceToHost, st);
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "mixed Lanczos: T");
+  if (na == 0) return fail(EDG_ERR_NOT_CONVERGED, "mixed Lanczos: no Ritz value survived the copy test");
+  // Ritz vectors in FP64
+  double2 *X = nullptr, *HX = nullptr;
+  if ((e = D.alloc(&X, (size_t)na * n)) != cudaSuccess || (e = D.alloc(&HX, (size_t)n)) != cudaSuccess)
+    return fail(EDG_ERR_NOMEM, "mixed Lanczos: FP64 Ritz vectors do not fit");
+  cudaMemsetAsync(X, 0, sizeof(double2) * na * n, st);
+  int passes = 1;
+  if (store) {
+    for (int j = 0; j < m; ++j) {
+      std::vector<double> c(na);
+      for (int q = 0; q < na; ++q) c[q] = yh[(size_t)q * m + j];
+      cudaMemcpyAsync(scal, c.data(), sizeof(double) * na, cudaMemcpyHostToDevice, st);
+      k_accumulate<<<grid_n(n), 256, sizeof(double) * na, st>>>(X, n, V + (int64_t)j * n, scal, na, n);
+      if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "mixed Lanczos: Ritz vectors");
+    }
+  } else {
+    passes = 2;
+    if ((e = run(true, X, na, yh)) != cudaSuccess) return cuda_fail(e, "mixed Lanczos: second pass");
+  }
+  // FP64 Rayleigh quotient and residual of each Ritz vector
+  for (int q = 0; q < na; ++q) {
+    double2* x = X + (int64_t)q * n;
+    if ((e = launch_hv(S, x, HX, true, st)) != cudaSuccess) return cuda_fail(e, "mixed Lanczos: FP64 H*v");
+    k_rq_partial<<<kRedBlocks, kRedThreads, 0, st>>>(x, HX, n, nullptr, part);
+    std::vector<double> p(3 * kRedBlocks);
+    cudaMemcpyAsync(p.data(), part, sizeof(double) * 3 * kRedBlocks, cudaMemcpyDeviceToHost, st);
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "mixed Lanczos: residual");
+    double nx = 0, xhx = 0;
+    for (int b = 0; b < kRedBlocks; ++b) {
+      nx += p[3 * b];
+      xhx += p[3 * b + 1];
+    }
+    const double rq = xhx / nx;
+    cudaMemcpyAsync(scal, &rq, sizeof(double), cudaMemcpyHostToDevice, st);
+    k_rq_partial<<<kRedBlocks, kRedThreads, 0, st>>>(x, HX, n, scal, part);
+    cudaMemcpyAsync(p.data(), part, sizeof(double) * 3 * kRedBlocks, cudaMemcpyDeviceToHost, st);
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "mixed Lanczos: residual");
+    double r2 = 0;
+    for (int b = 0; b < kRedBlocks; ++b) r2 += p[3 * b + 2];
+    eigs[q] = rq;
+    if (ritz) ritz[q] = th[acc_h[q]];
+    if (resid) resid[q] = std::sqrt(r2 / nx);
+    if (evecs) {
+      // normalised FP64 eigenvector to the host
+      std::vector<double2> hx(n);
+      cudaMemcpyAsync(hx.data(), x, sizeof(double2) * n, cudaMemcpyDeviceToHost, st);
+      if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "mixed Lanczos: vectors");
+      const double s = 1.0 / std::sqrt(nx);
+      for (int64_t i = 0; i < n; ++i) {
+        evecs[2 * ((int64_t)q * n + i)] = hx[i].x * s;
+        evecs[2 * ((int64_t)q * n + i) + 1] = hx[i].y * s;
+      }
+    }
+  }
+  *n_out = na;
+  if (stats) {
+    stats->hv_calls = hv_calls + na;
+    stats->hv_seconds = t_hv;
+    stats->passes = passes;
+    stats->total_seconds = std::chrono::duration<double>(clk::now() - t_start).count();
+  }
+  return EDG_OK;
+}
+
+}  // namespace edg

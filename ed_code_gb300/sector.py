@@ -48,6 +48,25 @@ class GpuSector:
         self.info = {f: getattr(info, f) for f, _ in N.edg_sector_info._fields_}
         self.n_p = int(info.n_p)
 
+    def refresh_info(self) -> None:
+        info = N.edg_sector_info()
+        N.check(N.lib().edg_sector_get_info(self._h, C.byref(info)))
+        self.info = {f: getattr(info, f) for f, _ in N.edg_sector_info._fields_}
+
+    def build_targets(self, max_bytes: int = 0) -> bool:
+        """Keep the searched targets in HBM (edg_sector_build_targets).
+        Returns False, leaving the sector matrix-free, when they do not fit."""
+        rc = N.lib().edg_sector_build_targets(self._h, int(max_bytes))
+        if rc == 5:  # EDG_ERR_NOMEM
+            return False
+        N.check(rc)
+        self.refresh_info()
+        return True
+
+    def free_targets(self) -> None:
+        N.check(N.lib().edg_sector_free_targets(self._h))
+        self.refresh_info()
+
     # -- basis tables ------------------------------------------------------
     def basis(self) -> Tuple[np.ndarray, np.ndarray, np.ndarray]:
         """(pblock_states, norm, norm_inv) as pConstruct_States returns them."""
@@ -122,6 +141,25 @@ class GpuSector:
         stats = {f: getattr(st, f) for f, _ in N.edg_solver_stats._fields_}
         return eigs[: n_out.value], evecs, stats
 
+    def solve_mixed(self, n_ev: int = 6, iterations: int = 300, reorth_every: int = 20, seed: int = 1,
+                    want_vectors: bool = False):
+        """Lowest eigenvalues with FP32 Krylov vectors (edg_solve_mixed).
+        Returns dict(eigs, ritz, residuals, evecs, stats)."""
+        k = min(n_ev, 32)
+        eigs = np.empty(k, np.float64)
+        ritz = np.empty(k, np.float64)
+        res = np.empty(k, np.float64)
+        evecs = np.empty((k, self.n_p), np.complex128) if want_vectors else None
+        opts = N.edg_mixed_opts(int(n_ev), int(iterations), int(reorth_every), int(seed), int(bool(want_vectors)))
+        n_out = C.c_int64()
+        st = N.edg_mixed_stats()
+        N.check(N.lib().edg_solve_mixed(self._h, C.byref(opts), eigs.ctypes.data, ritz.ctypes.data, res.ctypes.data,
+                                        C.byref(n_out), evecs.ctypes.data if want_vectors else None, C.byref(st)))
+        n = n_out.value
+        return {"eigs": eigs[:n], "ritz": ritz[:n], "residuals": res[:n],
+                "evecs": evecs[:n] if want_vectors else None,
+                "stats": {f: getattr(st, f) for f, _ in N.edg_mixed_stats._fields_}}
+
     def count_offdiag(self) -> int:
         n = C.c_int64()
         N.check(N.lib().edg_count_offdiag(self._h, C.byref(n)))
@@ -129,10 +167,15 @@ class GpuSector:
 
     def algorithmic_bytes(self, elem_bytes: int, nnz_off: Optional[int] = None) -> int:
         """Bytes one H*v must move at minimum: per row the representative (8),
-        the stabiliser byte (1), v_i and w_i; per off-diagonal target one v_j."""
+        the stabiliser byte (1), v_i and w_i; per off-diagonal target one v_j.
+        With stored targets add their 4-byte words, the 8-byte row offset and
+        the u = v/norm pass (read v and the stabiliser byte, write u)."""
         if nnz_off is None:
             nnz_off = self.count_offdiag()
-        return self.n_p * (8 + 1 + 2 * elem_bytes) + nnz_off * elem_bytes
+        b = self.n_p * (8 + 1 + 2 * elem_bytes) + nnz_off * elem_bytes
+        if self.info.get("n_targets", 0):
+            b += 4 * self.info["n_targets"] + 8 * self.n_p + self.n_p * (2 * elem_bytes + 1)
+        return b
 
     def close(self) -> None:
         if getattr(self, "_h", None):

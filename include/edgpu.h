@@ -64,6 +64,7 @@ typedef struct {
   int64_t n_p;           /* sector dimension */
   int64_t n_configs;     /* C(N, n_ones) */
   int64_t device_bytes;  /* device memory held by the sector */
+  int64_t n_targets;     /* stored target words (0: H*v searches on the fly) */
 } edg_sector_info;
 
 const char* edg_last_error(void);
@@ -98,6 +99,19 @@ int edg_sector_copy_config_tables(const edg_sector* s, int64_t max_configs, int6
  * stream).  v and w must not overlap.
  * Replaces: sHv (H_v.cpp:192-357, declared H_v.h:36-57). */
 int edg_hv(edg_sector* s, const void* v, void* w, int dtype, void* stream);
+
+/* Search every row's flipped states once and keep the result in HBM: one
+ * 32-bit word per (row, anti-aligned pair) holding the representative's
+ * position and phase class (4 bytes x ~55 pairs per row; 56 GB for the
+ * 36-site Sz=0 sector).  Afterwards edg_hv streams these words instead of
+ * searching; coefficients are still computed from the state bits.  Fails with
+ * EDG_ERR_NOMEM (sector unchanged) when the words need more than max_bytes
+ * (<= 0: no limit) or than is free.  Calls on one sector must not overlap:
+ * the H*v keeps a scratch vector in the sector.  No reference counterpart:
+ * the reference precomputes per-configuration tables instead
+ * (Momentum_Basis.cpp:750-777). */
+int edg_sector_build_targets(edg_sector* s, int64_t max_bytes);
+int edg_sector_free_targets(edg_sector* s);
 
 /* Same with host buffers: copies v in, applies H, copies w out, synchronises.
  * This is the call the reference's sHv(v, w, ...) adapter makes. */
@@ -135,6 +149,34 @@ typedef struct {
  * eigenvectors of n_p complex128 entries each, in the same order. */
 int edg_solve_plain(edg_sector* s, const edg_solver_opts* opts, double* eigs, int64_t eigs_capacity,
                     int64_t* n_eigs, double* evecs, int64_t evecs_capacity, edg_solver_stats* stats);
+
+/* Options of the mixed-precision solver. */
+typedef struct {
+  int n_ev;                 /* lowest eigenvalues wanted (at most 32) */
+  int iterations;           /* Lanczos steps (2 .. 2000) */
+  int reorth_every;         /* > 0: keep every FP32 Krylov vector and reorthogonalise
+                               against all of them every reorth_every steps;
+                               0: three resident vectors, Ritz vectors by a second pass */
+  uint64_t seed;            /* start vector: splitmix64 stream */
+  int want_vectors;         /* copy the FP64 eigenvectors out */
+} edg_mixed_opts;
+
+typedef struct {
+  int64_t hv_calls;         /* FP32 H*v (both passes) plus one FP64 H*v per Ritz vector */
+  double hv_seconds, total_seconds;
+  int passes;
+} edg_mixed_stats;
+
+/* Lowest eigenvalues with FP32 Krylov vectors and FP32 H*v; FP64 for alpha/beta
+ * (compensated sums), reorthogonalisation coefficients, the tridiagonal
+ * eigensolve (on the GPU) and one FP64 H*v per Ritz vector.  Copies of
+ * converged eigenvalues that lost orthogonality produces are removed, so each
+ * level is returned once.  eigs: FP64 Rayleigh quotients; ritz: the Ritz
+ * values of T; residuals: |Hx - eig x|/|x| in FP64; evecs (NULL allowed):
+ * n_ev x n_p complex128.  No reference counterpart: the reference keeps every
+ * Krylov vector in FP64 (lanczos.cpp:241), which does not fit at N = 36. */
+int edg_solve_mixed(edg_sector* s, const edg_mixed_opts* opts, double* eigs, double* ritz, double* residuals,
+                    int64_t* n_eigs, double* evecs, edg_mixed_stats* stats);
 
 /* Deterministic complex test vector (splitmix64, entries uniform in [-1,1)^2)
  * written to device memory; the same generator as the test suite's. */

@@ -78,6 +78,51 @@ def test_hv_matches_reference(gpu, name, idx, dtype):
             assert abs(np.vdot(w, w).real - g[f"{tag}_w{k}_norm2"][0]) <= 100 * tol * g[f"{tag}_w{k}_norm2"][0]
 
 
+@pytest.mark.parametrize("name,idx", all_golden_sectors(max_configs=3_000_000))
+def test_hv_stored_targets_match_reference(gpu, name, idx):
+    """H*v streaming the stored search results equals the reference's sHv."""
+    meta = golden_cases()[name]["sectors"][idx]
+    sec = gpu.GpuSector(golden_model(name, idx))
+    model_has_chch = golden_model(name, idx).ChCh != 0.0
+    if model_has_chch:
+        from ed_code_gb300._native import EdgError
+
+        with pytest.raises(EdgError):
+            sec.build_targets()
+        return
+    assert sec.build_targets()
+    assert sec.info["n_targets"] > 0
+    g = golden_arrays(name)
+    tag = f"s{idx}"
+    for dtype, tol in ((np.complex128, FP64_TOL), (np.complex64, FP32_TOL)):
+        for k, seed in enumerate(meta["vec_seeds"]):
+            v = O.splitmix_vector(sec.n_p, seed)
+            w = sec.sHv(v.astype(dtype), dtype=dtype).astype(np.complex128)
+            if meta["full"]:
+                ref = g[f"{tag}_w{k}"]
+                assert np.abs(w - ref).max() / max(1.0, np.abs(ref).max()) <= tol
+            else:
+                rows = g[f"{tag}_rows"]
+                ref = g[f"{tag}_w{k}_at_rows"]
+                assert np.abs(w[rows] - ref).max() / max(1.0, np.abs(ref).max()) <= tol
+
+
+def test_stored_targets_equal_matrix_free(gpu):
+    """Both H*v kernels give the same vector (FP64) on a torus with chirality and J2."""
+    from ed_code_gb300 import lattice as L
+
+    model = L.make_model(L.TorusSpec("triangular", 5, 4, Jz=1.1, J2=0.3, Ch=0.2), 0, 2, 1)
+    sec = gpu.GpuSector(model)
+    v = O.splitmix_vector(sec.n_p, 21)
+    w0 = sec.sHv(v)
+    assert sec.build_targets()
+    w1 = sec.sHv(v)
+    assert np.abs(w1 - w0).max() <= 1e-13 * max(1.0, np.abs(w0).max())
+    sec.free_targets()
+    assert sec.info["n_targets"] == 0
+    assert np.array_equal(sec.sHv(v), w0)
+
+
 def test_hv_device_equals_host(gpu):
     import torch
 
@@ -153,6 +198,11 @@ def large_sector_check(gpu, spec, Sz, kx, ky, n_rows=512, seed=9):
     assert np.abs(w[rows] - ref).max() / scale <= FP64_TOL
     w32 = sec.sHv(v.astype(np.complex64), dtype=np.complex64)
     assert np.abs(w32[rows] - ref).max() / scale <= FP32_TOL
+    # the stored-target kernel on the same sector
+    assert sec.build_targets()
+    ws = sec.sHv(v)
+    assert np.abs(ws[rows] - ref).max() / scale <= FP64_TOL
+    sec.free_targets()
     # Hermiticity as a size-independent property: <u|H v> = conj(<v|H u>)
     u = O.splitmix_vector(sec.n_p, seed + 1)
     hu = sec.sHv(u)
