@@ -6,9 +6,12 @@
 //    reduced in FP64 with compensated (Neumaier) sums over the FP32 vectors,
 //    on the device, so a step needs no host round trip;
 //  * reorth_every > 0 keeps every Krylov vector (FP32) and, every
-//    reorth_every steps, orthogonalises the new vector against all of them
-//    twice (classical Gram-Schmidt with FP64 coefficients); reorth_every = 0
-//    keeps three vectors resident (the 36-site case: 2 GB each);
+//    reorth_every steps, orthogonalises the last two vectors against all of
+//    them, twice (classical Gram-Schmidt with FP64 coefficients).  With FP32
+//    vectors orthogonality decays within a few steps once a level converges:
+//    every step (1) or every few steps keeps T exact; every 20 steps does not;
+//    reorth_every = 0 keeps three vectors resident (the 36-site case: 2 GB
+//    each) and removes the copies of converged levels afterwards;
 //  * T's lowest eigenvalues by bisection and their eigenvectors by inverse
 //    iteration, in FP64 in one CTA on the GPU; Ritz values that T shares with
 //    T-without-its-first-row are copies produced by lost orthogonality and are
@@ -138,9 +141,8 @@ __global__ void __launch_bounds__(kRedThreads) k_step(float2* __restrict__ w, co
   }
 }
 
-// dst = src / beta
-__global__ void k_scale_inv(float2* __restrict__ dst, const float2* __restrict__ src, const double* __restrict__ beta,
-                            int64_t n) {
+// dst = src / beta (dst may be src)
+__global__ void k_scale_inv(float2* dst, const float2* src, const double* __restrict__ beta, int64_t n) {
   const double s = 1.0 / *beta;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const float2 x = src[i];
@@ -240,15 +242,20 @@ __global__ void k_tridiag(const double* __restrict__ alpha, const double* __rest
     // Cullum-Willoughby: a simple eigenvalue of T that T-hat also has is a copy.
     double scale = 0;
     for (int i = 0; i < m; ++i) scale = fmax(scale, fabs(d[i]) + fabs(e[i]) + (i + 1 < m ? fabs(e[i + 1]) : 0.0));
-    const double tol = 1e-10 * fmax(scale, 1.0);
+    scale = fmax(scale, 1.0);
+    // Copies of a converged level built from FP32 vectors agree only to about
+    // the FP32 backward error, ~1e-7 |T|; T and T-hat share a spurious value to
+    // FP64 accuracy.
+    const double tol_cluster = 1e-7 * scale, tol_hat = 1e-10 * scale;
     int na = 0;
     for (int k = 0; k < nc && na < want; ++k) {
-      const bool multiple = (k > 0 && fabs(theta[k] - theta[k - 1]) < tol) || (k + 1 < nc && fabs(theta[k + 1] - theta[k]) < tol);
+      const bool prev_close = k > 0 && fabs(theta[k] - theta[k - 1]) < tol_cluster;
+      const bool next_close = k + 1 < nc && fabs(theta[k + 1] - theta[k]) < tol_cluster;
       bool in_hat = false;
       for (int q = 0; q < min(kCand, m - 1); ++q)
-        if (fabs(theta_hat[q] - theta[k]) < tol) in_hat = true;
-      if (in_hat && !multiple) continue;                         // spurious copy
-      if (multiple && k > 0 && fabs(theta[k] - theta[k - 1]) < tol) continue;  // keep one per cluster
+        if (fabs(theta_hat[q] - theta[k]) < tol_hat) in_hat = true;
+      if (in_hat && !prev_close && !next_close) continue;  // spurious copy
+      if (prev_close) continue;                            // keep one per cluster
       accepted[na++] = k;
     }
     *n_acc = na;
@@ -301,7 +308,7 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
   if ((e = D.alloc(&w, (size_t)n)) != cudaSuccess) return fail(EDG_ERR_NOMEM, "mixed Lanczos: w");
   const int64_t kparts = (int64_t)std::max(m + 1, 4) * kRedBlocks * 2;
   if ((e = D.alloc(&alpha, m + 1)) != cudaSuccess || (e = D.alloc(&beta, m + 2)) != cudaSuccess ||
-      (e = D.alloc(&part, kparts)) != cudaSuccess || (e = D.alloc(&scal, 2 * (m + 2))) != cudaSuccess ||
+      (e = D.alloc(&part, kparts)) != cudaSuccess || (e = D.alloc(&scal, 2 * (m + 2) + 2)) != cudaSuccess ||
       (e = D.alloc(&theta, kCand)) != cudaSuccess || (e = D.alloc(&theta_hat, kCand)) != cudaSuccess ||
       (e = D.alloc(&y, (size_t)kMaxEv * m)) != cudaSuccess || (e = D.alloc(&work, (size_t)kMaxEv * 5 * m)) != cudaSuccess ||
       (e = D.alloc(&acc, kMaxEv)) != cudaSuccess || (e = D.alloc(&nacc, 1)) != cudaSuccess)
@@ -340,16 +347,26 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
       }
       k_step<<<kRedBlocks, kRedThreads, 0, st>>>(w, vec(j), j > 0 ? vec(j - 1) : nullptr, alpha + j, beta + j, n, part);
       if (!second && store && ((j + 1) % o.reorth_every == 0)) {
-        // periodic full reorthogonalisation of w against v_0..v_j, twice
-        for (int pass = 0; pass < 2; ++pass) {
-          const int K = j + 1;
-          for (int k0 = 0; k0 < K; k0 += 512) {
-            const int kk = std::min(512, K - k0);
-            k_dot32<<<dim3(kRedBlocks, kk), kRedThreads, 0, st>>>(V + (int64_t)k0 * n, n, w, n, part);
-            k_finish<<<kk, kRedThreads, 0, st>>>(part, kRedBlocks, scal, 0);
-            k_sub32<<<grid_n(n), 256, sizeof(double) * 2 * kk, st>>>(w, V + (int64_t)k0 * n, n, scal, kk, n);
-          }
+        // Periodic reorthogonalisation in its two-vector form: between two
+        // reorthogonalisations v_j has drifted too, so it is cleaned against
+        // v_0..v_{j-1} first, then w against v_0..v_j; each classical
+        // Gram-Schmidt pass runs twice.  (Cleaning w alone lets the
+        // recurrence carry v_j's error into every later vector.)
+        auto cgs2 = [&](float2* x, int K) {
+          for (int pass = 0; pass < 2; ++pass)
+            for (int k0 = 0; k0 < K; k0 += 512) {
+              const int kk = std::min(512, K - k0);
+              k_dot32<<<dim3(kRedBlocks, kk), kRedThreads, 0, st>>>(V + (int64_t)k0 * n, n, x, n, part);
+              k_finish<<<kk, kRedThreads, 0, st>>>(part, kRedBlocks, scal, 0);
+              k_sub32<<<grid_n(n), 256, sizeof(double) * 2 * kk, st>>>(x, V + (int64_t)k0 * n, n, scal, kk, n);
+            }
+        };
+        if (o.reorth_every > 1 && j > 0) {
+          cgs2(vec(j), j);
+          norm_into(vec(j), scal + 2 * (m + 1));
+          k_scale_inv<<<grid_n(n), 256, 0, st>>>(vec(j), vec(j), scal + 2 * (m + 1), n);
         }
+        cgs2(w, j + 1);
         norm_into(w, beta + j + 1);
       } else if (!second) {
         k_finish<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, beta + j + 1, 2);
@@ -363,7 +380,8 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
   if ((e = run(false, nullptr, 0, {})) != cudaSuccess) return cuda_fail(e, "mixed Lanczos");
   // eigenvalues and Ritz coefficients of T on the device
   const size_t tsh = sizeof(double) * 2 * m;
-  k_tridiag<<<1, 128, tsh, st>>>(alpha, beta, m, want, theta, theta_hat, y, work, acc, nacc);
+  const int n_try = std::min(kMaxEv, std::min(want + 4, m));
+  k_tridiag<<<1, 128, tsh, st>>>(alpha, beta, m, n_try, theta, theta_hat, y, work, acc, nacc);
   int na = 0;
   std::vector<int> acc_h(kMaxEv);
   std::vector<double> th(kCand), yh;
@@ -394,7 +412,11 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
     passes = 2;
     if ((e = run(true, X, na, yh)) != cudaSuccess) return cuda_fail(e, "mixed Lanczos: second pass");
   }
-  // FP64 Rayleigh quotient and residual of each Ritz vector
+  // FP64 Rayleigh quotient and residual of each Ritz vector; a Rayleigh
+  // quotient within 1e-8 relative of an earlier one is the same level again
+  // (a copy that slipped through) and is dropped.
+  std::vector<double> rq_all(na), res_all(na), ritz_all(na);
+  std::vector<int> keep;
   for (int q = 0; q < na; ++q) {
     double2* x = X + (int64_t)q * n;
     if ((e = launch_hv(S, x, HX, true, st)) != cudaSuccess) return cuda_fail(e, "mixed Lanczos: FP64 H*v");
@@ -414,9 +436,18 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "mixed Lanczos: residual");
     double r2 = 0;
     for (int b = 0; b < kRedBlocks; ++b) r2 += p[3 * b + 2];
-    eigs[q] = rq;
-    if (ritz) ritz[q] = th[acc_h[q]];
-    if (resid) resid[q] = std::sqrt(r2 / nx);
+    rq_all[q] = rq;
+    res_all[q] = std::sqrt(r2 / nx);
+    ritz_all[q] = th[acc_h[q]];
+    bool dup = false;
+    for (int k : keep)
+      if (std::fabs(rq_all[k] - rq) <= 1e-8 * std::fabs(rq)) dup = true;
+    if (dup || (int)keep.size() >= want) continue;
+    const int slot = (int)keep.size();
+    keep.push_back(q);
+    eigs[slot] = rq;
+    if (ritz) ritz[slot] = ritz_all[q];
+    if (resid) resid[slot] = res_all[q];
     if (evecs) {
       // normalised FP64 eigenvector to the host
       std::vector<double2> hx(n);
@@ -424,12 +455,12 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
       if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "mixed Lanczos: vectors");
       const double s = 1.0 / std::sqrt(nx);
       for (int64_t i = 0; i < n; ++i) {
-        evecs[2 * ((int64_t)q * n + i)] = hx[i].x * s;
-        evecs[2 * ((int64_t)q * n + i) + 1] = hx[i].y * s;
+        evecs[2 * ((int64_t)slot * n + i)] = hx[i].x * s;
+        evecs[2 * ((int64_t)slot * n + i) + 1] = hx[i].y * s;
       }
     }
   }
-  *n_out = na;
+  *n_out = (int64_t)keep.size();
   if (stats) {
     stats->hv_calls = hv_calls + na;
     stats->hv_seconds = t_hv;

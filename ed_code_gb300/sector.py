@@ -141,7 +141,7 @@ class GpuSector:
         stats = {f: getattr(st, f) for f, _ in N.edg_solver_stats._fields_}
         return eigs[: n_out.value], evecs, stats
 
-    def solve_mixed(self, n_ev: int = 6, iterations: int = 300, reorth_every: int = 20, seed: int = 1,
+    def solve_mixed(self, n_ev: int = 6, iterations: int = 300, reorth_every: int = 1, seed: int = 1,
                     want_vectors: bool = False):
         """Lowest eigenvalues with FP32 Krylov vectors (edg_solve_mixed).
         Returns dict(eigs, ritz, residuals, evecs, stats)."""

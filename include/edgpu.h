@@ -154,8 +154,9 @@ int edg_solve_plain(edg_sector* s, const edg_solver_opts* opts, double* eigs, in
 typedef struct {
   int n_ev;                 /* lowest eigenvalues wanted (at most 32) */
   int iterations;           /* Lanczos steps (2 .. 2000) */
-  int reorth_every;         /* > 0: keep every FP32 Krylov vector and reorthogonalise
-                               against all of them every reorth_every steps;
+  int reorth_every;         /* > 0: keep every FP32 Krylov vector and reorthogonalise the
+                               last two against all of them every reorth_every steps
+                               (1 or a few: FP32 vectors lose orthogonality fast);
                                0: three resident vectors, Ritz vectors by a second pass */
   uint64_t seed;            /* start vector: splitmix64 stream */
   int want_vectors;         /* copy the FP64 eigenvectors out */
