@@ -626,9 +626,7 @@ int edg_sector_build_targets(edg_sector* s, int64_t max_bytes) {
 
 int edg_sector_free_targets(edg_sector* s) {
   if (!s) return fail(EDG_ERR_INVALID, "NULL sector");
-  const int64_t before = s->s.P.n_targets;
   free_targets(s->s);
-  s->s.device_bytes -= 4 * before + 8 * s->s.P.n_p + 16 * s->s.P.n_p;
   cudaMemcpy(s->s.dP, &s->s.P, sizeof(SectorParams), cudaMemcpyHostToDevice);
   return EDG_OK;
 }

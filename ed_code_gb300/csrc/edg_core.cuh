@@ -114,11 +114,10 @@ struct SectorParams {
   double chi_re[64], chi_im[64];
   // Torus search tables (row length Lx = L1, Ly = L2 rows).
   uint64_t rot_hi[kMaxTorusRow], rot_lo[kMaxTorusRow];  // per-row masks of bits x >= a / x < a
-  // Stored targets (see targets in hv.cu): phase class of each translation g
-  // and the phase of each class; an entry is j | class << jbits.
-  double cph_re[64], cph_im[64];
+  // Stored targets (targets.cu): phase class of each translation g, number
+  // of classes, value-table offset of each group, number of stored targets.
   uint8_t g2cls[64];
-  int jbits, cbits;
+  int n_cls, pad2;
   int64_t n_targets;
 };
 

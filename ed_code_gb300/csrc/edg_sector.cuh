@@ -87,10 +87,16 @@ struct Sector {
   // H*v kernel: 0 = hv.cu (default), 1 = hv_torus.cu when the sector has a
   // torus plan.  Chosen at sector creation from EDG_HV_VARIANT (for A/B timing).
   int hv_variant = 0;
-  // stored targets: one u32 per (row, anti-aligned pair), rows at row_ptr
-  uint32_t* tgt = nullptr;
-  uint64_t* row_ptr = nullptr;
-  DeviceBuffer ubuf;  // v_j / norm_j scratch for the stored-target H*v
+  // stored targets (targets.cu): CSR rows of (column, value id)
+  uint64_t* row_ptr = nullptr;  // n_p + 1
+  uint32_t* col = nullptr;
+  uint16_t* vid = nullptr;
+  double* ezz = nullptr;        // diagonal of each row
+  double2* vtab64 = nullptr;    // value table: pair coefficient x phase class
+  float2* vtab32 = nullptr;
+  int n_vals = 0;
+  DeviceBuffer ubuf;            // u = v / norm scratch
+  size_t targets_bytes = 0;
 };
 
 // basis.cu

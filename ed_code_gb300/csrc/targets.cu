@@ -1,28 +1,30 @@
-// Stored targets: the orbit search of H*v done once per sector.
+// Stored targets: the orbit search of H*v done once per sector, the result
+// kept in HBM as compressed sparse rows.
 //
-// For every row i and every anti-aligned flip group of its state (in the
-// fixed order of the groups), one 32-bit word is kept in HBM:
-//     entry = j | cls << jbits      (j: position of the flipped state's
-//                                    representative, cls: its phase class)
-// or 0xFFFFFFFF when the representative is not an allowed state.  Row i's
-// words start at row_ptr[i]; their count is the number of anti-aligned
-// groups of reps[i], which the H*v recomputes from the state.
+// For row i, every anti-aligned flip group g whose flipped state has an
+// allowed representative j contributes one stored entry
+//     col = j                         (u32)
+//     vid = (off[g] + variant) * n_cls + cls        (u16)
+// where `variant` packs bit a of the state and the bits z of the group's
+// chirality terms (the inputs of the coefficient, H_v.cpp:232-303) and `cls`
+// is the phase class of the translation to the representative.  The value
+// table vtab[vid] = coefficient(g, variant) * phase(cls) is built on the host
+// from the same term lists.  Rows also keep their diagonal Ezz.
 //
-// H*v then streams these words (coalesced: one warp per row, lane k handles
-// the row's k-th word) and computes everything else on the fly from the state
-// bits -- the bond and chirality coefficients (H_v.cpp:219-303), the diagonal
-// Ezz, the phase from a per-class table -- exactly as the matrix-free kernel
-// does.  The norm ratio norm_i/norm_j is split: u_j = v_j / norm_j is formed
-// by a streaming pass before the row loop, norm_i multiplies the row sum.
-//
-// Memory: 4 bytes per (row, anti-aligned pair), 56 GB for the 36-site Sz=0
-// sector, plus 8 bytes per row for row_ptr.
+// H*v is then a CSR SpMV with a value dictionary (one warp per row, lanes
+// over the row's entries):
+//     w_i = norm_i * sum_t vtab[vid_t] * u[col_t] + Ezz_i * v_i,
+//     u_j = v_j / norm_j (a streaming pass before the row loop).
+// This stores the Hamiltonian's structure (6 bytes per nonzero, 84 GB for the
+// 36-site Sz=0 sector) instead of searching orbits every H*v; the matrix-free
+// kernels (hv.cu) remain for sectors whose entries do not fit.  The reference
+// has the same trade as an option of its own (sHv on an sMatrix, H_v.cpp:3-19).
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
+#include <complex>
 #include <cstddef>
-#include <iterator>
-#include <numeric>
 #include <string>
 #include <vector>
 
@@ -34,11 +36,12 @@ namespace {
 
 constexpr int kWarpsPerBlock = 8;
 constexpr int kTgtThreads = 32 * kWarpsPerBlock;
+constexpr int kMaxChPerGroup = 4;
 
 // anti-aligned groups of state s, 32 at a time: bit l of word r is group 32r+l
-template <typename Real, int NW>
-__device__ __forceinline__ void anti_words(uint64_t s, const HvSmem<Real>& H, int ng, uint32_t (&words)[NW],
-                                           Real& fac_lane) {
+template <int NW>
+__device__ __forceinline__ void anti_words(uint64_t s, const HvSmem<double>& H, int ng, uint32_t (&words)[NW],
+                                           double& fac_lane) {
   const int lane = threadIdx.x & 31;
 #pragma unroll
   for (int r = 0; r < NW; ++r) {
@@ -78,24 +81,73 @@ __device__ __forceinline__ int total(const uint32_t (&words)[NW]) {
   return n;
 }
 
-// number of anti-aligned groups per row
-__global__ void __launch_bounds__(kTgtThreads) k_tgt_count(SectorView V, uint32_t* __restrict__ counts) {
+// Pass 1 (count) and pass 2 (fill) share this walk over a row's targets: one
+// warp per row, lane k resolves the row's k-th anti-aligned pair.
+template <bool kTorus, int NW, bool kFill>
+__global__ void __launch_bounds__(kTgtThreads) k_tgt_pass(SectorView V, const uint16_t* __restrict__ voff,
+                                                          uint32_t* __restrict__ counts, double* __restrict__ ezz,
+                                                          const uint64_t* __restrict__ row_ptr,
+                                                          uint32_t* __restrict__ col, uint16_t* __restrict__ vid) {
   __shared__ SectorParams P;
-  __shared__ uint64_t masks[kMaxGroups];
+  __shared__ uint16_t off[kMaxGroups];
+  extern __shared__ __align__(16) uint8_t sm[];
   for (int i = threadIdx.x; i < (int)(sizeof(SectorParams) / 8); i += blockDim.x)
     reinterpret_cast<uint64_t*>(&P)[i] = reinterpret_cast<const uint64_t*>(V.params)[i];
   __syncthreads();
-  for (int g = threadIdx.x; g < P.n_groups; g += blockDim.x) masks[g] = V.groups[g].mask;
+  for (int g = threadIdx.x; g < P.n_groups; g += blockDim.x) off[g] = voff[g];
+  const HvSmem<double> H = stage_hv<double, kTorus>(V, P, sm);
   __syncthreads();
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < P.n_p; i += (int64_t)gridDim.x * blockDim.x) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t lt = (1u << lane) - 1u;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t i = warp; i < P.n_p; i += n_warps) {
     const uint64_t s = V.reps[i];
-    uint32_t c = 0;
-    for (int g = 0; g < P.n_groups; ++g) c += (popc64(s & masks[g]) == 1);
-    counts[i] = c;
+    uint32_t words[NW];
+    double fac = 0.0;
+    anti_words<NW>(s, H, P.n_groups, words, fac);
+    const int nt = total(words);
+    uint64_t pos = kFill ? row_ptr[i] : 0;
+    uint32_t cnt = 0;
+    for (int k0 = 0; k0 < nt; k0 += 32) {
+      const int k = k0 + lane;
+      bool ok = false;
+      uint32_t j = 0;
+      uint16_t id = 0;
+      if (k < nt) {
+        const int g = select_group(words, k);
+        const SmemGroup<double>& gr = H.groups[g];
+        Orbit o;
+        const int64_t jj = locate<double, kTorus>(s ^ gr.mask, V, P, H, o);
+        if (jj >= 0) {
+          ok = true;
+          j = (uint32_t)jj;
+          int variant = (int)((s >> gr.a) & 1u);
+          for (int m = gr.ch_begin, b = 1; m < gr.ch_end; ++m, ++b) variant |= (int)((s >> H.ch[m].z) & 1u) << b;
+          id = (uint16_t)((off[g] + variant) * P.n_cls + P.g2cls[o.g]);
+        }
+      }
+      const uint32_t bal = __ballot_sync(0xffffffffu, ok);
+      if (kFill && ok) {
+        const uint64_t t = pos + __popc(bal & lt);
+        col[t] = j;
+        vid[t] = id;
+      }
+      pos += __popc(bal);
+      cnt += __popc(bal);
+    }
+    if (!kFill) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) fac += __shfl_down_sync(0xffffffffu, fac, o);
+      if (lane == 0) {
+        counts[i] = cnt;
+        ezz[i] = P.total_fac - 2.0 * fac;  // Ezz = sum_bonds lJ/4 - 2 sum_anti lJ/4
+      }
+    }
   }
 }
 
-// 64-bit exclusive scan: chunk sums, one CTA over the chunk sums, apply
+// 64-bit exclusive scan of the counts into row_ptr[0..n] (row_ptr[n] = total)
 constexpr int kScan = 256, kScanPer = 16, kChunk = kScan * kScanPer;
 
 __device__ __forceinline__ unsigned long long block_scan64(unsigned long long x, unsigned long long* tot) {
@@ -155,6 +207,7 @@ __global__ void __launch_bounds__(kScan) k_scan64_sums(unsigned long long* __res
 
 __global__ void __launch_bounds__(kScan) k_scan64_apply(const uint32_t* __restrict__ in, int64_t n,
                                                          const unsigned long long* __restrict__ offs,
+                                                         const unsigned long long* __restrict__ total,
                                                          uint64_t* __restrict__ out) {
   const int64_t b = (int64_t)blockIdx.x * kChunk + (int64_t)threadIdx.x * kScanPer;
   unsigned long long s = 0;
@@ -167,36 +220,7 @@ __global__ void __launch_bounds__(kScan) k_scan64_apply(const uint32_t* __restri
       out[b + k] = run;
       run += in[b + k];
     }
-}
-
-// one warp per row: search every anti-aligned target once, store its word
-template <bool kTorus, int NW>
-__global__ void __launch_bounds__(kTgtThreads) k_tgt_fill(SectorView V, const uint64_t* __restrict__ row_ptr,
-                                                          uint32_t* __restrict__ tgt) {
-  __shared__ SectorParams P;
-  extern __shared__ __align__(16) uint8_t sm[];
-  for (int i = threadIdx.x; i < (int)(sizeof(SectorParams) / 8); i += blockDim.x)
-    reinterpret_cast<uint64_t*>(&P)[i] = reinterpret_cast<const uint64_t*>(V.params)[i];
-  __syncthreads();
-  const HvSmem<float> H = stage_hv<float, kTorus>(V, P, sm);
-  __syncthreads();
-  const int lane = threadIdx.x & 31;
-  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t i = warp; i < P.n_p; i += n_warps) {
-    const uint64_t s = V.reps[i];
-    uint32_t words[NW];
-    float fac = 0.f;
-    anti_words<float, NW>(s, H, P.n_groups, words, fac);
-    const int nt = total(words);
-    const uint64_t base = row_ptr[i];
-    for (int k = lane; k < nt; k += 32) {
-      const int g = select_group(words, k);
-      Orbit o;
-      const int64_t j = locate<float, kTorus>(s ^ H.groups[g].mask, V, P, H, o);
-      tgt[base + k] = j < 0 ? 0xFFFFFFFFu : (uint32_t)j | ((uint32_t)P.g2cls[o.g] << P.jbits);
-    }
-  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = *total;
 }
 
 template <typename Real>
@@ -222,75 +246,53 @@ __global__ void k_u_scale(const typename CT2<Real>::T* __restrict__ v, const uin
   }
 }
 
-// H*v from the stored targets: one warp per row
-template <typename Real, int NW>
-__global__ void __launch_bounds__(kTgtThreads) k_hv_stored(SectorView V, const uint64_t* __restrict__ row_ptr,
-                                                           const uint32_t* __restrict__ tgt,
-                                                           const typename CT2<Real>::T* __restrict__ v,
-                                                           const typename CT2<Real>::T* __restrict__ u,
-                                                           typename CT2<Real>::T* __restrict__ w) {
+// CSR SpMV with a value dictionary: one warp per row
+template <typename Real, bool kSmemTab>
+__global__ void __launch_bounds__(kTgtThreads) k_hv_csr(const uint64_t* __restrict__ row_ptr,
+                                                        const uint32_t* __restrict__ col,
+                                                        const uint16_t* __restrict__ vid,
+                                                        const typename CT2<Real>::T* __restrict__ vtab, int n_vals,
+                                                        const double* __restrict__ ezz,
+                                                        const uint8_t* __restrict__ lid,
+                                                        const double* __restrict__ nrm_tab, int64_t n_p,
+                                                        const typename CT2<Real>::T* __restrict__ v,
+                                                        const typename CT2<Real>::T* __restrict__ u,
+                                                        typename CT2<Real>::T* __restrict__ w) {
   using CT = typename CT2<Real>::T;
-  __shared__ SectorParams P;
-  __shared__ Real cph_re[64], cph_im[64];
   extern __shared__ __align__(16) uint8_t sm[];
-  for (int i = threadIdx.x; i < (int)(sizeof(SectorParams) / 8); i += blockDim.x)
-    reinterpret_cast<uint64_t*>(&P)[i] = reinterpret_cast<const uint64_t*>(V.params)[i];
-  __syncthreads();
-  for (int k = threadIdx.x; k < 64; k += blockDim.x) {
-    cph_re[k] = (Real)P.cph_re[k];
-    cph_im[k] = (Real)P.cph_im[k];
-  }
-  // only the group and chirality tables are needed here (no search)
-  const HvSmem<Real> H = stage_hv<Real, true>(V, P, sm);
+  __shared__ Real nrm[65];
+  CT* tab = reinterpret_cast<CT*>(sm);
+  for (int k = threadIdx.x; k < 65; k += blockDim.x) nrm[k] = (Real)nrm_tab[k];
+  if (kSmemTab)
+    for (int k = threadIdx.x; k < n_vals; k += blockDim.x) tab[k] = vtab[k];
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  const uint32_t jmask = (P.jbits >= 32) ? 0xFFFFFFFFu : ((1u << P.jbits) - 1u);
-  const bool use_ch = P.use_ch != 0;
-  for (int64_t i = warp; i < P.n_p; i += n_warps) {
-    const uint64_t s = __ldg(reinterpret_cast<const unsigned long long*>(V.reps) + i);
-    uint32_t words[NW];
-    Real anti = 0;
-    anti_words<Real, NW>(s, H, P.n_groups, words, anti);
-    const int nt = total(words);
-    const uint64_t base = __ldg(reinterpret_cast<const unsigned long long*>(row_ptr) + i);
-    Real accr = 0, acci = 0;
-    for (int k = lane; k < nt; k += 32) {
-      const uint32_t e = __ldg(tgt + base + k);
-      if (e == 0xFFFFFFFFu) continue;
-      const int g = select_group(words, k);
-      const SmemGroup<Real>& gr = H.groups[g];
-      const int cs = (int)((s >> gr.a) & 1u);
-      Real cr = gr.Bre[cs], ci = gr.Bim[cs];
-      if (use_ch) {
-        for (int m = gr.ch_begin; m < gr.ch_end; ++m) {
-          const SmemCh<Real>& c = H.ch[m];
-          const Real sg = ((s >> c.z) & 1u) ? Real(1) : Real(-1);
-          cr += sg * c.Are[cs];
-          ci += sg * c.Aim[cs];
-        }
-      }
-      const uint32_t cls = e >> P.jbits;
-      const Real pr = cph_re[cls], pi = cph_im[cls];
-      const Real er = cr * pr - ci * pi, ei = cr * pi + ci * pr;
-      const CT uj = u[e & jmask];
-      accr += er * uj.x - ei * uj.y;
-      acci += er * uj.y + ei * uj.x;
+  for (int64_t i = warp; i < n_p; i += n_warps) {
+    const uint64_t beg = __ldg(reinterpret_cast<const unsigned long long*>(row_ptr) + i);
+    const uint64_t end = __ldg(reinterpret_cast<const unsigned long long*>(row_ptr) + i + 1);
+    Real ar = 0, ai = 0;
+    for (uint64_t t = beg + lane; t < end; t += 32) {
+      const uint32_t j = __ldg(col + t);
+      const int id = __ldg(vid + t);
+      const CT c = kSmemTab ? tab[id] : __ldg(vtab + id);
+      const CT x = u[j];
+      ar += c.x * x.x - c.y * x.y;
+      ai += c.x * x.y + c.y * x.x;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      accr += __shfl_down_sync(0xffffffffu, accr, o);
-      acci += __shfl_down_sync(0xffffffffu, acci, o);
-      anti += __shfl_down_sync(0xffffffffu, anti, o);
+      ar += __shfl_down_sync(0xffffffffu, ar, o);
+      ai += __shfl_down_sync(0xffffffffu, ai, o);
     }
     if (lane == 0) {
       const CT vi = v[i];
-      const Real ni = H.nrm[__ldg(V.lid + i)];
-      const Real ezz = (Real)P.total_fac - Real(2) * anti;
+      const Real ni = nrm[lid[i]];
+      const Real d = (Real)ezz[i];
       CT out;
-      out.x = accr * ni + ezz * vi.x;
-      out.y = acci * ni + ezz * vi.y;
+      out.x = ar * ni + d * vi.x;
+      out.y = ai * ni + d * vi.y;
       w[i] = out;
     }
   }
@@ -310,19 +312,31 @@ int grid_for(K kernel, size_t smem, int64_t work, int threads) {
   return (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sms * per_sm));
 }
 
-template <typename Real, int NW>
-cudaError_t launch_stored_t(const Sector& S, const void* v, void* w, cudaStream_t st) {
+const double* params_field(const Sector& S, size_t offset) {
+  return reinterpret_cast<const double*>(reinterpret_cast<const char*>(S.dP) + offset);
+}
+
+template <typename Real>
+cudaError_t launch_csr_t(const Sector& S, const void* v, void* w, cudaStream_t st) {
   using CT = typename CT2<Real>::T;
   const int64_t n = S.P.n_p;
-  const size_t smem = hv_smem_bytes<Real>(S.P.n_groups, S.P.n_ch, true, S.V.row_bits, S.V.n_chunks);
-  const double* nrm_inv_dev =
-      reinterpret_cast<const double*>(reinterpret_cast<const char*>(S.dP) + offsetof(SectorParams, nrm_inv));
   k_u_scale<Real><<<(int)std::min<int64_t>((n + 255) / 256, 152 * 32), 256, 0, st>>>(
-      reinterpret_cast<const CT*>(v), S.lid, nrm_inv_dev, n, reinterpret_cast<CT*>(S.ubuf.ptr));
-  auto kern = k_hv_stored<Real, NW>;
-  const int grid = grid_for(kern, smem, n * 32, kTgtThreads);
-  kern<<<grid, kTgtThreads, smem, st>>>(S.V, S.row_ptr, S.tgt, reinterpret_cast<const CT*>(v),
-                                        reinterpret_cast<const CT*>(S.ubuf.ptr), reinterpret_cast<CT*>(w));
+      reinterpret_cast<const CT*>(v), S.lid, params_field(S, offsetof(SectorParams, nrm_inv)), n,
+      reinterpret_cast<CT*>(S.ubuf.ptr));
+  const CT* tab = reinterpret_cast<const CT*>(sizeof(Real) == 8 ? (const void*)S.vtab64 : (const void*)S.vtab32);
+  const size_t tab_bytes = sizeof(CT) * S.n_vals;
+  const double* nrm = params_field(S, offsetof(SectorParams, nrm));
+  if (tab_bytes <= 96 * 1024) {
+    auto kern = k_hv_csr<Real, true>;
+    kern<<<grid_for(kern, tab_bytes, n * 32, kTgtThreads), kTgtThreads, tab_bytes, st>>>(
+        S.row_ptr, S.col, S.vid, tab, S.n_vals, S.ezz, S.lid, nrm, n, reinterpret_cast<const CT*>(v),
+        reinterpret_cast<const CT*>(S.ubuf.ptr), reinterpret_cast<CT*>(w));
+  } else {
+    auto kern = k_hv_csr<Real, false>;
+    kern<<<grid_for(kern, 0, n * 32, kTgtThreads), kTgtThreads, 0, st>>>(
+        S.row_ptr, S.col, S.vid, tab, S.n_vals, S.ezz, S.lid, nrm, n, reinterpret_cast<const CT*>(v),
+        reinterpret_cast<const CT*>(S.ubuf.ptr), reinterpret_cast<CT*>(w));
+  }
   return cudaGetLastError();
 }
 
@@ -338,20 +352,27 @@ int64_t gcd64(int64_t a, int64_t b) {
 }  // namespace
 
 void free_targets(Sector& S) {
-  if (S.tgt) cudaFree(S.tgt);
-  if (S.row_ptr) cudaFree(S.row_ptr);
-  if (S.ubuf.ptr) cudaFree(S.ubuf.ptr);
-  S.tgt = nullptr;
+  void* ptrs[] = {S.row_ptr, S.col, S.vid, S.ezz, S.vtab64, S.vtab32, S.ubuf.ptr};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
   S.row_ptr = nullptr;
+  S.col = nullptr;
+  S.vid = nullptr;
+  S.ezz = nullptr;
+  S.vtab64 = nullptr;
+  S.vtab32 = nullptr;
+  S.n_vals = 0;
   S.ubuf = DeviceBuffer{};
   S.P.n_targets = 0;
+  S.device_bytes -= S.targets_bytes;
+  S.targets_bytes = 0;
 }
 
 // Returns EDG_OK, or a reason (EDG_ERR_NOMEM / EDG_ERR_UNSUPPORTED) with the
 // sector left on the matrix-free kernels.
 int build_targets(Sector& S, int64_t max_bytes, std::string& err) {
   SectorParams& P = S.P;
-  if (S.tgt) return EDG_OK;
+  if (S.col) return EDG_OK;
   if (P.use_chch) {
     err = "stored targets do not cover ChCh terms";
     return EDG_ERR_UNSUPPORTED;
@@ -360,21 +381,17 @@ int build_targets(Sector& S, int64_t max_bytes, std::string& err) {
     err = "stored targets need at most 256 flip groups";
     return EDG_ERR_UNSUPPORTED;
   }
+  // host copies of the term groups (for the value table)
+  std::vector<TermGroup> groups(P.n_groups);
+  std::vector<ChTerm> ch(P.n_ch);
+  cudaMemcpy(groups.data(), S.groups, sizeof(TermGroup) * groups.size(), cudaMemcpyDeviceToHost);
+  if (!ch.empty()) cudaMemcpy(ch.data(), S.ch, sizeof(ChTerm) * ch.size(), cudaMemcpyDeviceToHost);
   // phase classes: translation (a, b) has phase index (kx a L2 + ky b L1) mod G
   const int G = P.L1 * P.L2;
   const int64_t d = gcd64(gcd64((int64_t)P.kx * P.L2, (int64_t)P.ky * P.L1), G);
   const int n_cls = (int)(G / (d ? d : G));
-  int cbits = 0;
-  while ((1 << cbits) < n_cls) ++cbits;
-  int jbits = 0;
-  while (jbits < 63 && ((int64_t)1 << jbits) <= P.n_p) ++jbits;  // 2^jbits > n_p: room for the sentinel
-  if (jbits + cbits > 32) {
-    err = "position and phase class do not fit in 32 bits";
-    return EDG_ERR_UNSUPPORTED;
-  }
-  std::fill(std::begin(P.cph_re), std::end(P.cph_re), 0.0);
-  std::fill(std::begin(P.cph_im), std::end(P.cph_im), 0.0);
-  std::vector<char> seen(64, 0);
+  std::vector<std::complex<double>> cph(n_cls);
+  std::vector<char> seen(n_cls, 0);
   for (int b = 0; b < P.L2; ++b)
     for (int a = 0; a < P.L1; ++a) {
       const int g = a + P.L1 * b;
@@ -383,88 +400,143 @@ int build_targets(Sector& S, int64_t max_bytes, std::string& err) {
       P.g2cls[g] = (uint8_t)c;
       if (!seen[c]) {  // the first translation of a class gives its phase value
         seen[c] = 1;
-        P.cph_re[c] = P.ph_re[g];
-        P.cph_im[c] = P.ph_im[g];
+        cph[c] = std::complex<double>(P.ph_re[g], P.ph_im[g]);
       }
     }
-  P.jbits = jbits;
-  P.cbits = cbits;
+  P.n_cls = n_cls;
+  // value table: for each group, every (bit a, chirality z bits) variant
+  std::vector<uint16_t> voff(P.n_groups);
+  std::vector<double2> tab64;
+  int64_t n_var = 0;
+  for (int g = 0; g < P.n_groups; ++g) {
+    const int nch = groups[g].ch_end - groups[g].ch_begin;
+    if (nch > kMaxChPerGroup) {
+      err = "stored targets: more than 4 chirality terms on one pair";
+      return EDG_ERR_UNSUPPORTED;
+    }
+    if (n_var > 65535) break;
+    voff[g] = (uint16_t)n_var;
+    n_var += 2 << nch;
+  }
+  if (n_var * n_cls > 65536) {
+    err = "stored targets: more than 65536 distinct values";
+    return EDG_ERR_UNSUPPORTED;
+  }
+  tab64.resize(n_var * n_cls);
+  for (int g = 0; g < P.n_groups; ++g) {
+    const TermGroup& gr = groups[g];
+    const int nch = gr.ch_end - gr.ch_begin;
+    for (int variant = 0; variant < (2 << nch); ++variant) {
+      const int cs = variant & 1;
+      std::complex<double> c(gr.Bre[cs], gr.Bim[cs]);
+      for (int q = 0; q < nch; ++q) {
+        const ChTerm& t = ch[gr.ch_begin + q];
+        const double sg = ((variant >> (q + 1)) & 1) ? 1.0 : -1.0;
+        c += sg * std::complex<double>(t.Are[cs], t.Aim[cs]);
+      }
+      for (int cl = 0; cl < n_cls; ++cl) {
+        const std::complex<double> val = c * cph[cl];
+        tab64[(voff[g] + variant) * n_cls + cl] = make_double2(val.real(), val.imag());
+      }
+    }
+  }
+  std::vector<float2> tab32(tab64.size());
+  for (size_t k = 0; k < tab64.size(); ++k) tab32[k] = make_float2((float)tab64[k].x, (float)tab64[k].y);
+
   cudaStream_t st = S.stream;
   const int64_t n = P.n_p;
   uint32_t* counts = nullptr;
+  uint16_t* d_voff = nullptr;
   unsigned long long *sums = nullptr, *tot = nullptr;
   const int64_t n_chunks = (n + kChunk - 1) / kChunk;
   cudaError_t e = cudaMemcpy(S.dP, &P, sizeof(P), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMalloc(&counts, sizeof(uint32_t) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&d_voff, sizeof(uint16_t) * voff.size());
   if (e == cudaSuccess) e = cudaMalloc(&sums, sizeof(unsigned long long) * n_chunks);
   if (e == cudaSuccess) e = cudaMalloc(&tot, sizeof(unsigned long long));
-  if (e == cudaSuccess) e = cudaMalloc(&S.row_ptr, sizeof(uint64_t) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&S.row_ptr, sizeof(uint64_t) * (n + 1));
+  if (e == cudaSuccess) e = cudaMalloc(&S.ezz, sizeof(double) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&S.vtab64, sizeof(double2) * tab64.size());
+  if (e == cudaSuccess) e = cudaMalloc(&S.vtab32, sizeof(float2) * tab32.size());
+  if (e == cudaSuccess) e = cudaMemcpy(d_voff, voff.data(), sizeof(uint16_t) * voff.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(S.vtab64, tab64.data(), sizeof(double2) * tab64.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(S.vtab32, tab32.data(), sizeof(float2) * tab32.size(), cudaMemcpyHostToDevice);
+  S.n_vals = (int)tab64.size();
   auto cleanup = [&]() {
     cudaFree(counts);
+    cudaFree(d_voff);
     cudaFree(sums);
     cudaFree(tot);
   };
   if (e != cudaSuccess) {
     cleanup();
     free_targets(S);
-    err = "stored targets: out of device memory for the row offsets";
+    err = "stored targets: out of device memory for the row data";
     return EDG_ERR_NOMEM;
   }
-  k_tgt_count<<<grid_for(k_tgt_count, 0, n, kTgtThreads), kTgtThreads, 0, st>>>(S.V, counts);
+  const bool torus = P.torus != 0;
+  const size_t smem = hv_smem_bytes<double>(P.n_groups, P.n_ch, torus, S.V.row_bits, S.V.n_chunks);
+  const int nw = n_words(P.n_groups);
+  auto pass = [&](auto kern, bool fill) {
+    kern<<<grid_for(kern, smem, n * 32, kTgtThreads), kTgtThreads, smem, st>>>(
+        S.V, d_voff, counts, S.ezz, S.row_ptr, fill ? S.col : nullptr, fill ? S.vid : nullptr);
+  };
+  if (torus) {
+    if (nw == 4) pass(k_tgt_pass<true, 4, false>, false);
+    else pass(k_tgt_pass<true, 8, false>, false);
+  } else {
+    if (nw == 4) pass(k_tgt_pass<false, 4, false>, false);
+    else pass(k_tgt_pass<false, 8, false>, false);
+  }
   k_scan64_chunks<<<(unsigned)n_chunks, kScan, 0, st>>>(counts, n, sums);
   k_scan64_sums<<<1, kScan, 0, st>>>(sums, n_chunks, tot);
-  k_scan64_apply<<<(unsigned)n_chunks, kScan, 0, st>>>(counts, n, sums, S.row_ptr);
-  unsigned long long n_tgt = 0;
-  e = cudaMemcpyAsync(&n_tgt, tot, sizeof(n_tgt), cudaMemcpyDeviceToHost, st);
+  k_scan64_apply<<<(unsigned)n_chunks, kScan, 0, st>>>(counts, n, sums, tot, S.row_ptr);
+  unsigned long long nnz = 0;
+  e = cudaMemcpyAsync(&nnz, tot, sizeof(nnz), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-  cleanup();
-  const int64_t elem = P.n_p * 16;  // u scratch, sized for FP64
   size_t free_b = 0, total_b = 0;
   cudaMemGetInfo(&free_b, &total_b);
-  const double need = 4.0 * (double)n_tgt + (double)elem;
+  const double need = 6.0 * (double)nnz + 16.0 * (double)n;
   if (e != cudaSuccess || need > (double)max_bytes || need > 0.9 * (double)free_b) {
+    cleanup();
     free_targets(S);
     err = e != cudaSuccess ? std::string("stored targets: ") + cudaGetErrorString(e)
                            : "stored targets do not fit in the allowed device memory";
     return e != cudaSuccess ? EDG_ERR_CUDA : EDG_ERR_NOMEM;
   }
-  e = cudaMalloc(&S.tgt, sizeof(uint32_t) * std::max<unsigned long long>(1, n_tgt));
-  if (e == cudaSuccess) e = cudaMalloc(&S.ubuf.ptr, (size_t)elem);
+  e = cudaMalloc(&S.col, sizeof(uint32_t) * std::max<unsigned long long>(1, nnz));
+  if (e == cudaSuccess) e = cudaMalloc(&S.vid, sizeof(uint16_t) * std::max<unsigned long long>(1, nnz));
+  if (e == cudaSuccess) e = cudaMalloc(&S.ubuf.ptr, (size_t)(16 * n));
   if (e != cudaSuccess) {
+    cleanup();
     free_targets(S);
     err = "stored targets: out of device memory";
     return EDG_ERR_NOMEM;
   }
-  S.ubuf.bytes = (size_t)elem;
-  const bool torus = P.torus != 0;
-  const size_t smem = hv_smem_bytes<float>(P.n_groups, P.n_ch, torus, S.V.row_bits, S.V.n_chunks);
-  const int nw = n_words(P.n_groups);
-  auto fill = [&](auto kern) {
-    kern<<<grid_for(kern, smem, n * 32, kTgtThreads), kTgtThreads, smem, st>>>(S.V, S.row_ptr, S.tgt);
-  };
+  S.ubuf.bytes = (size_t)(16 * n);
   if (torus) {
-    if (nw == 4) fill(k_tgt_fill<true, 4>);
-    else fill(k_tgt_fill<true, 8>);
+    if (nw == 4) pass(k_tgt_pass<true, 4, true>, true);
+    else pass(k_tgt_pass<true, 8, true>, true);
   } else {
-    if (nw == 4) fill(k_tgt_fill<false, 4>);
-    else fill(k_tgt_fill<false, 8>);
+    if (nw == 4) pass(k_tgt_pass<false, 4, true>, true);
+    else pass(k_tgt_pass<false, 8, true>, true);
   }
   e = cudaStreamSynchronize(st);
+  cleanup();
   if (e != cudaSuccess) {
     free_targets(S);
     err = std::string("stored targets: ") + cudaGetErrorString(e);
     return EDG_ERR_CUDA;
   }
-  P.n_targets = (int64_t)n_tgt;
-  S.device_bytes += sizeof(uint32_t) * n_tgt + sizeof(uint64_t) * n + elem;
+  P.n_targets = (int64_t)nnz;
+  S.targets_bytes = 6 * nnz + 8 * (n + 1) + 8 * n + 16 * n + 24 * tab64.size();
+  S.device_bytes += S.targets_bytes;
   e = cudaMemcpy(S.dP, &P, sizeof(P), cudaMemcpyHostToDevice);
   return e == cudaSuccess ? EDG_OK : EDG_ERR_CUDA;
 }
 
 cudaError_t launch_hv_stored(const Sector& S, const void* v, void* w, bool fp64, cudaStream_t st) {
-  const int nw = n_words(S.P.n_groups);
-  if (fp64) return nw == 4 ? launch_stored_t<double, 4>(S, v, w, st) : launch_stored_t<double, 8>(S, v, w, st);
-  return nw == 4 ? launch_stored_t<float, 4>(S, v, w, st) : launch_stored_t<float, 8>(S, v, w, st);
+  return fp64 ? launch_csr_t<double>(S, v, w, st) : launch_csr_t<float>(S, v, w, st);
 }
 
 }  // namespace edg

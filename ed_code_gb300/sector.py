@@ -166,16 +166,19 @@ class GpuSector:
         return int(n.value)
 
     def algorithmic_bytes(self, elem_bytes: int, nnz_off: Optional[int] = None) -> int:
-        """Bytes one H*v must move at minimum: per row the representative (8),
-        the stabiliser byte (1), v_i and w_i; per off-diagonal target one v_j.
-        With stored targets add their 4-byte words, the 8-byte row offset and
-        the u = v/norm pass (read v and the stabiliser byte, write u)."""
+        """Bytes one H*v must move at minimum.  Matrix-free: per row the
+        representative (8), the stabiliser byte (1), v_i and w_i; per
+        off-diagonal target one v_j.  Stored rows: see the comment below."""
         if nnz_off is None:
             nnz_off = self.count_offdiag()
-        b = self.n_p * (8 + 1 + 2 * elem_bytes) + nnz_off * elem_bytes
+        S = elem_bytes
         if self.info.get("n_targets", 0):
-            b += 4 * self.info["n_targets"] + 8 * self.n_p + self.n_p * (2 * elem_bytes + 1)
-        return b
+            # stored rows: v_i, stabiliser byte, w_i; per nonzero u32 column,
+            # u16 value id and one u_j; row offsets and diagonal; the u pass
+            nnz = self.info["n_targets"]
+            return (self.n_p * (2 * S + 1) + nnz * (S + 6) + 8 * (self.n_p + 1) + 8 * self.n_p
+                    + self.n_p * (2 * S + 1))
+        return self.n_p * (8 + 1 + 2 * S) + nnz_off * S
 
     def close(self) -> None:
         if getattr(self, "_h", None):

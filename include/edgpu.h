@@ -100,16 +100,16 @@ int edg_sector_copy_config_tables(const edg_sector* s, int64_t max_configs, int6
  * Replaces: sHv (H_v.cpp:192-357, declared H_v.h:36-57). */
 int edg_hv(edg_sector* s, const void* v, void* w, int dtype, void* stream);
 
-/* Search every row's flipped states once and keep the result in HBM: one
- * 32-bit word per (row, anti-aligned pair) holding the representative's
- * position and phase class (4 bytes x ~55 pairs per row; 56 GB for the
- * 36-site Sz=0 sector).  Afterwards edg_hv streams these words instead of
- * searching; coefficients are still computed from the state bits.  Fails with
- * EDG_ERR_NOMEM (sector unchanged) when the words need more than max_bytes
- * (<= 0: no limit) or than is free.  Calls on one sector must not overlap:
- * the H*v keeps a scratch vector in the sector.  No reference counterpart:
- * the reference precomputes per-configuration tables instead
- * (Momentum_Basis.cpp:750-777). */
+/* Search every row's flipped states once and keep the result in HBM as
+ * compressed sparse rows: per nonzero a u32 column and a u16 index into a
+ * table of (pair coefficient x phase) values, per row its diagonal (6 bytes
+ * per nonzero, 84 GB for the 36-site Sz=0 sector).  Afterwards edg_hv streams
+ * these rows instead of searching orbits.  Fails with EDG_ERR_NOMEM (sector
+ * unchanged, still matrix-free) when they need more than max_bytes (<= 0: no
+ * limit) or than is free; EDG_ERR_UNSUPPORTED for ChCh terms or more than
+ * 65536 distinct values.  H*v calls on one sector must not overlap: they
+ * share a scratch vector.  Counterpart in the reference: the optional
+ * sparse-matrix sHv (H_v.cpp:3-19), which stores complex values per nonzero. */
 int edg_sector_build_targets(edg_sector* s, int64_t max_bytes);
 int edg_sector_free_targets(edg_sector* s);
 
