@@ -248,7 +248,7 @@ def run_device(args, world, rank, local_rank):
         if sec.build_targets():
             torch.cuda.synchronize()
             t_tgt = time.perf_counter() - t0
-            mode = "stored-targets"
+            mode = "stored-rows"
             B = sec.algorithmic_bytes(elem, nnz)
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
@@ -322,7 +322,7 @@ def run_device(args, world, rank, local_rank):
         "config": {"workload": args.workload, "n_p": sec.n_p, "nnz_off": nnz, "vector": args.dtype,
                    "hv_mode": mode, "algorithmic_bytes_per_hv": B, "basis_seconds": round(t_basis, 3),
                    "target_build_seconds": None if t_tgt is None else round(t_tgt, 3),
-                   "stored_target_bytes": 4 * sec.info.get("n_targets", 0),
+                   "stored_row_bytes": 6 * sec.info.get("n_targets", 0) + 16 * sec.n_p,
                    "matrix_free_ms_per_step": mf_ms,
                    "matrix_free_GBps": B_mf / (mf_ms / 1e3) / 1e9,
                    "l2": "inputs larger than L2 (no flush needed)", "orbit_search": "torus" if sec.info["torus"] else "walk"},
@@ -332,7 +332,7 @@ def run_device(args, world, rank, local_rank):
         "e2e": e2e,
         "clocks": clocks,
         # one H*v kernel per step; the stored-target path adds the u = v/norm pass
-        "gpu_launches": args.steps * (2 if mode == "stored-targets" else 1),
+        "gpu_launches": args.steps * (2 if mode == "stored-rows" else 1),
     }
     if rank == 0:
         print(json.dumps(out), flush=True)

@@ -246,7 +246,10 @@ __global__ void k_u_scale(const typename CT2<Real>::T* __restrict__ v, const uin
   }
 }
 
-// CSR SpMV with a value dictionary: one warp per row
+// CSR SpMV with a value dictionary: one warp per row.  The row's first 128
+// entries are handled in one unrolled step -- all column/value-id loads, then
+// all gathers, so a row costs two memory round trips instead of one per 32
+// entries -- and the next row's offsets are loaded while this row runs.
 template <typename Real, bool kSmemTab>
 __global__ void __launch_bounds__(kTgtThreads) k_hv_csr(const uint64_t* __restrict__ row_ptr,
                                                         const uint32_t* __restrict__ col,
@@ -259,6 +262,7 @@ __global__ void __launch_bounds__(kTgtThreads) k_hv_csr(const uint64_t* __restri
                                                         const typename CT2<Real>::T* __restrict__ u,
                                                         typename CT2<Real>::T* __restrict__ w) {
   using CT = typename CT2<Real>::T;
+  constexpr int kU = 4;  // 32-entry chunks resolved together
   extern __shared__ __align__(16) uint8_t sm[];
   __shared__ Real nrm[65];
   CT* tab = reinterpret_cast<CT*>(sm);
@@ -269,17 +273,45 @@ __global__ void __launch_bounds__(kTgtThreads) k_hv_csr(const uint64_t* __restri
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t i = warp; i < n_p; i += n_warps) {
-    const uint64_t beg = __ldg(reinterpret_cast<const unsigned long long*>(row_ptr) + i);
-    const uint64_t end = __ldg(reinterpret_cast<const unsigned long long*>(row_ptr) + i + 1);
+  const unsigned long long* rp = reinterpret_cast<const unsigned long long*>(row_ptr);
+  int64_t i = warp;
+  uint64_t beg = 0, end = 0;
+  if (i < n_p) {
+    beg = __ldg(rp + i);
+    end = __ldg(rp + i + 1);
+  }
+  while (i < n_p) {
+    const int64_t inext = i + n_warps;
+    uint64_t nbeg = 0, nend = 0;
+    if (inext < n_p) {
+      nbeg = __ldg(rp + inext);
+      nend = __ldg(rp + inext + 1);
+    }
     Real ar = 0, ai = 0;
-    for (uint64_t t = beg + lane; t < end; t += 32) {
-      const uint32_t j = __ldg(col + t);
-      const int id = __ldg(vid + t);
-      const CT c = kSmemTab ? tab[id] : __ldg(vtab + id);
-      const CT x = u[j];
-      ar += c.x * x.x - c.y * x.y;
-      ai += c.x * x.y + c.y * x.x;
+    uint32_t j[kU];
+    int id[kU];
+#pragma unroll
+    for (int q = 0; q < kU; ++q) {
+      const uint64_t t = beg + lane + 32 * q;
+      j[q] = t < end ? __ldg(col + t) : 0xFFFFFFFFu;
+      id[q] = t < end ? (int)__ldg(vid + t) : 0;
+    }
+    CT x[kU];
+#pragma unroll
+    for (int q = 0; q < kU; ++q)
+      if (j[q] != 0xFFFFFFFFu) x[q] = u[j[q]];
+#pragma unroll
+    for (int q = 0; q < kU; ++q) {
+      if (j[q] == 0xFFFFFFFFu) continue;
+      const CT c = kSmemTab ? tab[id[q]] : __ldg(vtab + id[q]);
+      ar += c.x * x[q].x - c.y * x[q].y;
+      ai += c.x * x[q].y + c.y * x[q].x;
+    }
+    for (uint64_t t = beg + lane + 32 * kU; t < end; t += 32) {  // rows longer than 128 entries
+      const CT c = kSmemTab ? tab[__ldg(vid + t)] : __ldg(vtab + __ldg(vid + t));
+      const CT y = u[__ldg(col + t)];
+      ar += c.x * y.x - c.y * y.y;
+      ai += c.x * y.y + c.y * y.x;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -295,6 +327,9 @@ __global__ void __launch_bounds__(kTgtThreads) k_hv_csr(const uint64_t* __restri
       out.y = ai * ni + d * vi.y;
       w[i] = out;
     }
+    i = inext;
+    beg = nbeg;
+    end = nend;
   }
 }
 
