@@ -243,6 +243,7 @@ def run_device(args, world, rank, local_rank):
     # stored targets: the search done once, its results streamed every H*v
     mode = "matrix-free"
     t_tgt = None
+    lpr, tune_ms = None, None
     if not args.matrix_free:
         t0 = time.perf_counter()
         if sec.build_targets():
@@ -250,6 +251,7 @@ def run_device(args, world, rank, local_rank):
             t_tgt = time.perf_counter() - t0
             mode = "stored-rows"
             B = sec.algorithmic_bytes(elem, nnz)
+            lpr, tune_ms = sec.tune(0)
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
             sec.hv(v, w, stream)
@@ -324,6 +326,8 @@ def run_device(args, world, rank, local_rank):
                    "target_build_seconds": None if t_tgt is None else round(t_tgt, 3),
                    "stored_row_bytes": 6 * sec.info.get("n_targets", 0) + 16 * sec.n_p,
                    "matrix_free_ms_per_step": mf_ms,
+                   "lanes_per_row": lpr,
+                   "tune_ms_lpr_8_16_32": None if tune_ms is None else [round(float(x), 3) for x in tune_ms],
                    "matrix_free_GBps": B_mf / (mf_ms / 1e3) / 1e9,
                    "l2": "inputs larger than L2 (no flush needed)", "orbit_search": "torus" if sec.info["torus"] else "walk"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,

@@ -100,6 +100,7 @@ SIGNATURES = {
     "edg_fill_random": (C.c_int, [C.c_void_p, C.c_int64, C.c_int, C.c_uint64, C.c_void_p]),
     "edg_sector_build_targets": (C.c_int, [C.c_void_p, C.c_int64]),
     "edg_sector_free_targets": (C.c_int, [C.c_void_p]),
+    "edg_sector_tune": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.c_void_p]),
     "edg_solve_plain": (C.c_int, [C.c_void_p, C.POINTER(edg_solver_opts), C.c_void_p, C.c_int64,
                                   C.POINTER(C.c_int64), C.c_void_p, C.c_int64, C.POINTER(edg_solver_stats)]),
     "edg_solve_mixed": (C.c_int, [C.c_void_p, C.POINTER(edg_mixed_opts), C.c_void_p, C.c_void_p, C.c_void_p,

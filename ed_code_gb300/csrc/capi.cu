@@ -631,6 +631,13 @@ int edg_sector_free_targets(edg_sector* s) {
   return EDG_OK;
 }
 
+int edg_sector_tune(edg_sector* s, int lanes_per_row, int* chosen, double* ms) {
+  if (!s) return fail(EDG_ERR_INVALID, "NULL sector");
+  const int rc = tune_rows(s->s, lanes_per_row, chosen, ms);
+  if (rc != EDG_OK) return fail(rc, "tuning the stored-row kernel failed");
+  return EDG_OK;
+}
+
 int edg_count_offdiag(edg_sector* s, int64_t* nnz_off) {
   if (!s || !nnz_off) return fail(EDG_ERR_INVALID, "NULL argument");
   Sector& S = s->s;

@@ -97,6 +97,7 @@ struct Sector {
   int n_vals = 0;
   DeviceBuffer ubuf;            // u = v / norm scratch
   size_t targets_bytes = 0;
+  int csr_lpr = 16;             // lanes per CSR row (8, 16 or 32): edg_sector_tune_rows
 };
 
 // basis.cu
@@ -116,6 +117,7 @@ cudaError_t count_offdiag(const Sector& S, unsigned long long* nnz_dev, cudaStre
 int build_targets(Sector& S, int64_t max_bytes, std::string& err);
 void free_targets(Sector& S);
 cudaError_t launch_hv_stored(const Sector& S, const void* v, void* w, bool fp64, cudaStream_t st);
+int tune_rows(Sector& S, int lpr, int* chosen, double* ms_out);
 int hv_grid_blocks(bool fp64, bool torus, bool chch);
 
 }  // namespace edg

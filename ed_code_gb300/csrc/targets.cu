@@ -246,11 +246,54 @@ __global__ void k_u_scale(const typename CT2<Real>::T* __restrict__ v, const uin
   }
 }
 
-// CSR SpMV with a value dictionary: one warp per row.  The row's first 128
-// entries are handled in one unrolled step -- all column/value-id loads, then
-// all gathers, so a row costs two memory round trips instead of one per 32
-// entries -- and the next row's offsets are loaded while this row runs.
-template <typename Real, bool kSmemTab>
+// One CSR row, handled by LPR lanes of a warp (sl = lane within the row).
+// The row's first LPR*kU entries are resolved in one unrolled step -- all
+// column/value-id loads, then all gathers -- longer rows finish in a loop.
+// Returns the row sum in lane sl == 0 after a segmented reduction.
+template <typename Real, int LPR, bool kSmemTab>
+__device__ __forceinline__ void csr_row(uint64_t beg, uint64_t end, int sl, const uint32_t* __restrict__ col,
+                                        const uint16_t* __restrict__ vid, const typename CT2<Real>::T* vtab,
+                                        const typename CT2<Real>::T* __restrict__ u, Real& ar, Real& ai) {
+  using CT = typename CT2<Real>::T;
+  constexpr int kU = 64 / LPR < 2 ? 2 : 64 / LPR;
+  ar = 0;
+  ai = 0;
+  uint32_t j[kU];
+  int id[kU];
+#pragma unroll
+  for (int q = 0; q < kU; ++q) {
+    const uint64_t t = beg + sl + LPR * q;
+    j[q] = t < end ? __ldg(col + t) : 0xFFFFFFFFu;
+    id[q] = t < end ? (int)__ldg(vid + t) : 0;
+  }
+  CT x[kU];
+#pragma unroll
+  for (int q = 0; q < kU; ++q)
+    if (j[q] != 0xFFFFFFFFu) x[q] = u[j[q]];
+#pragma unroll
+  for (int q = 0; q < kU; ++q) {
+    if (j[q] == 0xFFFFFFFFu) continue;
+    const CT c = kSmemTab ? vtab[id[q]] : __ldg(vtab + id[q]);
+    ar += c.x * x[q].x - c.y * x[q].y;
+    ai += c.x * x[q].y + c.y * x[q].x;
+  }
+  for (uint64_t t = beg + sl + LPR * kU; t < end; t += LPR) {
+    const int idt = __ldg(vid + t);
+    const CT c = kSmemTab ? vtab[idt] : __ldg(vtab + idt);
+    const CT y = u[__ldg(col + t)];
+    ar += c.x * y.x - c.y * y.y;
+    ai += c.x * y.y + c.y * y.x;
+  }
+#pragma unroll
+  for (int o = LPR / 2; o > 0; o >>= 1) {
+    ar += __shfl_down_sync(0xffffffffu, ar, o, LPR);
+    ai += __shfl_down_sync(0xffffffffu, ai, o, LPR);
+  }
+}
+
+// CSR SpMV with a value dictionary: 32/LPR rows per warp, the next rows'
+// offsets loaded while the current ones run.
+template <typename Real, int LPR, bool kSmemTab>
 __global__ void __launch_bounds__(kTgtThreads) k_hv_csr(const uint64_t* __restrict__ row_ptr,
                                                         const uint32_t* __restrict__ col,
                                                         const uint16_t* __restrict__ vid,
@@ -262,7 +305,7 @@ __global__ void __launch_bounds__(kTgtThreads) k_hv_csr(const uint64_t* __restri
                                                         const typename CT2<Real>::T* __restrict__ u,
                                                         typename CT2<Real>::T* __restrict__ w) {
   using CT = typename CT2<Real>::T;
-  constexpr int kU = 4;  // 32-entry chunks resolved together
+  constexpr int kRows = 32 / LPR;  // rows per warp
   extern __shared__ __align__(16) uint8_t sm[];
   __shared__ Real nrm[65];
   CT* tab = reinterpret_cast<CT*>(sm);
@@ -270,55 +313,26 @@ __global__ void __launch_bounds__(kTgtThreads) k_hv_csr(const uint64_t* __restri
   if (kSmemTab)
     for (int k = threadIdx.x; k < n_vals; k += blockDim.x) tab[k] = vtab[k];
   __syncthreads();
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, sl = lane % LPR, sub = lane / LPR;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const unsigned long long* rp = reinterpret_cast<const unsigned long long*>(row_ptr);
-  int64_t i = warp;
+  int64_t i = warp * kRows + sub;
   uint64_t beg = 0, end = 0;
   if (i < n_p) {
     beg = __ldg(rp + i);
     end = __ldg(rp + i + 1);
   }
-  while (i < n_p) {
-    const int64_t inext = i + n_warps;
+  for (int64_t base = warp * kRows; base < n_p; base += n_warps * kRows) {
+    const int64_t inext = i + n_warps * kRows;
     uint64_t nbeg = 0, nend = 0;
     if (inext < n_p) {
       nbeg = __ldg(rp + inext);
       nend = __ldg(rp + inext + 1);
     }
-    Real ar = 0, ai = 0;
-    uint32_t j[kU];
-    int id[kU];
-#pragma unroll
-    for (int q = 0; q < kU; ++q) {
-      const uint64_t t = beg + lane + 32 * q;
-      j[q] = t < end ? __ldg(col + t) : 0xFFFFFFFFu;
-      id[q] = t < end ? (int)__ldg(vid + t) : 0;
-    }
-    CT x[kU];
-#pragma unroll
-    for (int q = 0; q < kU; ++q)
-      if (j[q] != 0xFFFFFFFFu) x[q] = u[j[q]];
-#pragma unroll
-    for (int q = 0; q < kU; ++q) {
-      if (j[q] == 0xFFFFFFFFu) continue;
-      const CT c = kSmemTab ? tab[id[q]] : __ldg(vtab + id[q]);
-      ar += c.x * x[q].x - c.y * x[q].y;
-      ai += c.x * x[q].y + c.y * x[q].x;
-    }
-    for (uint64_t t = beg + lane + 32 * kU; t < end; t += 32) {  // rows longer than 128 entries
-      const CT c = kSmemTab ? tab[__ldg(vid + t)] : __ldg(vtab + __ldg(vid + t));
-      const CT y = u[__ldg(col + t)];
-      ar += c.x * y.x - c.y * y.y;
-      ai += c.x * y.y + c.y * y.x;
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      ar += __shfl_down_sync(0xffffffffu, ar, o);
-      ai += __shfl_down_sync(0xffffffffu, ai, o);
-    }
-    if (lane == 0) {
+    Real ar, ai;
+    csr_row<Real, LPR, kSmemTab>(beg, i < n_p ? end : beg, sl, col, vid, kSmemTab ? tab : vtab, u, ar, ai);
+    if (sl == 0 && i < n_p) {
       const CT vi = v[i];
       const Real ni = nrm[lid[i]];
       const Real d = (Real)ezz[i];
@@ -351,8 +365,8 @@ const double* params_field(const Sector& S, size_t offset) {
   return reinterpret_cast<const double*>(reinterpret_cast<const char*>(S.dP) + offset);
 }
 
-template <typename Real>
-cudaError_t launch_csr_t(const Sector& S, const void* v, void* w, cudaStream_t st) {
+template <typename Real, int LPR>
+cudaError_t launch_csr_lpr(const Sector& S, const void* v, void* w, cudaStream_t st) {
   using CT = typename CT2<Real>::T;
   const int64_t n = S.P.n_p;
   k_u_scale<Real><<<(int)std::min<int64_t>((n + 255) / 256, 152 * 32), 256, 0, st>>>(
@@ -361,18 +375,28 @@ cudaError_t launch_csr_t(const Sector& S, const void* v, void* w, cudaStream_t s
   const CT* tab = reinterpret_cast<const CT*>(sizeof(Real) == 8 ? (const void*)S.vtab64 : (const void*)S.vtab32);
   const size_t tab_bytes = sizeof(CT) * S.n_vals;
   const double* nrm = params_field(S, offsetof(SectorParams, nrm));
+  const int64_t threads_needed = (n * LPR + 31) / 32 * 32;
   if (tab_bytes <= 96 * 1024) {
-    auto kern = k_hv_csr<Real, true>;
-    kern<<<grid_for(kern, tab_bytes, n * 32, kTgtThreads), kTgtThreads, tab_bytes, st>>>(
+    auto kern = k_hv_csr<Real, LPR, true>;
+    kern<<<grid_for(kern, tab_bytes, threads_needed, kTgtThreads), kTgtThreads, tab_bytes, st>>>(
         S.row_ptr, S.col, S.vid, tab, S.n_vals, S.ezz, S.lid, nrm, n, reinterpret_cast<const CT*>(v),
         reinterpret_cast<const CT*>(S.ubuf.ptr), reinterpret_cast<CT*>(w));
   } else {
-    auto kern = k_hv_csr<Real, false>;
-    kern<<<grid_for(kern, 0, n * 32, kTgtThreads), kTgtThreads, 0, st>>>(
+    auto kern = k_hv_csr<Real, LPR, false>;
+    kern<<<grid_for(kern, 0, threads_needed, kTgtThreads), kTgtThreads, 0, st>>>(
         S.row_ptr, S.col, S.vid, tab, S.n_vals, S.ezz, S.lid, nrm, n, reinterpret_cast<const CT*>(v),
         reinterpret_cast<const CT*>(S.ubuf.ptr), reinterpret_cast<CT*>(w));
   }
   return cudaGetLastError();
+}
+
+template <typename Real>
+cudaError_t launch_csr_t(const Sector& S, const void* v, void* w, cudaStream_t st) {
+  switch (S.csr_lpr) {
+    case 8: return launch_csr_lpr<Real, 8>(S, v, w, st);
+    case 16: return launch_csr_lpr<Real, 16>(S, v, w, st);
+    default: return launch_csr_lpr<Real, 32>(S, v, w, st);
+  }
 }
 
 int64_t gcd64(int64_t a, int64_t b) {
@@ -568,6 +592,57 @@ int build_targets(Sector& S, int64_t max_bytes, std::string& err) {
   S.device_bytes += S.targets_bytes;
   e = cudaMemcpy(S.dP, &P, sizeof(P), cudaMemcpyHostToDevice);
   return e == cudaSuccess ? EDG_OK : EDG_ERR_CUDA;
+}
+
+// Lanes per CSR row: lpr in {8, 16, 32}, or 0 to time each (FP32, three
+// launches after a warm-up) on this sector and keep the fastest.
+int tune_rows(Sector& S, int lpr, int* chosen, double* ms_out) {
+  if (!S.col) {
+    if (chosen) *chosen = 0;
+    return EDG_OK;  // matrix-free sectors have nothing to tune
+  }
+  if (lpr == 8 || lpr == 16 || lpr == 32) {
+    S.csr_lpr = lpr;
+    if (chosen) *chosen = lpr;
+    return EDG_OK;
+  }
+  if (lpr != 0) return EDG_ERR_INVALID;
+  const int64_t n = S.P.n_p;
+  float2 *v = nullptr, *w = nullptr;
+  if (cudaMalloc(&v, sizeof(float2) * n) != cudaSuccess || cudaMalloc(&w, sizeof(float2) * n) != cudaSuccess) {
+    cudaFree(v);
+    return EDG_ERR_NOMEM;
+  }
+  cudaStream_t st = S.stream;
+  cudaMemsetAsync(v, 0, sizeof(float2) * n, st);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int cand[3] = {8, 16, 32};
+  int best = 16;
+  float best_ms = 1e30f;
+  for (int c : cand) {
+    S.csr_lpr = c;
+    launch_hv_stored(S, v, w, false, st);
+    cudaEventRecord(e0, st);
+    for (int r = 0; r < 3; ++r) launch_hv_stored(S, v, w, false, st);
+    cudaEventRecord(e1, st);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms_out) ms_out[c == 8 ? 0 : (c == 16 ? 1 : 2)] = ms / 3;
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = c;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(v);
+  cudaFree(w);
+  S.csr_lpr = best;
+  if (chosen) *chosen = best;
+  return cudaGetLastError() == cudaSuccess ? EDG_OK : EDG_ERR_CUDA;
 }
 
 cudaError_t launch_hv_stored(const Sector& S, const void* v, void* w, bool fp64, cudaStream_t st) {

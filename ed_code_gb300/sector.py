@@ -63,6 +63,14 @@ class GpuSector:
         self.refresh_info()
         return True
 
+    def tune(self, lanes_per_row: int = 0):
+        """Choose the lanes per stored row (0: time 8/16/32 and keep the fastest).
+        Returns (choice, [ms for 8, 16, 32])."""
+        ch = C.c_int()
+        ms = np.zeros(3, np.float64)
+        N.check(N.lib().edg_sector_tune(self._h, int(lanes_per_row), C.byref(ch), ms.ctypes.data))
+        return ch.value, ms
+
     def free_targets(self) -> None:
         N.check(N.lib().edg_sector_free_targets(self._h))
         self.refresh_info()

@@ -113,6 +113,11 @@ int edg_hv(edg_sector* s, const void* v, void* w, int dtype, void* stream);
 int edg_sector_build_targets(edg_sector* s, int64_t max_bytes);
 int edg_sector_free_targets(edg_sector* s);
 
+/* Lanes of a warp per stored row (8, 16 or 32, i.e. 4, 2 or 1 rows per warp);
+ * 0 times the three on this sector and keeps the fastest.  *chosen receives
+ * the choice, ms (NULL allowed) the three timings in that order. */
+int edg_sector_tune(edg_sector* s, int lanes_per_row, int* chosen, double* ms);
+
 /* Same with host buffers: copies v in, applies H, copies w out, synchronises.
  * This is the call the reference's sHv(v, w, ...) adapter makes. */
 int edg_hv_host(edg_sector* s, const void* v, void* w, int dtype);
