@@ -96,6 +96,7 @@ SIGNATURES = {
     "edg_sector_copy_config_tables": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
     "edg_hv": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "edg_hv_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    "edg_hv_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "edg_count_offdiag": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
     "edg_fill_random": (C.c_int, [C.c_void_p, C.c_int64, C.c_int, C.c_uint64, C.c_void_p]),
     "edg_sector_build_targets": (C.c_int, [C.c_void_p, C.c_int64]),

@@ -122,6 +122,20 @@ int edg_sector_tune(edg_sector* s, int lanes_per_row, int* chosen, double* ms);
  * This is the call the reference's sHv(v, w, ...) adapter makes. */
 int edg_hv_host(edg_sector* s, const void* v, void* w, int dtype);
 
+/* w = H v like edg_hv, for callers that must not have the library allocate
+ * device memory during the call: applications whose own allocator already
+ * holds the device's free memory, and loops where a cudaMalloc or cudaFree
+ * would synchronise the device.  No counterpart in the reference (its sHv runs
+ * on the host).  Needs stored rows (edg_sector_build_targets) and the sector's
+ * device current.  The u = v/norm scratch is a fixed 16 MiB array in the
+ * library's device image, held on every GPU that loads it until exit, so
+ * n_p may be at most 1,048,576 (EDG_C128) or 2,097,152 (EDG_C64); larger
+ * sectors return EDG_ERR_INVALID.  The first call on a device looks the
+ * array's address up (cudaGetSymbolAddress); make that first call before any
+ * stream capture.  All calls on a device share the array: calls that overlap
+ * on the GPU race and must be ordered by the caller. */
+int edg_hv_noalloc(edg_sector* s, const void* v, void* w, int dtype, void* stream);
+
 /* Number of nonzero off-diagonal bond/chirality targets summed over rows
  * (the nnz_off of the algorithmic byte count). */
 int edg_count_offdiag(edg_sector* s, int64_t* nnz_off);
