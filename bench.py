@@ -251,7 +251,12 @@ def run_device(args, world, rank, local_rank):
             t_tgt = time.perf_counter() - t0
             mode = "stored-rows"
             B = sec.algorithmic_bytes(elem, nnz)
-            lpr, tune_ms = sec.tune(0)
+            if args.rows:
+                lanes, pol = (int(x) for x in args.rows.split(","))
+                sec.set_rows(lanes, pol)
+                lpr = lanes
+            else:
+                lpr, tune_ms = sec.tune(0)
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
             sec.hv(v, w, stream)
@@ -326,7 +331,7 @@ def run_device(args, world, rank, local_rank):
                    "target_build_seconds": None if t_tgt is None else round(t_tgt, 3),
                    "stored_row_bytes": 6 * sec.info.get("n_targets", 0) + 16 * sec.n_p,
                    "matrix_free_ms_per_step": mf_ms,
-                   "lanes_per_row": lpr,
+                   "lanes_per_row": lpr, "cache_policy": sec.info.get("cache_policy"),
                    "tune_ms_lpr_8_16_32": None if tune_ms is None else [round(float(x), 3) for x in tune_ms],
                    "matrix_free_GBps": B_mf / (mf_ms / 1e3) / 1e9,
                    "l2": "inputs larger than L2 (no flush needed)", "orbit_search": "torus" if sec.info["torus"] else "walk"},
@@ -354,6 +359,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--matrix-free", action="store_true", help="do not store the searched targets")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--rows", default=None, help="LANES,POLICY: fix the stored-row kernel instead of timing it")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-step-seconds", type=float, default=4.0)
     args = ap.parse_args()

@@ -53,7 +53,8 @@ class edg_sector_info(C.Structure):
     _fields_ = [
         ("n_sites", C.c_int), ("n_ones", C.c_int), ("L1", C.c_int), ("L2", C.c_int), ("kx", C.c_int),
         ("ky", C.c_int), ("torus", C.c_int), ("n_groups", C.c_int), ("n_p", C.c_int64), ("n_configs", C.c_int64),
-        ("device_bytes", C.c_int64), ("n_targets", C.c_int64),
+        ("device_bytes", C.c_int64), ("n_targets", C.c_int64), ("lanes_per_row", C.c_int),
+        ("cache_policy", C.c_int),
     ]
 
 
@@ -96,6 +97,7 @@ SIGNATURES = {
     "edg_sector_copy_config_tables": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
     "edg_hv": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "edg_hv_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    "edg_sector_set_rows": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "edg_hv_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "edg_count_offdiag": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
     "edg_fill_random": (C.c_int, [C.c_void_p, C.c_int64, C.c_int, C.c_uint64, C.c_void_p]),

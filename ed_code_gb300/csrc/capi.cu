@@ -485,6 +485,8 @@ int edg_sector_get_info(const edg_sector* s, edg_sector_info* info) {
   info->n_configs = P.n_configs;
   info->device_bytes = (int64_t)s->s.device_bytes;
   info->n_targets = P.n_targets;
+  info->lanes_per_row = s->s.col ? s->s.csr_lpr : 0;
+  info->cache_policy = s->s.col ? s->s.csr_pol : 0;
   return EDG_OK;
 }
 
@@ -635,6 +637,16 @@ int edg_sector_tune(edg_sector* s, int lanes_per_row, int* chosen, double* ms) {
   if (!s) return fail(EDG_ERR_INVALID, "NULL sector");
   const int rc = tune_rows(s->s, lanes_per_row, chosen, ms);
   if (rc != EDG_OK) return fail(rc, "tuning the stored-row kernel failed");
+  return EDG_OK;
+}
+
+int edg_sector_set_rows(edg_sector* s, int lanes_per_row, int cache_policy) {
+  if (!s) return fail(EDG_ERR_INVALID, "NULL sector");
+  if (lanes_per_row != 8 && lanes_per_row != 16 && lanes_per_row != 32)
+    return fail(EDG_ERR_INVALID, "lanes_per_row must be 8, 16 or 32");
+  if (cache_policy != 1 && cache_policy != 2) return fail(EDG_ERR_INVALID, "cache_policy must be 1 or 2");
+  s->s.csr_lpr = lanes_per_row;
+  s->s.csr_pol = cache_policy;
   return EDG_OK;
 }
 

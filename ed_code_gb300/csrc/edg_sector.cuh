@@ -97,7 +97,8 @@ struct Sector {
   int n_vals = 0;
   DeviceBuffer ubuf;            // u = v / norm scratch
   size_t targets_bytes = 0;
-  int csr_lpr = 16;             // lanes per CSR row (8, 16 or 32): edg_sector_tune_rows
+  int csr_lpr = 16;             // lanes per CSR row (8, 16 or 32): edg_sector_tune
+  int csr_pol = 1;              // cache policy of the CSR loads (1 or 2): edg_sector_tune
 };
 
 // basis.cu

@@ -246,11 +246,53 @@ __global__ void k_u_scale(const typename CT2<Real>::T* __restrict__ v, const uin
   }
 }
 
+// Cache policy of the CSR loads (tuned per sector with the lanes per row).
+// The row data (col, vid) are read once per H*v; the gathered u entries are
+// reused by other rows while they stay in L2.  Policy 1 reads the row data
+// with the streaming hint (ld.global.cs); policy 2 gives them the L2
+// evict_first priority instead.  Both give the u gathers L2 evict_last.  At
+// 36 sites (a 2 GB u against a 129 MB L2) policy 2 measured 68 ms against
+// 84 ms; at 30-32 sites policy 1 is the faster one.
+__device__ __forceinline__ uint64_t l2_evict_first() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t l2_evict_last() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+template <int kPol>
+__device__ __forceinline__ uint32_t ld_row(const uint32_t* a, uint64_t pol) {
+  if (kPol == 1) return __ldcs(a);
+  uint32_t r;
+  asm volatile("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(r) : "l"(a), "l"(pol));
+  return r;
+}
+template <int kPol>
+__device__ __forceinline__ int ld_row(const uint16_t* a, uint64_t pol) {
+  if (kPol == 1) return __ldcs(a);
+  uint16_t r;
+  asm volatile("ld.global.nc.L2::cache_hint.u16 %0, [%1], %2;" : "=h"(r) : "l"(a), "l"(pol));
+  return r;
+}
+__device__ __forceinline__ float2 ld_keep(const float2* a, uint64_t pol) {
+  float2 r;
+  asm volatile("ld.global.nc.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;" : "=f"(r.x), "=f"(r.y) : "l"(a), "l"(pol));
+  return r;
+}
+__device__ __forceinline__ double2 ld_keep(const double2* a, uint64_t pol) {
+  double2 r;
+  asm volatile("ld.global.nc.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;" : "=d"(r.x), "=d"(r.y) : "l"(a), "l"(pol));
+  return r;
+}
+
 // One CSR row, handled by LPR lanes of a warp (sl = lane within the row).
 // The row's first LPR*kU entries are resolved in one unrolled step -- all
 // column/value-id loads, then all gathers -- longer rows finish in a loop.
 // Returns the row sum in lane sl == 0 after a segmented reduction.
-template <typename Real, int LPR, bool kSmemTab>
+template <typename Real, int LPR, bool kSmemTab, int kPol>
 __device__ __forceinline__ void csr_row(uint64_t beg, uint64_t end, int sl, const uint32_t* __restrict__ col,
                                         const uint16_t* __restrict__ vid, const typename CT2<Real>::T* vtab,
                                         const typename CT2<Real>::T* __restrict__ u, Real& ar, Real& ai) {
@@ -258,18 +300,19 @@ __device__ __forceinline__ void csr_row(uint64_t beg, uint64_t end, int sl, cons
   constexpr int kU = 64 / LPR < 2 ? 2 : 64 / LPR;
   ar = 0;
   ai = 0;
+  const uint64_t pf = kPol == 2 ? l2_evict_first() : 0, pl = l2_evict_last();
   uint32_t j[kU];
   int id[kU];
 #pragma unroll
   for (int q = 0; q < kU; ++q) {
     const uint64_t t = beg + sl + LPR * q;
-    j[q] = t < end ? __ldg(col + t) : 0xFFFFFFFFu;
-    id[q] = t < end ? (int)__ldg(vid + t) : 0;
+    j[q] = t < end ? ld_row<kPol>(col + t, pf) : 0xFFFFFFFFu;
+    id[q] = t < end ? ld_row<kPol>(vid + t, pf) : 0;
   }
   CT x[kU];
 #pragma unroll
   for (int q = 0; q < kU; ++q)
-    if (j[q] != 0xFFFFFFFFu) x[q] = u[j[q]];
+    if (j[q] != 0xFFFFFFFFu) x[q] = ld_keep(u + j[q], pl);
 #pragma unroll
   for (int q = 0; q < kU; ++q) {
     if (j[q] == 0xFFFFFFFFu) continue;
@@ -278,9 +321,9 @@ __device__ __forceinline__ void csr_row(uint64_t beg, uint64_t end, int sl, cons
     ai += c.x * x[q].y + c.y * x[q].x;
   }
   for (uint64_t t = beg + sl + LPR * kU; t < end; t += LPR) {
-    const int idt = __ldg(vid + t);
+    const int idt = ld_row<kPol>(vid + t, pf);
     const CT c = kSmemTab ? vtab[idt] : __ldg(vtab + idt);
-    const CT y = u[__ldg(col + t)];
+    const CT y = ld_keep(u + ld_row<kPol>(col + t, pf), pl);
     ar += c.x * y.x - c.y * y.y;
     ai += c.x * y.y + c.y * y.x;
   }
@@ -293,7 +336,7 @@ __device__ __forceinline__ void csr_row(uint64_t beg, uint64_t end, int sl, cons
 
 // CSR SpMV with a value dictionary: 32/LPR rows per warp, the next rows'
 // offsets loaded while the current ones run.
-template <typename Real, int LPR, bool kSmemTab>
+template <typename Real, int LPR, bool kSmemTab, int kPol>
 __global__ void __launch_bounds__(kTgtThreads) k_hv_csr(const uint64_t* __restrict__ row_ptr,
                                                         const uint32_t* __restrict__ col,
                                                         const uint16_t* __restrict__ vid,
@@ -331,7 +374,7 @@ __global__ void __launch_bounds__(kTgtThreads) k_hv_csr(const uint64_t* __restri
       nend = __ldg(rp + inext + 1);
     }
     Real ar, ai;
-    csr_row<Real, LPR, kSmemTab>(beg, i < n_p ? end : beg, sl, col, vid, kSmemTab ? tab : vtab, u, ar, ai);
+    csr_row<Real, LPR, kSmemTab, kPol>(beg, i < n_p ? end : beg, sl, col, vid, kSmemTab ? tab : vtab, u, ar, ai);
     if (sl == 0 && i < n_p) {
       const CT vi = v[i];
       const Real ni = nrm[lid[i]];
@@ -365,7 +408,7 @@ const double* params_field(const Sector& S, size_t offset) {
   return reinterpret_cast<const double*>(reinterpret_cast<const char*>(S.dP) + offset);
 }
 
-template <typename Real, int LPR>
+template <typename Real, int LPR, int kPol>
 cudaError_t launch_csr_lpr(const Sector& S, const void* v, void* w, cudaStream_t st) {
   using CT = typename CT2<Real>::T;
   const int64_t n = S.P.n_p;
@@ -377,12 +420,12 @@ cudaError_t launch_csr_lpr(const Sector& S, const void* v, void* w, cudaStream_t
   const double* nrm = params_field(S, offsetof(SectorParams, nrm));
   const int64_t threads_needed = (n * LPR + 31) / 32 * 32;
   if (tab_bytes <= 96 * 1024) {
-    auto kern = k_hv_csr<Real, LPR, true>;
+    auto kern = k_hv_csr<Real, LPR, true, kPol>;
     kern<<<grid_for(kern, tab_bytes, threads_needed, kTgtThreads), kTgtThreads, tab_bytes, st>>>(
         S.row_ptr, S.col, S.vid, tab, S.n_vals, S.ezz, S.lid, nrm, n, reinterpret_cast<const CT*>(v),
         reinterpret_cast<const CT*>(S.ubuf.ptr), reinterpret_cast<CT*>(w));
   } else {
-    auto kern = k_hv_csr<Real, LPR, false>;
+    auto kern = k_hv_csr<Real, LPR, false, kPol>;
     kern<<<grid_for(kern, 0, threads_needed, kTgtThreads), kTgtThreads, 0, st>>>(
         S.row_ptr, S.col, S.vid, tab, S.n_vals, S.ezz, S.lid, nrm, n, reinterpret_cast<const CT*>(v),
         reinterpret_cast<const CT*>(S.ubuf.ptr), reinterpret_cast<CT*>(w));
@@ -390,13 +433,18 @@ cudaError_t launch_csr_lpr(const Sector& S, const void* v, void* w, cudaStream_t
   return cudaGetLastError();
 }
 
+template <typename Real, int kPol>
+cudaError_t launch_csr_p(const Sector& S, const void* v, void* w, cudaStream_t st) {
+  switch (S.csr_lpr) {
+    case 8: return launch_csr_lpr<Real, 8, kPol>(S, v, w, st);
+    case 16: return launch_csr_lpr<Real, 16, kPol>(S, v, w, st);
+    default: return launch_csr_lpr<Real, 32, kPol>(S, v, w, st);
+  }
+}
+
 template <typename Real>
 cudaError_t launch_csr_t(const Sector& S, const void* v, void* w, cudaStream_t st) {
-  switch (S.csr_lpr) {
-    case 8: return launch_csr_lpr<Real, 8>(S, v, w, st);
-    case 16: return launch_csr_lpr<Real, 16>(S, v, w, st);
-    default: return launch_csr_lpr<Real, 32>(S, v, w, st);
-  }
+  return S.csr_pol == 2 ? launch_csr_p<Real, 2>(S, v, w, st) : launch_csr_p<Real, 1>(S, v, w, st);
 }
 
 int64_t gcd64(int64_t a, int64_t b) {
@@ -594,19 +642,16 @@ int build_targets(Sector& S, int64_t max_bytes, std::string& err) {
   return e == cudaSuccess ? EDG_OK : EDG_ERR_CUDA;
 }
 
-// Lanes per CSR row: lpr in {8, 16, 32}, or 0 to time each (FP32, three
-// launches after a warm-up) on this sector and keep the fastest.
+// Lanes per CSR row and cache policy.  lpr in {8, 16, 32} fixes the lanes and
+// times the two policies; 0 times all six combinations (FP32, three launches
+// after a warm-up each) on this sector and keeps the fastest.  ms_out[k]
+// receives the best time of lane count 8, 16, 32 (-1 when not timed).
 int tune_rows(Sector& S, int lpr, int* chosen, double* ms_out) {
   if (!S.col) {
     if (chosen) *chosen = 0;
     return EDG_OK;  // matrix-free sectors have nothing to tune
   }
-  if (lpr == 8 || lpr == 16 || lpr == 32) {
-    S.csr_lpr = lpr;
-    if (chosen) *chosen = lpr;
-    return EDG_OK;
-  }
-  if (lpr != 0) return EDG_ERR_INVALID;
+  if (lpr != 0 && lpr != 8 && lpr != 16 && lpr != 32) return EDG_ERR_INVALID;
   const int64_t n = S.P.n_p;
   float2 *v = nullptr, *w = nullptr;
   if (cudaMalloc(&v, sizeof(float2) * n) != cudaSuccess || cudaMalloc(&w, sizeof(float2) * n) != cudaSuccess) {
@@ -619,23 +664,30 @@ int tune_rows(Sector& S, int lpr, int* chosen, double* ms_out) {
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   const int cand[3] = {8, 16, 32};
-  int best = 16;
+  int best = 16, best_pol = 1;
   float best_ms = 1e30f;
-  for (int c : cand) {
-    S.csr_lpr = c;
-    launch_hv_stored(S, v, w, false, st);
-    cudaEventRecord(e0, st);
-    for (int r = 0; r < 3; ++r) launch_hv_stored(S, v, w, false, st);
-    cudaEventRecord(e1, st);
-    cudaEventSynchronize(e1);
-    float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
-    if (ms_out) ms_out[c == 8 ? 0 : (c == 16 ? 1 : 2)] = ms / 3;
-    if (ms < best_ms) {
-      best_ms = ms;
-      best = c;
+  for (int k = 0; k < 3; ++k) {
+    if (ms_out) ms_out[k] = -1;
+    if (lpr != 0 && cand[k] != lpr) continue;
+    for (int pol = 1; pol <= 2; ++pol) {
+      S.csr_lpr = cand[k];
+      S.csr_pol = pol;
+      launch_hv_stored(S, v, w, false, st);
+      cudaEventRecord(e0, st);
+      for (int r = 0; r < 3; ++r) launch_hv_stored(S, v, w, false, st);
+      cudaEventRecord(e1, st);
+      cudaEventSynchronize(e1);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms_out && (ms_out[k] < 0 || ms / 3 < ms_out[k])) ms_out[k] = ms / 3;
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = cand[k];
+        best_pol = pol;
+      }
     }
   }
+  S.csr_pol = best_pol;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaFree(v);

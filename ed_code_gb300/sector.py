@@ -64,12 +64,20 @@ class GpuSector:
         return True
 
     def tune(self, lanes_per_row: int = 0):
-        """Choose the lanes per stored row (0: time 8/16/32 and keep the fastest).
-        Returns (choice, [ms for 8, 16, 32])."""
+        """Choose the lanes per stored row and the cache policy of its loads by
+        timing them on this sector (0: all lane counts; 8/16/32: that count).
+        Returns (lanes, [best ms for 8, 16, 32], -1 where not timed); the
+        choices are also in ``info["lanes_per_row"]`` and ``info["cache_policy"]``."""
         ch = C.c_int()
         ms = np.zeros(3, np.float64)
         N.check(N.lib().edg_sector_tune(self._h, int(lanes_per_row), C.byref(ch), ms.ctypes.data))
+        self.refresh_info()
         return ch.value, ms
+
+    def set_rows(self, lanes_per_row: int, cache_policy: int) -> None:
+        """Fix the stored-row kernel's lanes per row (8/16/32) and cache policy (1/2)."""
+        N.check(N.lib().edg_sector_set_rows(self._h, int(lanes_per_row), int(cache_policy)))
+        self.refresh_info()
 
     def free_targets(self) -> None:
         N.check(N.lib().edg_sector_free_targets(self._h))

@@ -17,7 +17,7 @@
 extern "C" {
 #endif
 
-#define EDGPU_ABI_VERSION 1
+#define EDGPU_ABI_VERSION 2
 
 enum {
   EDG_OK = 0,
@@ -64,7 +64,9 @@ typedef struct {
   int64_t n_p;           /* sector dimension */
   int64_t n_configs;     /* C(N, n_ones) */
   int64_t device_bytes;  /* device memory held by the sector */
-  int64_t n_targets;     /* stored target words (0: H*v searches on the fly) */
+  int64_t n_targets;     /* stored nonzeros (0: H*v searches on the fly) */
+  int lanes_per_row;     /* stored-row H*v: lanes of a warp per row (edg_sector_tune) */
+  int cache_policy;      /* stored-row H*v: 1 streaming row loads, 2 L2 evict-first row loads */
 } edg_sector_info;
 
 const char* edg_last_error(void);
@@ -113,10 +115,17 @@ int edg_hv(edg_sector* s, const void* v, void* w, int dtype, void* stream);
 int edg_sector_build_targets(edg_sector* s, int64_t max_bytes);
 int edg_sector_free_targets(edg_sector* s);
 
-/* Lanes of a warp per stored row (8, 16 or 32, i.e. 4, 2 or 1 rows per warp);
- * 0 times the three on this sector and keeps the fastest.  *chosen receives
- * the choice, ms (NULL allowed) the three timings in that order. */
+/* Lanes of a warp per stored row (8, 16 or 32, i.e. 4, 2 or 1 rows per warp)
+ * and the cache policy of the row loads, timed on this sector: a nonzero
+ * lanes_per_row fixes the lanes and times the two policies, 0 times all six
+ * combinations.  The fastest is kept.  *chosen receives the lanes, ms (NULL
+ * allowed) the best time of 8, 16 and 32 lanes in that order (-1: not timed);
+ * edg_sector_info reports both choices. */
 int edg_sector_tune(edg_sector* s, int lanes_per_row, int* chosen, double* ms);
+
+/* Set both choices without timing: lanes_per_row 8, 16 or 32, cache_policy 1
+ * or 2.  Results do not depend on either; only the speed does. */
+int edg_sector_set_rows(edg_sector* s, int lanes_per_row, int cache_policy);
 
 /* Same with host buffers: copies v in, applies H, copies w out, synchronises.
  * This is the call the reference's sHv(v, w, ...) adapter makes. */

@@ -123,6 +123,41 @@ def test_stored_targets_equal_matrix_free(gpu):
     assert np.array_equal(sec.sHv(v), w0)
 
 
+@pytest.mark.parametrize("lanes", [8, 16, 32])
+@pytest.mark.parametrize("policy", [1, 2])
+def test_stored_rows_every_kernel_choice(gpu, lanes, policy):
+    """The lanes per row and the cache policy change speed only: FP64 equal to the
+    matrix-free kernel, FP32 within its tolerance, on a torus with chirality and J2."""
+    from ed_code_gb300 import lattice as L
+
+    model = L.make_model(L.TorusSpec("triangular", 5, 4, Jz=1.1, J2=0.3, Ch=0.2), 0, 2, 1)
+    sec = gpu.GpuSector(model)
+    v = O.splitmix_vector(sec.n_p, 5)
+    w0 = sec.sHv(v)
+    w0_32 = sec.sHv(v.astype(np.complex64), dtype=np.complex64).astype(np.complex128)
+    assert sec.build_targets()
+    sec.set_rows(lanes, policy)
+    assert sec.info["lanes_per_row"] == lanes and sec.info["cache_policy"] == policy
+    scale = max(1.0, np.abs(w0).max())
+    assert np.abs(sec.sHv(v) - w0).max() <= 1e-13 * scale
+    w32 = sec.sHv(v.astype(np.complex64), dtype=np.complex64).astype(np.complex128)
+    assert np.abs(w32 - w0).max() <= FP32_TOL * scale
+    assert np.abs(w32 - w0_32).max() <= FP32_TOL * scale
+
+
+def test_tune_keeps_a_valid_choice(gpu):
+    from ed_code_gb300 import lattice as L
+
+    sec = gpu.GpuSector(L.make_model(L.TorusSpec("triangular", 5, 4, Jz=1.0, Ch=0.1), 0, 0, 0))
+    assert sec.build_targets()
+    lanes, ms = sec.tune(0)
+    assert lanes in (8, 16, 32) and sec.info["lanes_per_row"] == lanes
+    assert sec.info["cache_policy"] in (1, 2)
+    assert (ms > 0).all()
+    lanes, ms = sec.tune(16)
+    assert lanes == 16 and ms[1] > 0 and ms[0] == -1 and ms[2] == -1
+
+
 def test_hv_device_equals_host(gpu):
     import torch
 
