@@ -58,6 +58,21 @@ class edg_sector_info(C.Structure):
     ]
 
 
+class edg_batch_opts(C.Structure):
+    _fields_ = [("tile_rows", C.c_int), ("lanes_per_row", C.c_int), ("check_every", C.c_int)]
+
+
+class edg_batch_request(C.Structure):
+    _fields_ = [("n_ev", C.c_int), ("max_iterations", C.c_int), ("tol", C.c_double), ("seed", C.c_uint64),
+                ("tag", C.c_int64)]
+
+
+class edg_batch_result(C.Structure):
+    _fields_ = [("tag", C.c_int64), ("status", C.c_int), ("n_found", C.c_int), ("iterations", C.c_int),
+                ("converged", C.c_int), ("eigs", C.c_double * 32), ("ritz", C.c_double * 32),
+                ("residuals", C.c_double * 32)]
+
+
 LOG_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_char_p)
 
 
@@ -98,6 +113,13 @@ SIGNATURES = {
     "edg_hv": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "edg_hv_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
     "edg_sector_set_rows": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "edg_batch_create": (C.c_int, [C.POINTER(edg_batch_opts), C.POINTER(C.c_void_p)]),
+    "edg_batch_destroy": (C.c_int, [C.c_void_p]),
+    "edg_batch_footprint": (C.c_int, [C.c_void_p, C.POINTER(edg_batch_request), C.POINTER(C.c_int64)]),
+    "edg_batch_add": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(edg_batch_request)]),
+    "edg_batch_step": (C.c_int, [C.c_void_p, C.c_int]),
+    "edg_batch_poll": (C.c_int, [C.c_void_p, C.POINTER(edg_batch_result), C.c_int, C.POINTER(C.c_int)]),
+    "edg_batch_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "edg_hv_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "edg_count_offdiag": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
     "edg_fill_random": (C.c_int, [C.c_void_p, C.c_int64, C.c_int, C.c_uint64, C.c_void_p]),

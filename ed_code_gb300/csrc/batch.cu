@@ -1,0 +1,699 @@
+// Batched mixed-precision Lanczos: many sectors of uneven dimension
+// ("segments") advanced together, one captured CUDA graph per Lanczos step for
+// all of them.
+//
+// Every segment is a sector with stored rows (targets.cu) and a request
+// (eigenvalues wanted, maximum steps, tolerance, seed).  Per segment the batch
+// keeps its FP32 Krylov vectors V_0..V_m, w, u = v/norm, its FP64 alpha/beta
+// and its own step counter and status in device memory, so segments join and
+// leave independently: a segment added while others are half way starts at
+// step 0 with the next graph.  The rows of all live segments are cut into
+// tiles of `tile_rows` rows, and each kernel below runs one CTA per tile that
+// reads its segment's descriptor:
+//
+//   u       u = V_j / norm
+//   hv      w = H V_j              (CSR rows, lanes_per_row lanes per row)
+//   dot     alpha_j = Re<V_j|w>    (tile partials; one CTA per segment sums
+//                                   its own tiles in order: deterministic, and
+//                                   independent of the other segments)
+//   step    w -= alpha_j V_j + beta_j V_{j-1}
+//   cgs     w -= sum_k <V_k|w> V_k over k <= j, twice (FP64 coefficients)
+//   norm    beta_{j+1} = |w|
+//   scale   V_{j+1} = w / beta_{j+1};  j += 1
+//   check   every check_every steps: the wanted Ritz pairs of T_j (bisection
+//           and inverse iteration in FP64, one CTA per segment); a segment
+//           whose residual bounds beta_j |y_k[j-1]| are all below
+//           tol * max(1, |theta_k|) stops, as does one that reached its
+//           maximum number of steps.
+//
+// The vectors are reorthogonalised every step: with FP32 vectors the copies
+// of converged levels otherwise appear within a few steps.  A stopped segment
+// is finished with the single-sector solver's code (MixedFinish): Ritz
+// vectors in FP64, one FP64 H*v each for the Rayleigh quotient (the returned
+// eigenvalue) and its residual.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstddef>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/edgpu.h"
+#include "blas1.cuh"
+#include "edg_sector.cuh"
+#include "tridiag.cuh"
+
+struct edg_sector {
+  edg::Sector s;
+};
+
+namespace edg {
+
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kMaxSteps = 511;  // Krylov vectors per segment: kMaxSteps + 1
+constexpr int kCgsY = 8;        // CTAs per tile over the Krylov index k
+constexpr int kBatchMaxEv = 32;
+
+enum { kRunning = 0, kConverged = 1, kMaxedOut = 2 };
+
+struct SegDev {
+  const uint64_t* row_ptr;
+  const uint32_t* col;
+  const uint16_t* vid;
+  const float2* vtab;
+  const double* ezz;
+  const uint8_t* lid;
+  const double* nrm;      // 65-entry tables in the sector's device parameters
+  const double* nrm_inv;
+  float2* V;              // (m_max + 1) x n
+  float2* w;
+  float2* u;
+  double* alpha;          // m_max + 1
+  double* beta;           // m_max + 2
+  double* q;              // 2 (m_max + 1): reorthogonalisation coefficients
+  double* ywork;          // want x 6 m_max: Ritz coefficients + inverse-iteration work
+  int64_t n;
+  int m_max, want, check_every, pad;
+  double tol;
+};
+
+struct SegState {
+  int j;       // steps taken
+  int status;  // kRunning, kConverged, kMaxedOut
+};
+
+struct TileDev {
+  int seg;
+  int rows;
+  int64_t row0;
+};
+
+__device__ __forceinline__ void block_sum2(double& a, double& b) {
+  __shared__ double sa[kThreads], sb[kThreads];
+  sa[threadIdx.x] = a;
+  sb[threadIdx.x] = b;
+  __syncthreads();
+  for (int h = kThreads / 2; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) {
+      sa[threadIdx.x] += sa[threadIdx.x + h];
+      sb[threadIdx.x] += sb[threadIdx.x + h];
+    }
+    __syncthreads();
+  }
+  a = sa[0];
+  b = sb[0];
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(kThreads) k_b_u(const SegDev* __restrict__ segs, const SegState* __restrict__ ss,
+                                                  const TileDev* __restrict__ tiles) {
+  const TileDev t = tiles[blockIdx.x];
+  if (ss[t.seg].status != kRunning) return;
+  const SegDev& S = segs[t.seg];
+  const float2* v = S.V + (int64_t)ss[t.seg].j * S.n;
+  for (int r = threadIdx.x; r < t.rows; r += blockDim.x) {
+    const int64_t i = t.row0 + r;
+    const float s = (float)S.nrm_inv[S.lid[i]];
+    const float2 x = v[i];
+    S.u[i] = make_float2(x.x * s, x.y * s);
+  }
+}
+
+// w = H V_j on the tile's rows: 32/LPR rows per warp, LPR lanes per row
+template <int LPR>
+__global__ void __launch_bounds__(kThreads) k_b_hv(const SegDev* __restrict__ segs, const SegState* __restrict__ ss,
+                                                   const TileDev* __restrict__ tiles) {
+  const TileDev t = tiles[blockIdx.x];
+  if (ss[t.seg].status != kRunning) return;
+  const SegDev& S = segs[t.seg];
+  constexpr int kRowsPerWarp = 32 / LPR;
+  const int lane = threadIdx.x & 31, sl = lane % LPR, sub = lane / LPR, wid = threadIdx.x >> 5;
+  const float2* v = S.V + (int64_t)ss[t.seg].j * S.n;
+  const int rows_per_pass = (kThreads / 32) * kRowsPerWarp;
+  for (int r0 = 0; r0 < t.rows; r0 += rows_per_pass) {
+    const int r = r0 + wid * kRowsPerWarp + sub;
+    const bool ok = r < t.rows;
+    const int64_t i = t.row0 + (ok ? r : 0);
+    const uint64_t beg = ok ? S.row_ptr[i] : 0, end = ok ? S.row_ptr[i + 1] : 0;
+    float ar = 0.f, ai = 0.f;
+    for (uint64_t e = beg + sl; e < end; e += LPR) {
+      const float2 c = __ldg(S.vtab + __ldg(S.vid + e));
+      const float2 x = S.u[__ldg(S.col + e)];
+      ar += c.x * x.x - c.y * x.y;
+      ai += c.x * x.y + c.y * x.x;
+    }
+#pragma unroll
+    for (int o = LPR / 2; o > 0; o >>= 1) {
+      ar += __shfl_down_sync(0xffffffffu, ar, o, LPR);
+      ai += __shfl_down_sync(0xffffffffu, ai, o, LPR);
+    }
+    if (ok && sl == 0) {
+      const float ni = (float)S.nrm[S.lid[i]];
+      const float d = (float)S.ezz[i];
+      const float2 vi = v[i];
+      S.w[i] = make_float2(ar * ni + d * vi.x, ai * ni + d * vi.y);
+    }
+  }
+}
+
+// tile partials of <V_j|w> (mode 0) or |w|^2 (mode 1), FP64 compensated
+__global__ void __launch_bounds__(kThreads) k_b_dot(const SegDev* __restrict__ segs, const SegState* __restrict__ ss,
+                                                    const TileDev* __restrict__ tiles, double* __restrict__ part,
+                                                    int mode) {
+  const TileDev t = tiles[blockIdx.x];
+  double a = 0, b = 0;
+  if (ss[t.seg].status == kRunning) {
+    const SegDev& S = segs[t.seg];
+    const float2* v = S.V + (int64_t)ss[t.seg].j * S.n;
+    Acc sr, si;
+    for (int r = threadIdx.x; r < t.rows; r += blockDim.x) {
+      const int64_t i = t.row0 + r;
+      const float2 y = S.w[i];
+      if (mode == 0) {
+        const float2 x = v[i];
+        sr.add((double)x.x * y.x + (double)x.y * y.y);
+        si.add((double)x.x * y.y - (double)x.y * y.x);
+      } else {
+        sr.add((double)y.x * y.x + (double)y.y * y.y);
+      }
+    }
+    a = sr.value();
+    b = si.value();
+  }
+  block_sum2(a, b);
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = a;
+    part[2 * blockIdx.x + 1] = b;
+  }
+}
+
+// one CTA per segment sums its tiles' partials in order:
+// mode 0 -> alpha_j, mode 1 -> beta_{j+1} = sqrt
+__global__ void __launch_bounds__(kThreads) k_b_finish(const SegDev* __restrict__ segs,
+                                                       const SegState* __restrict__ ss, const int* __restrict__ tb,
+                                                       const double* __restrict__ part, int mode) {
+  if (ss[blockIdx.x].status != kRunning) return;
+  const SegDev& S = segs[blockIdx.x];
+  const int j = ss[blockIdx.x].j;
+  double a = 0, b = 0;
+  for (int k = tb[blockIdx.x] + threadIdx.x; k < tb[blockIdx.x + 1]; k += blockDim.x) {
+    a += part[2 * k];
+    b += part[2 * k + 1];
+  }
+  block_sum2(a, b);
+  if (threadIdx.x == 0) {
+    if (mode == 0) S.alpha[j] = a;
+    else S.beta[j + 1] = sqrt(a);
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_b_step(const SegDev* __restrict__ segs, const SegState* __restrict__ ss,
+                                                     const TileDev* __restrict__ tiles) {
+  const TileDev t = tiles[blockIdx.x];
+  if (ss[t.seg].status != kRunning) return;
+  const SegDev& S = segs[t.seg];
+  const int j = ss[t.seg].j;
+  const double a = S.alpha[j], b = j > 0 ? S.beta[j] : 0.0;
+  const float2* v = S.V + (int64_t)j * S.n;
+  const float2* vp = j > 0 ? v - S.n : nullptr;
+  for (int r = threadIdx.x; r < t.rows; r += blockDim.x) {
+    const int64_t i = t.row0 + r;
+    const float2 y = S.w[i], x = v[i];
+    double re = (double)y.x - a * x.x, im = (double)y.y - a * x.y;
+    if (vp) {
+      const float2 p = vp[i];
+      re -= b * p.x;
+      im -= b * p.y;
+    }
+    S.w[i] = make_float2((float)re, (float)im);
+  }
+}
+
+// tile partials of <V_k|w> for k <= j; CTA (tile, y) takes k = y, y + kCgsY, ...
+__global__ void __launch_bounds__(kThreads) k_b_cgs_dot(const SegDev* __restrict__ segs,
+                                                        const SegState* __restrict__ ss,
+                                                        const TileDev* __restrict__ tiles, int n_tiles,
+                                                        double* __restrict__ part) {
+  const TileDev t = tiles[blockIdx.x];
+  const SegDev& S = segs[t.seg];
+  const int K = ss[t.seg].status == kRunning ? ss[t.seg].j + 1 : 0;
+  for (int k = blockIdx.y; k < K; k += kCgsY) {  // K is the same for every thread of the CTA
+    const float2* vk = S.V + (int64_t)k * S.n;
+    Acc sr, si;
+    for (int r = threadIdx.x; r < t.rows; r += blockDim.x) {
+      const int64_t i = t.row0 + r;
+      const float2 x = vk[i], y = S.w[i];
+      sr.add((double)x.x * y.x + (double)x.y * y.y);
+      si.add((double)x.x * y.y - (double)x.y * y.x);
+    }
+    double a = sr.value(), b = si.value();
+    block_sum2(a, b);
+    if (threadIdx.x == 0) {
+      const int64_t o = ((int64_t)k * n_tiles + blockIdx.x) * 2;
+      part[o] = a;
+      part[o + 1] = b;
+    }
+  }
+}
+
+// CTA (segment, y): q_k = sum of the segment's tile partials, k = y, y + kCgsY, ...
+__global__ void __launch_bounds__(kThreads) k_b_cgs_finish(const SegDev* __restrict__ segs,
+                                                           const SegState* __restrict__ ss,
+                                                           const int* __restrict__ tb, int n_tiles,
+                                                           const double* __restrict__ part) {
+  if (ss[blockIdx.x].status != kRunning) return;
+  const SegDev& S = segs[blockIdx.x];
+  const int K = ss[blockIdx.x].j + 1;
+  for (int k = blockIdx.y; k < K; k += kCgsY) {
+    double a = 0, b = 0;
+    for (int t = tb[blockIdx.x] + threadIdx.x; t < tb[blockIdx.x + 1]; t += blockDim.x) {
+      a += part[((int64_t)k * n_tiles + t) * 2];
+      b += part[((int64_t)k * n_tiles + t) * 2 + 1];
+    }
+    block_sum2(a, b);
+    if (threadIdx.x == 0) {
+      S.q[2 * k] = a;
+      S.q[2 * k + 1] = b;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_b_cgs_sub(const SegDev* __restrict__ segs,
+                                                        const SegState* __restrict__ ss,
+                                                        const TileDev* __restrict__ tiles) {
+  const TileDev t = tiles[blockIdx.x];
+  if (ss[t.seg].status != kRunning) return;
+  const SegDev& S = segs[t.seg];
+  __shared__ double sq[2 * (kMaxSteps + 1)];
+  const int K = ss[t.seg].j + 1;
+  for (int k = threadIdx.x; k < 2 * K; k += blockDim.x) sq[k] = S.q[k];
+  __syncthreads();
+  for (int r = threadIdx.x; r < t.rows; r += blockDim.x) {
+    const int64_t i = t.row0 + r;
+    const float2 y = S.w[i];
+    double re = y.x, im = y.y;
+    for (int k = 0; k < K; ++k) {
+      const float2 x = S.V[(int64_t)k * S.n + i];
+      re -= sq[2 * k] * x.x - sq[2 * k + 1] * x.y;
+      im -= sq[2 * k] * x.y + sq[2 * k + 1] * x.x;
+    }
+    S.w[i] = make_float2((float)re, (float)im);
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_b_scale(const SegDev* __restrict__ segs,
+                                                      const SegState* __restrict__ ss,
+                                                      const TileDev* __restrict__ tiles) {
+  const TileDev t = tiles[blockIdx.x];
+  if (ss[t.seg].status != kRunning) return;
+  const SegDev& S = segs[t.seg];
+  const int j = ss[t.seg].j;
+  const double s = 1.0 / S.beta[j + 1];
+  float2* vn = S.V + (int64_t)(j + 1) * S.n;
+  for (int r = threadIdx.x; r < t.rows; r += blockDim.x) {
+    const int64_t i = t.row0 + r;
+    const float2 y = S.w[i];
+    vn[i] = make_float2((float)(y.x * s), (float)(y.y * s));
+  }
+}
+
+__global__ void k_b_advance(const SegDev* __restrict__ segs, SegState* __restrict__ ss, int n_seg) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n_seg && ss[s].status == kRunning) {
+    ss[s].j += 1;
+    if (ss[s].j >= segs[s].m_max) ss[s].status = kMaxedOut;
+  }
+}
+
+// Convergence test, one CTA per segment, every check_every steps: the wanted
+// lowest Ritz pairs of T_j and their residual bounds beta_j |y_k[j-1]|.
+__global__ void __launch_bounds__(128) k_b_check(const SegDev* __restrict__ segs, SegState* __restrict__ ss) {
+  const SegDev& S = segs[blockIdx.x];
+  const int j = ss[blockIdx.x].j;
+  if (ss[blockIdx.x].status != kRunning || S.tol <= 0 || j % S.check_every != 0 || j < 2 * S.want + 2) return;
+  __shared__ double d[kMaxSteps + 1], e[kMaxSteps + 1];
+  __shared__ int ok;
+  for (int i = threadIdx.x; i < j; i += blockDim.x) {
+    d[i] = S.alpha[i];
+    e[i] = i > 0 ? S.beta[i] : 0.0;
+  }
+  if (threadIdx.x == 0) ok = 1;
+  __syncthreads();
+  for (int k = threadIdx.x; k < S.want; k += blockDim.x) {
+    const double th = tridiag_eigenvalue(d, e, j, k);
+    double* y = S.ywork + (int64_t)k * 6 * S.m_max;
+    tridiag_eigenvector(d, e, j, th, y, y + S.m_max);
+    if (S.beta[j] * fabs(y[j - 1]) > S.tol * fmax(1.0, fabs(th))) ok = 0;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && ok) ss[blockIdx.x].status = kConverged;
+}
+
+// start vector V_0 = x / |x| of one segment (one CTA: the norm is FP64 compensated)
+__global__ void __launch_bounds__(kThreads) k_b_start(float2* __restrict__ V0, const float2* __restrict__ x,
+                                                      int64_t n) {
+  Acc s;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s.add((double)x[i].x * x[i].x + (double)x[i].y * x[i].y);
+  double a = s.value(), b = 0;
+  block_sum2(a, b);
+  const double inv = 1.0 / sqrt(a);
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x)
+    V0[i] = make_float2((float)(x[i].x * inv), (float)(x[i].y * inv));
+}
+
+struct Segment {
+  edg_sector* sec = nullptr;
+  edg_batch_request req{};
+  SegDev d{};
+  SegState st{};
+  int64_t bytes = 0;
+};
+
+void release(Segment& g) {
+  void* p[] = {g.d.V, g.d.w, g.d.u, g.d.alpha, g.d.beta, g.d.q, g.d.ywork};
+  for (void* x : p)
+    if (x) cudaFree(x);
+  g.d = SegDev{};
+}
+
+}  // namespace
+
+struct Batch {
+  edg_batch_opts opts{};
+  std::vector<Segment> segs;  // the first n_dev are in the device tables, in order
+  std::vector<edg_batch_result> done;
+  cudaStream_t st = nullptr;
+  SegDev* d_segs = nullptr;
+  SegState* d_state = nullptr;
+  TileDev* d_tiles = nullptr;
+  int* d_tb = nullptr;
+  double* d_part = nullptr;
+  size_t part_cap = 0;
+  int n_tiles = 0, n_dev = 0;
+  bool dirty = true;
+  cudaGraphExec_t graph = nullptr;
+  int64_t device_bytes = 0, steps = 0;
+  MixedFinish fin;
+
+  ~Batch() {
+    if (st) cudaStreamSynchronize(st);
+    if (graph) cudaGraphExecDestroy(graph);
+    for (Segment& g : segs) release(g);
+    cudaFree(d_segs);
+    cudaFree(d_state);
+    cudaFree(d_tiles);
+    cudaFree(d_tb);
+    cudaFree(d_part);
+    if (st) cudaStreamDestroy(st);
+  }
+};
+
+namespace {
+
+int64_t segment_bytes(int64_t n, int m, int want) {
+  return (int64_t)sizeof(float2) * n * (m + 3) + (int64_t)sizeof(double) * (4 * (m + 2) + 6 * (int64_t)want * m);
+}
+
+// copy the device step counters and statuses into the host mirror
+cudaError_t pull_state(Batch& B) {
+  if (!B.n_dev) return cudaSuccess;
+  std::vector<SegState> h(B.n_dev);
+  cudaError_t e = cudaMemcpyAsync(h.data(), B.d_state, sizeof(SegState) * B.n_dev, cudaMemcpyDeviceToHost, B.st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(B.st);
+  if (e != cudaSuccess) return e;
+  for (int k = 0; k < B.n_dev; ++k) B.segs[k].st = h[k];
+  return cudaSuccess;
+}
+
+// finish every stopped segment: Ritz values, FP64 Rayleigh quotients, residuals
+void finish_stopped(Batch& B) {
+  std::vector<Segment> keep;
+  for (size_t k = 0; k < B.segs.size(); ++k) {
+    Segment& g = B.segs[k];
+    if (g.st.status == kRunning) {
+      keep.push_back(g);
+      continue;
+    }
+    edg_batch_result r{};
+    r.tag = g.req.tag;
+    r.iterations = g.st.j;
+    r.converged = g.st.status == kConverged;
+    const int m = g.st.j, n_try = std::min(kBatchMaxEv, std::min(g.req.n_ev + 4, m));
+    const int64_t n = g.d.n;
+    int na = 0, rc = EDG_OK;
+    std::vector<int> acc_h;
+    std::vector<double> th, rr;
+    if (B.fin.reserve(n, m) != cudaSuccess) rc = fail(EDG_ERR_NOMEM, "batch: finishing scratch");
+    if (rc == EDG_OK) rc = B.fin.tridiag(B.st, g.d.alpha, g.d.beta, m, n_try, &na, acc_h, th);
+    if (rc == EDG_OK && na == 0) rc = fail(EDG_ERR_NOT_CONVERGED, "batch: no Ritz value survived the copy test");
+    if (rc == EDG_OK && B.fin.reserve_x(n, na) != cudaSuccess) rc = fail(EDG_ERR_NOMEM, "batch: FP64 Ritz vectors");
+    if (rc == EDG_OK) rc = B.fin.ritz_stored(B.st, g.d.V, n, m, na);
+    if (rc == EDG_OK) rc = B.fin.rayleigh(g.sec->s, B.st, n, na, rr);
+    if (rc == EDG_OK) {
+      std::vector<int> sel;
+      pick_levels(rr, th, acc_h, na, g.req.n_ev, r.eigs, r.ritz, r.residuals, sel);
+      r.n_found = (int)sel.size();
+    }
+    r.status = rc;
+    B.done.push_back(r);
+    B.device_bytes -= g.bytes;
+    release(g);
+    B.dirty = true;
+  }
+  B.segs.swap(keep);
+}
+
+// upload the tables of the current segments and capture one step as a graph
+int rebuild(Batch& B) {
+  if (B.graph) {
+    cudaGraphExecDestroy(B.graph);
+    B.graph = nullptr;
+  }
+  std::vector<SegDev> sd;
+  std::vector<SegState> ss;
+  std::vector<TileDev> tiles;
+  std::vector<int> tb;
+  const int rows = B.opts.tile_rows;
+  int m_cap = 1;
+  for (size_t k = 0; k < B.segs.size(); ++k) {
+    sd.push_back(B.segs[k].d);
+    ss.push_back(B.segs[k].st);
+    m_cap = std::max(m_cap, B.segs[k].d.m_max);
+    tb.push_back((int)tiles.size());
+    for (int64_t r0 = 0; r0 < B.segs[k].d.n; r0 += rows)
+      tiles.push_back(TileDev{(int)k, (int)std::min<int64_t>(rows, B.segs[k].d.n - r0), r0});
+  }
+  tb.push_back((int)tiles.size());
+  cudaFree(B.d_segs);
+  cudaFree(B.d_state);
+  cudaFree(B.d_tiles);
+  cudaFree(B.d_tb);
+  B.d_segs = nullptr;
+  B.d_state = nullptr;
+  B.d_tiles = nullptr;
+  B.d_tb = nullptr;
+  B.n_tiles = (int)tiles.size();
+  B.n_dev = 0;
+  B.dirty = false;
+  if (sd.empty()) return EDG_OK;
+  const size_t need_part = (size_t)2 * B.n_tiles * (m_cap + 1);
+  if (need_part > B.part_cap) {
+    cudaFree(B.d_part);
+    B.d_part = nullptr;
+    B.part_cap = 0;
+    if (cudaMalloc(&B.d_part, sizeof(double) * need_part) != cudaSuccess) return EDG_ERR_NOMEM;
+    B.part_cap = need_part;
+  }
+  if (cudaMalloc(&B.d_segs, sizeof(SegDev) * sd.size()) != cudaSuccess ||
+      cudaMalloc(&B.d_state, sizeof(SegState) * ss.size()) != cudaSuccess ||
+      cudaMalloc(&B.d_tiles, sizeof(TileDev) * tiles.size()) != cudaSuccess ||
+      cudaMalloc(&B.d_tb, sizeof(int) * tb.size()) != cudaSuccess)
+    return EDG_ERR_NOMEM;
+  cudaMemcpyAsync(B.d_segs, sd.data(), sizeof(SegDev) * sd.size(), cudaMemcpyHostToDevice, B.st);
+  cudaMemcpyAsync(B.d_state, ss.data(), sizeof(SegState) * ss.size(), cudaMemcpyHostToDevice, B.st);
+  cudaMemcpyAsync(B.d_tiles, tiles.data(), sizeof(TileDev) * tiles.size(), cudaMemcpyHostToDevice, B.st);
+  cudaMemcpyAsync(B.d_tb, tb.data(), sizeof(int) * tb.size(), cudaMemcpyHostToDevice, B.st);
+  if (cudaStreamSynchronize(B.st) != cudaSuccess) return EDG_ERR_CUDA;  // the host vectors go out of scope
+  B.n_dev = (int)sd.size();
+  const int nt = B.n_tiles, ns = B.n_dev, lpr = B.opts.lanes_per_row;
+  cudaGraph_t g;
+  if (cudaStreamBeginCapture(B.st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return EDG_ERR_CUDA;
+  k_b_u<<<nt, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles);
+  if (lpr == 8) k_b_hv<8><<<nt, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles);
+  else if (lpr == 32) k_b_hv<32><<<nt, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles);
+  else k_b_hv<16><<<nt, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles);
+  k_b_dot<<<nt, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles, B.d_part, 0);
+  k_b_finish<<<ns, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tb, B.d_part, 0);
+  k_b_step<<<nt, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles);
+  for (int pass = 0; pass < 2; ++pass) {
+    k_b_cgs_dot<<<dim3(nt, kCgsY), kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles, nt, B.d_part);
+    k_b_cgs_finish<<<dim3(ns, kCgsY), kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tb, nt, B.d_part);
+    k_b_cgs_sub<<<nt, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles);
+  }
+  k_b_dot<<<nt, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles, B.d_part, 1);
+  k_b_finish<<<ns, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tb, B.d_part, 1);
+  k_b_scale<<<nt, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles);
+  k_b_advance<<<(ns + 127) / 128, 128, 0, B.st>>>(B.d_segs, B.d_state, ns);
+  k_b_check<<<ns, 128, 0, B.st>>>(B.d_segs, B.d_state);
+  cudaError_t e = cudaStreamEndCapture(B.st, &g);
+  if (e != cudaSuccess) return EDG_ERR_CUDA;
+  e = cudaGraphInstantiate(&B.graph, g, 0);
+  cudaGraphDestroy(g);
+  return e == cudaSuccess ? EDG_OK : EDG_ERR_CUDA;
+}
+
+// statuses back from the device; stopped segments finished; tables rebuilt
+int settle(Batch& B) {
+  cudaError_t e = pull_state(B);
+  if (e != cudaSuccess) return cuda_fail(e, "batch: step counters");
+  for (int k = 0; k < B.n_dev; ++k)
+    if (B.segs[k].st.status != kRunning) B.dirty = true;
+  if (!B.dirty) return EDG_OK;
+  finish_stopped(B);
+  const int rc = rebuild(B);
+  return rc == EDG_OK ? EDG_OK : fail(rc, "batch: rebuilding the step graph failed");
+}
+
+}  // namespace
+
+}  // namespace edg
+
+using namespace edg;
+
+struct edg_batch {
+  Batch b;
+};
+
+extern "C" {
+
+int edg_batch_create(const edg_batch_opts* opts, edg_batch** out) {
+  if (!out) return fail(EDG_ERR_INVALID, "NULL argument");
+  edg_batch* h = new edg_batch();
+  if (opts) h->b.opts = *opts;
+  edg_batch_opts& o = h->b.opts;
+  if (o.tile_rows <= 0) o.tile_rows = 1024;
+  o.tile_rows = std::max(32, std::min(o.tile_rows, 1 << 20));
+  if (o.lanes_per_row != 8 && o.lanes_per_row != 16 && o.lanes_per_row != 32) o.lanes_per_row = 8;
+  if (o.check_every <= 0) o.check_every = 10;
+  if (cudaStreamCreateWithFlags(&h->b.st, cudaStreamNonBlocking) != cudaSuccess) {
+    delete h;
+    return fail(EDG_ERR_CUDA, "batch stream");
+  }
+  *out = h;
+  return EDG_OK;
+}
+
+int edg_batch_destroy(edg_batch* b) {
+  delete b;
+  return EDG_OK;
+}
+
+int edg_batch_footprint(const edg_sector* s, const edg_batch_request* req, int64_t* bytes) {
+  if (!s || !req || !bytes) return fail(EDG_ERR_INVALID, "NULL argument");
+  const int m = (int)std::min<int64_t>(std::max(2, req->max_iterations), s->s.P.n_p);
+  *bytes = segment_bytes(s->s.P.n_p, m, std::min(std::max(1, req->n_ev), m));
+  return EDG_OK;
+}
+
+int edg_batch_add(edg_batch* bh, edg_sector* sec, const edg_batch_request* req) {
+  if (!bh || !sec || !req) return fail(EDG_ERR_INVALID, "NULL argument");
+  Batch& B = bh->b;
+  Sector& S = sec->s;
+  if (!S.col) return fail(EDG_ERR_INVALID, "batch segments need stored rows (edg_sector_build_targets)");
+  if (req->n_ev < 1 || req->n_ev > kBatchMaxEv) return fail(EDG_ERR_INVALID, "n_ev must be in [1, 32]");
+  if (req->max_iterations < 2 || req->max_iterations > kMaxSteps)
+    return fail(EDG_ERR_INVALID, "max_iterations must be in [2, 511]");
+  const int64_t n = S.P.n_p;
+  Segment g;
+  g.sec = sec;
+  g.req = *req;
+  const int m = (int)std::min<int64_t>(req->max_iterations, n);
+  if (m < 2) return fail(EDG_ERR_INVALID, "batch: the sector needs at least 2 states");
+  g.req.max_iterations = m;
+  SegDev& d = g.d;
+  d.row_ptr = S.row_ptr;
+  d.col = S.col;
+  d.vid = S.vid;
+  d.vtab = S.vtab32;
+  d.ezz = S.ezz;
+  d.lid = S.lid;
+  d.nrm = reinterpret_cast<const double*>(reinterpret_cast<const char*>(S.dP) + offsetof(SectorParams, nrm));
+  d.nrm_inv = reinterpret_cast<const double*>(reinterpret_cast<const char*>(S.dP) + offsetof(SectorParams, nrm_inv));
+  d.n = n;
+  d.m_max = m;
+  d.want = std::min(req->n_ev, m);
+  d.check_every = B.opts.check_every;
+  d.tol = req->tol;
+  cudaError_t e = cudaMalloc(&d.V, sizeof(float2) * n * (m + 1));
+  if (e == cudaSuccess) e = cudaMalloc(&d.w, sizeof(float2) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&d.u, sizeof(float2) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&d.alpha, sizeof(double) * (m + 1));
+  if (e == cudaSuccess) e = cudaMalloc(&d.beta, sizeof(double) * (m + 2));
+  if (e == cudaSuccess) e = cudaMalloc(&d.q, sizeof(double) * 2 * (m + 1));
+  if (e == cudaSuccess) e = cudaMalloc(&d.ywork, sizeof(double) * 6 * (size_t)d.want * m);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    release(g);
+    return fail(EDG_ERR_NOMEM, "batch: the segment's vectors do not fit");
+  }
+  g.bytes = segment_bytes(n, m, d.want);
+  // start vector: the splitmix64 stream of edg_fill_random with this seed, normalised
+  const int rc = edg_fill_random(d.w, n, EDG_C64, req->seed, B.st);
+  if (rc != EDG_OK) {
+    release(g);
+    return rc;
+  }
+  k_b_start<<<1, kThreads, 0, B.st>>>(d.V, d.w, n);
+  cudaMemsetAsync(d.beta, 0, sizeof(double) * (m + 2), B.st);
+  if ((e = cudaGetLastError()) != cudaSuccess) {
+    release(g);
+    return cuda_fail(e, "batch: start vector");
+  }
+  B.segs.push_back(g);
+  B.device_bytes += g.bytes;
+  B.dirty = true;
+  return EDG_OK;
+}
+
+int edg_batch_step(edg_batch* bh, int n_steps) {
+  if (!bh) return fail(EDG_ERR_INVALID, "NULL batch");
+  Batch& B = bh->b;
+  int rc = EDG_OK;
+  for (int s = 0; s < n_steps && rc == EDG_OK; ++s) {
+    if (B.dirty && (rc = settle(B)) != EDG_OK) break;
+    if (B.n_dev == 0) break;
+    const cudaError_t e = cudaGraphLaunch(B.graph, B.st);
+    if (e != cudaSuccess) return cuda_fail(e, "batch step");
+    ++B.steps;
+    if (B.steps % B.opts.check_every == 0) rc = settle(B);
+  }
+  if (rc == EDG_OK) rc = settle(B);
+  return rc;
+}
+
+int edg_batch_poll(edg_batch* bh, edg_batch_result* out, int cap, int* n_out) {
+  if (!bh || !n_out || (cap > 0 && !out)) return fail(EDG_ERR_INVALID, "NULL argument");
+  Batch& B = bh->b;
+  const int n = std::max(0, std::min<int>(cap, (int)B.done.size()));
+  for (int k = 0; k < n; ++k) out[k] = B.done[k];
+  B.done.erase(B.done.begin(), B.done.begin() + n);
+  *n_out = n;
+  return EDG_OK;
+}
+
+int edg_batch_info(const edg_batch* bh, int* n_active, int64_t* device_bytes, int64_t* steps) {
+  if (!bh) return fail(EDG_ERR_INVALID, "NULL batch");
+  if (n_active) *n_active = (int)bh->b.segs.size();
+  if (device_bytes) *device_bytes = bh->b.device_bytes;
+  if (steps) *steps = bh->b.steps;
+  return EDG_OK;
+}
+
+}  // extern "C"

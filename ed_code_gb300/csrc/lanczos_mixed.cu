@@ -218,6 +218,68 @@ __global__ void __launch_bounds__(kRedThreads) k_rq_partial(const double2* __res
   }
 }
 
+// X_q = sum_j y[q*m + j] V_j for q in [q0, q0 + qn), qn <= kRitzChunk, in FP64:
+// each V_j is read once per chunk of Ritz vectors.
+constexpr int kRitzChunk = 8;
+__global__ void __launch_bounds__(256) k_ritz_vectors(double2* __restrict__ X, int64_t n,
+                                                      const float2* __restrict__ V, int64_t ldv,
+                                                      const double* __restrict__ y, int m, int q0, int qn) {
+  extern __shared__ double sy[];  // qn * m
+  for (int k = threadIdx.x; k < qn * m; k += blockDim.x) sy[k] = y[(int64_t)q0 * m + k];
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double ar[kRitzChunk], ai[kRitzChunk];
+#pragma unroll
+    for (int q = 0; q < kRitzChunk; ++q) ar[q] = ai[q] = 0.0;
+    for (int j = 0; j < m; ++j) {
+      const float2 v = V[(int64_t)j * ldv + i];
+#pragma unroll
+      for (int q = 0; q < kRitzChunk; ++q)
+        if (q < qn) {
+          ar[q] += sy[q * m + j] * v.x;
+          ai[q] += sy[q * m + j] * v.y;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < kRitzChunk; ++q)
+      if (q < qn) X[(int64_t)(q0 + q) * n + i] = make_double2(ar[q], ai[q]);
+  }
+}
+
+// Sum k_rq_partial's partials in one CTA.  mode 0: out = {|x|^2, <x|Hx>,
+// theta = <x|Hx>/|x|^2}; mode 1: out[3] = |Hx - theta x| / |x|.
+__global__ void __launch_bounds__(kRedThreads) k_rq_sum(const double* __restrict__ part, int nb, double* out,
+                                                        int mode) {
+  __shared__ double s0[kRedThreads], s1[kRedThreads], s2[kRedThreads];
+  double a = 0, b = 0, c = 0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    a += part[3 * i];
+    b += part[3 * i + 1];
+    c += part[3 * i + 2];
+  }
+  s0[threadIdx.x] = a;
+  s1[threadIdx.x] = b;
+  s2[threadIdx.x] = c;
+  __syncthreads();
+  for (int h = kRedThreads / 2; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) {
+      s0[threadIdx.x] += s0[threadIdx.x + h];
+      s1[threadIdx.x] += s1[threadIdx.x + h];
+      s2[threadIdx.x] += s2[threadIdx.x + h];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    if (mode == 0) {
+      out[0] = s0[0];
+      out[1] = s1[0];
+      out[2] = s1[0] / s0[0];
+    } else {
+      out[3] = sqrt(s2[0] / out[0]);
+    }
+  }
+}
+
 int grid_n(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16)); }
 
 struct Dev {
@@ -235,6 +297,103 @@ struct Dev {
 
 }  // namespace
 
+MixedFinish::~MixedFinish() {
+  void* p[] = {theta, theta_hat, y, work, acc, nacc, X, HX, part, res};
+  for (void* q : p)
+    if (q) cudaFree(q);
+}
+
+cudaError_t MixedFinish::reserve(int64_t n, int m) {
+  auto grow = [](void** p, size_t bytes, size_t& have) -> cudaError_t {
+    if (bytes <= have) return cudaSuccess;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    have = 0;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e == cudaSuccess) have = bytes;
+    return e;
+  };
+  cudaError_t e = cudaSuccess;
+  if (!theta) {
+    if ((e = cudaMalloc(&theta, sizeof(double) * kCand)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&theta_hat, sizeof(double) * kCand)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&acc, sizeof(int) * kMaxEv)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&nacc, sizeof(int))) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&part, sizeof(double) * 3 * kRedBlocks)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&res, sizeof(double) * 4 * kMaxEv)) != cudaSuccess) return e;
+  }
+  if ((e = grow((void**)&y, sizeof(double) * kMaxEv * m, y_bytes)) != cudaSuccess) return e;
+  if ((e = grow((void**)&work, sizeof(double) * kMaxEv * 5 * m, work_bytes)) != cudaSuccess) return e;
+  if ((e = grow((void**)&HX, sizeof(double2) * n, hx_bytes)) != cudaSuccess) return e;
+  return cudaSuccess;
+}
+
+cudaError_t MixedFinish::reserve_x(int64_t n, int na) {
+  if (sizeof(double2) * n * na <= x_bytes) return cudaSuccess;
+  if (X) cudaFree(X);
+  X = nullptr;
+  x_bytes = 0;
+  cudaError_t e = cudaMalloc(&X, sizeof(double2) * n * na);
+  if (e == cudaSuccess) x_bytes = sizeof(double2) * n * na;
+  return e;
+}
+
+int MixedFinish::tridiag(cudaStream_t st, const double* alpha, const double* beta, int m, int n_try, int* na,
+                         std::vector<int>& acc_h, std::vector<double>& th) {
+  k_tridiag<<<1, 128, sizeof(double) * 2 * m, st>>>(alpha, beta, m, n_try, theta, theta_hat, y, work, acc, nacc);
+  acc_h.assign(kMaxEv, 0);
+  th.assign(kCand, 0.0);
+  cudaMemcpyAsync(na, nacc, sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(acc_h.data(), acc, sizeof(int) * kMaxEv, cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(th.data(), theta, sizeof(double) * std::min(kCand, m), cudaMemcpyDeviceToHost, st);
+  const cudaError_t e = cudaStreamSynchronize(st);
+  return e == cudaSuccess ? EDG_OK : cuda_fail(e, "mixed Lanczos: T");
+}
+
+int MixedFinish::ritz_stored(cudaStream_t st, const float2* V, int64_t n, int m, int na) {
+  for (int q0 = 0; q0 < na; q0 += kRitzChunk) {
+    const int qn = std::min(kRitzChunk, na - q0);
+    k_ritz_vectors<<<grid_n(n), 256, sizeof(double) * qn * m, st>>>(X, n, V, n, y, m, q0, qn);
+  }
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? EDG_OK : cuda_fail(e, "mixed Lanczos: Ritz vectors");
+}
+
+int MixedFinish::rayleigh(Sector& S, cudaStream_t st, int64_t n, int na, std::vector<double>& out) {
+  for (int q = 0; q < na; ++q) {
+    double2* x = X + (int64_t)q * n;
+    cudaError_t e = launch_hv(S, x, HX, true, st);
+    if (e != cudaSuccess) return cuda_fail(e, "mixed Lanczos: FP64 H*v");
+    k_rq_partial<<<kRedBlocks, kRedThreads, 0, st>>>(x, HX, n, nullptr, part);
+    k_rq_sum<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, res + 4 * q, 0);
+    k_rq_partial<<<kRedBlocks, kRedThreads, 0, st>>>(x, HX, n, res + 4 * q + 2, part);
+    k_rq_sum<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, res + 4 * q, 1);
+  }
+  out.assign(4 * (size_t)na, 0.0);
+  cudaMemcpyAsync(out.data(), res, sizeof(double) * 4 * na, cudaMemcpyDeviceToHost, st);
+  const cudaError_t e = cudaStreamSynchronize(st);
+  return e == cudaSuccess ? EDG_OK : cuda_fail(e, "mixed Lanczos: residual");
+}
+
+// A Rayleigh quotient within 1e-8 relative of an earlier one is the same level
+// again (a copy that slipped through the test on T) and is dropped.
+void pick_levels(const std::vector<double>& rr, const std::vector<double>& th, const std::vector<int>& acc_h, int na,
+                 int want, double* eigs, double* ritz, double* resid, std::vector<int>& keep) {
+  keep.clear();
+  for (int q = 0; q < na; ++q) {
+    const double rq = rr[4 * q + 2];
+    bool dup = false;
+    for (int k : keep)
+      if (std::fabs(rr[4 * k + 2] - rq) <= 1e-8 * std::fabs(rq)) dup = true;
+    if (dup || (int)keep.size() >= want) continue;
+    const int slot = (int)keep.size();
+    keep.push_back(q);
+    eigs[slot] = rq;
+    if (ritz) ritz[slot] = th[acc_h[q]];
+    if (resid) resid[slot] = rr[4 * q + 3];
+  }
+}
+
 int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, double* resid, int64_t* n_out,
                 double* evecs, edg_mixed_stats* stats) {
   const int64_t n = S.P.n_p;
@@ -247,8 +406,7 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
   const auto t_start = clk::now();
   Dev D;
   float2 *V = nullptr, *w = nullptr, *buf[3] = {nullptr, nullptr, nullptr};
-  double *alpha, *beta, *part, *scal, *theta, *theta_hat, *y, *work;
-  int *acc, *nacc;
+  double *alpha, *beta, *part, *scal;
   cudaError_t e = cudaSuccess;
   if (store) {
     if ((e = D.alloc(&V, (size_t)n * (m + 1))) != cudaSuccess)
@@ -260,10 +418,7 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
   if ((e = D.alloc(&w, (size_t)n)) != cudaSuccess) return fail(EDG_ERR_NOMEM, "mixed Lanczos: w");
   const int64_t kparts = (int64_t)std::max(m + 1, 4) * kRedBlocks * 2;
   if ((e = D.alloc(&alpha, m + 1)) != cudaSuccess || (e = D.alloc(&beta, m + 2)) != cudaSuccess ||
-      (e = D.alloc(&part, kparts)) != cudaSuccess || (e = D.alloc(&scal, 2 * (m + 2) + 2)) != cudaSuccess ||
-      (e = D.alloc(&theta, kCand)) != cudaSuccess || (e = D.alloc(&theta_hat, kCand)) != cudaSuccess ||
-      (e = D.alloc(&y, (size_t)kMaxEv * m)) != cudaSuccess || (e = D.alloc(&work, (size_t)kMaxEv * 5 * m)) != cudaSuccess ||
-      (e = D.alloc(&acc, kMaxEv)) != cudaSuccess || (e = D.alloc(&nacc, 1)) != cudaSuccess)
+      (e = D.alloc(&part, kparts)) != cudaSuccess || (e = D.alloc(&scal, 2 * (m + 2) + 2)) != cudaSuccess)
     return fail(EDG_ERR_NOMEM, "mixed Lanczos: scratch");
   cudaMemsetAsync(beta, 0, sizeof(double) * (m + 2), st);
 
@@ -331,84 +486,43 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
   };
   if ((e = run(false, nullptr, 0, {})) != cudaSuccess) return cuda_fail(e, "mixed Lanczos");
   // eigenvalues and Ritz coefficients of T on the device
-  const size_t tsh = sizeof(double) * 2 * m;
+  MixedFinish F;
+  if ((e = F.reserve(n, m)) != cudaSuccess) return fail(EDG_ERR_NOMEM, "mixed Lanczos: scratch");
   const int n_try = std::min(kMaxEv, std::min(want + 4, m));
-  k_tridiag<<<1, 128, tsh, st>>>(alpha, beta, m, n_try, theta, theta_hat, y, work, acc, nacc);
   int na = 0;
-  std::vector<int> acc_h(kMaxEv);
-  std::vector<double> th(kCand), yh;
-  if ((e = cudaMemcpyAsync(&na, nacc, sizeof(int), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
-      (e = cudaStreamSynchronize(st)) != cudaSuccess)
-    return cuda_fail(e, "mixed Lanczos: T");
-  yh.resize((size_t)std::max(na, 1) * m);
-  cudaMemcpyAsync(acc_h.data(), acc, sizeof(int) * kMaxEv, cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(th.data(), theta, sizeof(double) * std::min(kCand, m), cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(yh.data(), y, sizeof(double) * na * m, cudaMemcpyDeviceToHost, st);
-  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "mixed Lanczos: T");
+  std::vector<int> acc_h;
+  std::vector<double> th;
+  int rc = F.tridiag(st, alpha, beta, m, n_try, &na, acc_h, th);
+  if (rc != EDG_OK) return rc;
   if (na == 0) return fail(EDG_ERR_NOT_CONVERGED, "mixed Lanczos: no Ritz value survived the copy test");
   // Ritz vectors in FP64
-  double2 *X = nullptr, *HX = nullptr;
-  if ((e = D.alloc(&X, (size_t)na * n)) != cudaSuccess || (e = D.alloc(&HX, (size_t)n)) != cudaSuccess)
-    return fail(EDG_ERR_NOMEM, "mixed Lanczos: FP64 Ritz vectors do not fit");
-  cudaMemsetAsync(X, 0, sizeof(double2) * na * n, st);
+  if ((e = F.reserve_x(n, na)) != cudaSuccess) return fail(EDG_ERR_NOMEM, "mixed Lanczos: FP64 Ritz vectors do not fit");
   int passes = 1;
   if (store) {
-    for (int j = 0; j < m; ++j) {
-      std::vector<double> c(na);
-      for (int q = 0; q < na; ++q) c[q] = yh[(size_t)q * m + j];
-      cudaMemcpyAsync(scal, c.data(), sizeof(double) * na, cudaMemcpyHostToDevice, st);
-      k_accumulate<<<grid_n(n), 256, sizeof(double) * na, st>>>(X, n, V + (int64_t)j * n, scal, na, n);
-      if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "mixed Lanczos: Ritz vectors");
-    }
+    if ((rc = F.ritz_stored(st, V, n, m, na)) != EDG_OK) return rc;
   } else {
     passes = 2;
-    if ((e = run(true, X, na, yh)) != cudaSuccess) return cuda_fail(e, "mixed Lanczos: second pass");
+    std::vector<double> yh((size_t)na * m);
+    cudaMemcpyAsync(yh.data(), F.y, sizeof(double) * na * m, cudaMemcpyDeviceToHost, st);
+    cudaMemsetAsync(F.X, 0, sizeof(double2) * na * n, st);
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "mixed Lanczos: T");
+    if ((e = run(true, F.X, na, yh)) != cudaSuccess) return cuda_fail(e, "mixed Lanczos: second pass");
   }
-  // FP64 Rayleigh quotient and residual of each Ritz vector; a Rayleigh
-  // quotient within 1e-8 relative of an earlier one is the same level again
-  // (a copy that slipped through) and is dropped.
-  std::vector<double> rq_all(na), res_all(na), ritz_all(na);
+  // FP64 Rayleigh quotient and residual of each Ritz vector
+  std::vector<double> rr;
+  if ((rc = F.rayleigh(S, st, n, na, rr)) != EDG_OK) return rc;
   std::vector<int> keep;
-  for (int q = 0; q < na; ++q) {
-    double2* x = X + (int64_t)q * n;
-    if ((e = launch_hv(S, x, HX, true, st)) != cudaSuccess) return cuda_fail(e, "mixed Lanczos: FP64 H*v");
-    k_rq_partial<<<kRedBlocks, kRedThreads, 0, st>>>(x, HX, n, nullptr, part);
-    std::vector<double> p(3 * kRedBlocks);
-    cudaMemcpyAsync(p.data(), part, sizeof(double) * 3 * kRedBlocks, cudaMemcpyDeviceToHost, st);
-    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "mixed Lanczos: residual");
-    double nx = 0, xhx = 0;
-    for (int b = 0; b < kRedBlocks; ++b) {
-      nx += p[3 * b];
-      xhx += p[3 * b + 1];
-    }
-    const double rq = xhx / nx;
-    cudaMemcpyAsync(scal, &rq, sizeof(double), cudaMemcpyHostToDevice, st);
-    k_rq_partial<<<kRedBlocks, kRedThreads, 0, st>>>(x, HX, n, scal, part);
-    cudaMemcpyAsync(p.data(), part, sizeof(double) * 3 * kRedBlocks, cudaMemcpyDeviceToHost, st);
-    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "mixed Lanczos: residual");
-    double r2 = 0;
-    for (int b = 0; b < kRedBlocks; ++b) r2 += p[3 * b + 2];
-    rq_all[q] = rq;
-    res_all[q] = std::sqrt(r2 / nx);
-    ritz_all[q] = th[acc_h[q]];
-    bool dup = false;
-    for (int k : keep)
-      if (std::fabs(rq_all[k] - rq) <= 1e-8 * std::fabs(rq)) dup = true;
-    if (dup || (int)keep.size() >= want) continue;
-    const int slot = (int)keep.size();
-    keep.push_back(q);
-    eigs[slot] = rq;
-    if (ritz) ritz[slot] = ritz_all[q];
-    if (resid) resid[slot] = res_all[q];
-    if (evecs) {
-      // normalised FP64 eigenvector to the host
-      std::vector<double2> hx(n);
-      cudaMemcpyAsync(hx.data(), x, sizeof(double2) * n, cudaMemcpyDeviceToHost, st);
+  pick_levels(rr, th, acc_h, na, want, eigs, ritz, resid, keep);
+  if (evecs) {
+    // normalised FP64 eigenvectors to the host
+    std::vector<double2> hx(n);
+    for (size_t slot = 0; slot < keep.size(); ++slot) {
+      cudaMemcpyAsync(hx.data(), F.X + (int64_t)keep[slot] * n, sizeof(double2) * n, cudaMemcpyDeviceToHost, st);
       if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "mixed Lanczos: vectors");
-      const double s = 1.0 / std::sqrt(nx);
+      const double sc = 1.0 / std::sqrt(rr[4 * keep[slot]]);
       for (int64_t i = 0; i < n; ++i) {
-        evecs[2 * ((int64_t)slot * n + i)] = hx[i].x * s;
-        evecs[2 * ((int64_t)slot * n + i) + 1] = hx[i].y * s;
+        evecs[2 * ((int64_t)slot * n + i)] = hx[i].x * sc;
+        evecs[2 * ((int64_t)slot * n + i) + 1] = hx[i].y * sc;
       }
     }
   }

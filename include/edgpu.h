@@ -207,6 +207,59 @@ typedef struct {
 int edg_solve_mixed(edg_sector* s, const edg_mixed_opts* opts, double* eigs, double* ritz, double* residuals,
                     int64_t* n_eigs, double* evecs, edg_mixed_stats* stats);
 
+/* ---- Batched solves: many sectors advanced together ----------------------
+ * No counterpart in the reference, which diagonalises one sector at a time
+ * (sector_lanczos in a loop over momenta, ED.cpp:120-131).  Each segment is a
+ * sector with stored rows and a request; every Lanczos step of all live
+ * segments is one replay of a captured CUDA graph.  FP32 Krylov vectors
+ * (reorthogonalised every step), FP64 alpha/beta, FP64 Rayleigh quotients and
+ * residuals as in edg_solve_mixed.  A segment stops when the residual bounds
+ * of its wanted Ritz pairs are below tol * max(1, |theta|) (tested every
+ * check_every steps) or after max_iterations steps, and is then finished and
+ * its memory released.  The caller keeps each sector alive until its result
+ * has been polled.  One thread drives a batch. */
+typedef struct {
+  int tile_rows;      /* rows per CTA tile (0: 1024) */
+  int lanes_per_row;  /* lanes per stored row: 8, 16 or 32 (0: 8) */
+  int check_every;    /* steps between convergence tests (0: 10) */
+} edg_batch_opts;
+
+typedef struct {
+  int n_ev;            /* eigenvalues wanted, 1..32 */
+  int max_iterations;  /* Lanczos steps at most, 2..511 */
+  double tol;          /* residual-bound tolerance; 0 runs max_iterations steps */
+  uint64_t seed;       /* start vector: edg_fill_random's stream, normalised */
+  int64_t tag;         /* returned with the result */
+} edg_batch_request;
+
+typedef struct {
+  int64_t tag;
+  int status;          /* EDG_OK or the error that stopped the finish */
+  int n_found;         /* distinct levels returned (<= n_ev) */
+  int iterations;      /* Lanczos steps taken */
+  int converged;       /* 1: stopped by the tolerance, 0: by max_iterations */
+  double eigs[32];     /* FP64 Rayleigh quotients, ascending */
+  double ritz[32];     /* the Ritz values of T they came from */
+  double residuals[32];/* |Hx - eig x| / |x| in FP64 */
+} edg_batch_result;
+
+typedef struct edg_batch edg_batch;
+
+int edg_batch_create(const edg_batch_opts* opts, edg_batch** out);
+int edg_batch_destroy(edg_batch* b);
+/* Device bytes a segment of this sector and request takes in a batch (the
+ * sector's own basis and stored rows not included). */
+int edg_batch_footprint(const edg_sector* s, const edg_batch_request* req, int64_t* bytes);
+/* Queue a segment; it starts with the next step.  EDG_ERR_NOMEM if its
+ * vectors do not fit (nothing is queued then). */
+int edg_batch_add(edg_batch* b, edg_sector* s, const edg_batch_request* req);
+/* Run up to n_steps steps of every live segment (fewer when none is left);
+ * segments that stop are finished before this returns or at the next call. */
+int edg_batch_step(edg_batch* b, int n_steps);
+/* Move up to cap finished results into out; *n_out receives how many. */
+int edg_batch_poll(edg_batch* b, edg_batch_result* out, int cap, int* n_out);
+int edg_batch_info(const edg_batch* b, int* n_active, int64_t* device_bytes, int64_t* steps);
+
 /* Deterministic complex test vector (splitmix64, entries uniform in [-1,1)^2)
  * written to device memory; the same generator as the test suite's. */
 int edg_fill_random(void* dst, int64_t n, int dtype, uint64_t seed, void* stream);

@@ -1,0 +1,111 @@
+"""Batched solves (edg_batch_*) against the reference's eigenvalues, and the
+same result for a sector alone and in a mix that changes around it.
+
+Target: |dE|/|E| <= 1e-9 against the eigenvalues the reference printed
+(ED2, FP64), with FP32 Krylov vectors and FP64 Rayleigh quotients.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_cases, golden_model
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL = 1e-9
+
+
+@pytest.fixture(scope="module")
+def mods(cuda_device):
+    from ed_code_gb300 import batch, sector
+
+    return batch, sector
+
+
+def distinct(levels, tol=1e-9):
+    out = []
+    for x in levels:
+        if not out or abs(x - out[-1]) > tol * abs(x):
+            out.append(x)
+    return np.array(out)
+
+
+def stored_sector(sector, name, idx):
+    sec = sector.GpuSector(golden_model(name, idx))
+    assert sec.build_targets()
+    return sec
+
+
+CASES = [("sq4x4", 0, 3), ("sq4x4_j2", 0, 3), ("sq4x4_j2", 1, 3), ("sq4x4_phase_sz1", 0, 3), ("tri4x3", 0, 3),
+         ("tri4x3", 4, 3), ("tri4x3_relabel", 1, 2), ("sq6x4_k00", 0, 3), ("tri6x4_k10", 0, 2)]
+
+
+def test_batch_matches_reference(mods):
+    batch, sector = mods
+    B = batch.BatchSolver(tile_rows=512)
+    secs = {}
+    for k, (name, idx, n_ev) in enumerate(CASES):
+        secs[k] = stored_sector(sector, name, idx)
+        B.add(secs[k], n_ev=n_ev, max_iterations=200, tol=0.0, seed=1, tag=k)
+    res = {r["tag"]: r for r in B.run()}
+    assert sorted(res) == list(range(len(CASES)))
+    for k, (name, idx, n_ev) in enumerate(CASES):
+        r = res[k]
+        assert r["status"] == 0, r
+        ref = distinct(golden_cases()[name]["sectors"][idx]["ed2_eigs"])
+        n = min(n_ev, len(ref))
+        assert r["n_found"] >= n, (name, r)
+        rel = np.abs(r["eigs"][:n] - ref[:n]) / np.abs(ref[:n])
+        assert rel.max() <= REL_TOL, (name, r["eigs"], ref[:n])
+        assert r["iterations"] == min(200, secs[k].n_p)
+
+
+def test_alone_equals_in_mix(mods):
+    """A segment's arithmetic reads only its own tiles: joining a batch whose
+    composition changes before, during and after it gives the same bits."""
+    batch, sector = mods
+    a = stored_sector(sector, "sq6x4_k00", 0)
+    B1 = batch.BatchSolver(tile_rows=512)
+    B1.add(a, n_ev=2, max_iterations=120, tol=0.0, seed=7, tag=0)
+    alone = B1.run()[0]
+    B2 = batch.BatchSolver(tile_rows=512)
+    others = [stored_sector(sector, "sq4x4", 0), stored_sector(sector, "tri6x4_k10", 0),
+              stored_sector(sector, "sq4x4_j2", 1)]
+    B2.add(others[0], n_ev=3, max_iterations=60, tol=0.0, seed=3, tag=10)
+    B2.add(others[1], n_ev=2, max_iterations=150, tol=0.0, seed=4, tag=11)
+    B2.step(37)
+    B2.add(a, n_ev=2, max_iterations=120, tol=0.0, seed=7, tag=0)
+    B2.step(15)
+    B2.add(others[2], n_ev=3, max_iterations=40, tol=0.0, seed=5, tag=12)
+    mixed = {r["tag"]: r for r in B2.run()}
+    assert set(mixed) == {0, 10, 11, 12}
+    assert mixed[0]["iterations"] == alone["iterations"] == 120
+    assert np.array_equal(mixed[0]["eigs"], alone["eigs"])
+    assert np.array_equal(mixed[0]["residuals"], alone["residuals"])
+
+
+def test_tolerance_stops_early(mods):
+    batch, sector = mods
+    sec = stored_sector(sector, "sq6x4_k00", 0)
+    B = batch.BatchSolver(tile_rows=1024, check_every=5)
+    B.add(sec, n_ev=2, max_iterations=400, tol=1e-6, seed=1)
+    r = B.run()[0]
+    assert r["converged"] and r["iterations"] < 400, r
+    ref = distinct(golden_cases()["sq6x4_k00"]["sectors"][0]["ed2_eigs"])[:2]
+    assert np.max(np.abs(r["eigs"][:2] - ref) / np.abs(ref)) <= REL_TOL, (r, ref)
+
+
+def test_batch_rejects_bad_requests(mods):
+    batch, sector = mods
+    from ed_code_gb300._native import EdgError
+
+    B = batch.BatchSolver()
+    plain = sector.GpuSector(golden_model("tri4x3", 0))
+    with pytest.raises(EdgError, match="stored rows"):
+        B.add(plain, n_ev=2)
+    assert plain.build_targets()
+    with pytest.raises(EdgError, match="n_ev"):
+        B.add(plain, n_ev=0)
+    with pytest.raises(EdgError, match="max_iterations"):
+        B.add(plain, n_ev=1, max_iterations=1000)
+    assert B.info()["active"] == 0
+    assert B.footprint(plain, 2, 50) > 0
