@@ -1,0 +1,79 @@
+"""The serving loop: each request's result is the same alone and in the mix,
+the eigenvalues meet the 1e-9 relative tolerance against the FP64 plain
+solver, and admission keeps to the memory budget."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def mods(cuda_device):
+    from ed_code_gb300 import batch, lattice, sector, serving
+
+    return batch, lattice, sector, serving
+
+
+@pytest.fixture(scope="module")
+def stream(mods):
+    serving = mods[3]
+    return serving.make_stream(10, rate=400.0, seed=11, sizes=(20, 24))
+
+
+@pytest.fixture(scope="module")
+def served(mods, stream):
+    serving = mods[3]
+    srv = serving.Server(max_iterations=300, res_tol=1e-6)
+    out = srv.run(stream)
+    srv.close()
+    return {s.rid: s for s in out}
+
+
+def test_every_request_served(served, stream, mods):
+    serving = mods[3]
+    assert sorted(served) == [r.rid for r in stream]
+    for s in served.values():
+        assert s.status == 0 and s.converged and s.finished >= s.admitted >= 0
+        assert len(s.eigs) >= 1
+    summ = serving.summarize(list(served.values()))
+    assert summ["p99_s"] >= summ["p50_s"] > 0 and summ["solves_per_s"] > 0
+
+
+def test_alone_equals_in_mix(served, stream, mods):
+    batch, lattice, sector, serving = mods
+    for req in stream[:4]:
+        sec = sector.GpuSector(lattice.make_model(req.spec, req.Sz, req.kx, req.ky))
+        assert sec.build_targets()
+        B = batch.BatchSolver(tile_rows=1024, lanes_per_row=8, check_every=10)
+        B.add(sec, n_ev=req.n_ev, max_iterations=min(300, sec.n_p), tol=1e-6, seed=1 + req.rid, tag=req.rid)
+        alone = B.run()[0]
+        mixed = served[req.rid]
+        assert alone["iterations"] == mixed.iterations
+        assert np.array_equal(alone["eigs"], mixed.eigs), (alone["eigs"], mixed.eigs)
+
+
+def test_eigenvalues_match_plain_fp64(served, stream, mods):
+    _, lattice, sector, _ = mods
+    for req in stream[:5]:
+        sec = sector.GpuSector(lattice.make_model(req.spec, req.Sz, req.kx, req.ky))
+        eigs, _, _ = sec.solve_plain(n_ev=max(req.n_ev, 4), iterations=200, ncycles=10, tol=1e-12)
+        levels = []
+        for x in eigs:
+            if not levels or abs(x - levels[-1]) > 1e-9 * abs(x):
+                levels.append(x)
+        got = served[req.rid].eigs
+        levels = np.array(levels)
+        assert abs(got[0] - levels[0]) <= 1e-9 * abs(levels[0]), (req, got, levels)
+        for x in got[1:]:
+            if x <= levels[-1]:  # levels the plain run reached
+                assert np.min(np.abs(levels - x)) <= 1e-9 * abs(x), (req, got, levels)
+
+
+def test_admission_keeps_to_the_budget(mods, stream):
+    serving = mods[3]
+    one = max(serving.estimate_bytes(r, 300) for r in stream[:6])
+    srv = serving.Server(hbm_budget=one, max_iterations=300, res_tol=1e-6)
+    out = srv.run(stream[:6])
+    srv.close()
+    assert len(out) == 6
+    assert srv.peak_live == 1 and srv.peak_bytes <= one
