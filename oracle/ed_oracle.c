@@ -224,16 +224,45 @@ typedef struct {
   const int64_t *reps;
   const int32_t *lid;
   int64_t n_p;
+  /* list-free mode (reps == NULL): v_j is value_vector(rep, vseed) */
+  uint64_t vseed;
 } or_lookup;
 
-static inline int64_t lookup_target(const or_lookup *L, int64_t tmp, double complex *ph, double *ninv) {
+/* Deterministic vector entry as a function of a representative's value (used
+ * where the representative list is not built): splitmix64, uniform in [-1,1)^2. */
+static uint64_t splitmix64_next(uint64_t *s) {
+  uint64_t z = (*s += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+static double complex value_vector(int64_t rep, uint64_t seed) {
+  uint64_t s = seed ^ ((uint64_t)rep * 0xD6E8FEB86659FD93ull);
+  double a = (double)(splitmix64_next(&s) >> 11) * 0x1.0p-53, b = (double)(splitmix64_next(&s) >> 11) * 0x1.0p-53;
+  return CMPLX(2 * a - 1, 2 * b - 1);
+}
+
+void or_value_vector(const int64_t *reps, int64_t n, uint64_t seed, double *v) {
+  for (int64_t j = 0; j < n; ++j) {
+    double complex x = value_vector(reps[j], seed);
+    v[2 * j] = creal(x);
+    v[2 * j + 1] = cimag(x);
+  }
+}
+
+/* j of a flipped state (or -1) with its phase and 1/norm; *vj = v_j. */
+static inline int64_t lookup_target(const or_lookup *L, int64_t tmp, const double *v, double complex *ph,
+                                    double *ninv, double complex *vj) {
   if (L->tab) {
     const or_basis *b = L->tab;
     int64_t left = tmp >> (b->n_sites / 2), right = tmp & b->bits_right;
     int64_t loc = b->Ia[right] + b->Ib[left] - 1;
     int64_t j = b->rep_loc[loc];
     *ph = CMPLX(b->state_ph[2 * loc], b->state_ph[2 * loc + 1]);
-    if (j >= 0) *ninv = b->norm_inv[j];
+    if (j >= 0) {
+      *ninv = b->norm_inv[j];
+      *vj = CMPLX(v[2 * j], v[2 * j + 1]);
+    }
     return j;
   }
   int lx, ly, lid, pid;
@@ -242,8 +271,17 @@ static inline int64_t lookup_target(const or_lookup *L, int64_t tmp, double comp
   if (lx < 0) lx += L->L1;
   if (ly < 0) ly += L->L2;
   *ph = cexp(CMPLX(0.0, -L->px * lx - L->py * ly));
+  if (!L->reps) {
+    if (!pid) return -1;
+    *ninv = 1 / sqrt((double)((int64_t)(L->L1 * L->L2) / lid));
+    *vj = value_vector(rep, L->vseed);
+    return 0;
+  }
   int64_t j = find_state(rep, L->reps, L->n_p);
-  if (j >= 0) *ninv = 1 / sqrt((double)((int64_t)(L->L1 * L->L2) / L->lid[j]));
+  if (j >= 0) {
+    *ninv = 1 / sqrt((double)((int64_t)(L->L1 * L->L2) / L->lid[j]));
+    *vj = CMPLX(v[2 * j], v[2 * j + 1]);
+  }
   return j;
 }
 
@@ -264,10 +302,9 @@ static double complex hv_row(const or_lookup *L, int64_t idi, double norm_i, dou
     } else {
       if (tx == 1) e = conj(e);
       Ezz += -(Ezzfac * J);
-      double complex ph; double ninv = 0;
-      int64_t j = lookup_target(L, flip2(idi, x, y), &ph, &ninv);
+      double complex ph, vj = 0; double ninv = 0;
+      int64_t j = lookup_target(L, flip2(idi, x, y), v, &ph, &ninv, &vj);
       if (j >= 0) {
-        double complex vj = CMPLX(v[2 * j], v[2 * j + 1]);
         w += e * J * 0.5 * vj * ph * norm_i * ninv;
       }
     }
@@ -279,13 +316,13 @@ static double complex hv_row(const or_lookup *L, int64_t idi, double norm_i, dou
       double complex ep = CMPLX(tris[k].re, tris[k].im);
       int tx = bit(idi, x), ty = bit(idi, y);
       if (tx != ty) {
-        double complex ph; double ninv = 0;
-        int64_t j = lookup_target(L, flip2(idi, x, y), &ph, &ninv);
+        double complex ph, vj = 0; double ninv = 0;
+        int64_t j = lookup_target(L, flip2(idi, x, y), v, &ph, &ninv, &vj);
         if (j >= 0) {
           double complex sgn = (ty == 1) ? CMPLX(0, 1) * ep : CMPLX(0, -1) * conj(ep);
           if (bit(idi, z) == 0) sgn = sgn * CMPLX(-1, 0);
           double complex ele = Ch * 0.25 * sgn * ph * norm_i * ninv;
-          w += ele * CMPLX(v[2 * j], v[2 * j + 1]);
+          w += ele * vj;
         }
       }
     }
@@ -303,12 +340,12 @@ static double complex hv_row(const or_lookup *L, int64_t idi, double norm_i, dou
         if (tp != tq) {
           int64_t tmp2 = flip2(tmp, p, q);
           int tr = bit(tmp2, r);
-          double complex ph; double ninv = 0;
-          int64_t j = lookup_target(L, tmp2, &ph, &ninv);
+          double complex ph, vj = 0; double ninv = 0;
+          int64_t j = lookup_target(L, tmp2, v, &ph, &ninv, &vj);
           if (j >= 0) {
             if (tr == 0) s2 = s2 * CMPLX(-1, 0);
             double complex ele = ChCh * 0.25 * 0.25 * s1 * s2 * ph * norm_i * ninv;
-            w += ele * CMPLX(v[2 * j], v[2 * j + 1]);
+            w += ele * vj;
           }
         }
       }
@@ -356,6 +393,63 @@ void or_hv_rows(int n_sites, const int *T1, const int *T2, int kx, int ky, const
     w_rows[2 * r] = creal(o);
     w_rows[2 * r + 1] = cimag(o);
   }
+}
+
+/* Rows of H v without the representative list, for sectors whose list is too
+ * large to build on the host: `rows` are representatives (or_sample_reps) and
+ * v is value_vector(representative, vseed), so a target costs its orbit walk
+ * (representative_p, Momentum_Basis.cpp:472-543) but no rank lookup. */
+void or_hv_rows_listless(int n_sites, const int *T1, const int *T2, int kx, int ky, const int64_t *rows,
+                         const int32_t *row_lid, int64_t n_rows, uint64_t vseed, double *w_rows, double lambda,
+                         const or_bond *bonds, int nb, double Ch, const or_tri *tris, int nt, double ChCh,
+                         const or_bowtie *bows, int nbw, int n_threads) {
+  or_lookup L;
+  memset(&L, 0, sizeof L);
+  L.n_sites = n_sites; L.T1 = T1; L.T2 = T2; L.vseed = vseed;
+  or_LxLy(T1, T2, n_sites, &L.L1, &L.L2);
+  L.px = 2 * kx * OR_PI / L.L1;
+  L.py = 2 * ky * OR_PI / L.L2;
+#ifdef _OPENMP
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+#else
+  (void)n_threads;
+#endif
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t r = 0; r < n_rows; ++r) {
+    double norm_i = sqrt((double)((int64_t)(L.L1 * L.L2) / row_lid[r]));
+    double complex o = hv_row(&L, rows[r], norm_i, value_vector(rows[r], vseed), NULL, lambda, bonds, nb, Ch, tris,
+                              nt, ChCh, bows, nbw);
+    w_rows[2 * r] = creal(o);
+    w_rows[2 * r + 1] = cimag(o);
+  }
+}
+
+/* n representatives drawn by taking random n_ones-subsets (splitmix64 stream
+ * `seed`) and keeping those that are their orbit's allowed representative. */
+int64_t or_sample_reps(int n_sites, int n_ones, const int *T1, const int *T2, int kx, int ky, uint64_t seed,
+                       int64_t n, int64_t *states, int32_t *lid_out) {
+  int L1, L2;
+  or_LxLy(T1, T2, n_sites, &L1, &L2);
+  const double px = 2 * kx * OR_PI / L1, py = 2 * ky * OR_PI / L2;
+  uint64_t s = seed;
+  int64_t got = 0;
+  for (int64_t tries = 0; got < n && tries < 1000 * (n + 10); ++tries) {
+    int idx[64];
+    for (int k = 0; k < n_sites; ++k) idx[k] = k;
+    int64_t t = 0;
+    for (int k = 0; k < n_ones; ++k) {
+      int r = k + (int)(splitmix64_next(&s) % (uint64_t)(n_sites - k));
+      int tmp = idx[k]; idx[k] = idx[r]; idx[r] = tmp;
+      t |= (int64_t)1 << idx[k];
+    }
+    int lx, ly, lid, pid;
+    int64_t rep = or_representative(t, T1, T2, n_sites, L1, L2, px, py, &lx, &ly, &lid, &pid);
+    if (!pid) continue;
+    states[got] = rep;
+    lid_out[got] = lid;
+    ++got;
+  }
+  return got;
 }
 
 int or_allowed_rep(int64_t state, const int *T1, const int *T2, int n_sites, int kx, int ky) {

@@ -73,6 +73,14 @@ def lib() -> C.CDLL:
         L.or_build_reps.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int, C.c_int,
                                     C.POINTER(C.POINTER(C.c_int64)), C.POINTER(C.POINTER(C.c_int32)), C.c_int]
         L.or_build_reps.restype = C.c_int64
+        L.or_hv_rows_listless.argtypes = [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int, C.c_int,
+                                          C.c_void_p, C.c_void_p, C.c_int64, C.c_uint64, C.c_void_p, C.c_double,
+                                          C.POINTER(Bond), C.c_int, C.c_double, C.POINTER(Tri), C.c_int,
+                                          C.c_double, C.POINTER(Bowtie), C.c_int, C.c_int]
+        L.or_sample_reps.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int, C.c_int,
+                                     C.c_uint64, C.c_int64, C.c_void_p, C.c_void_p]
+        L.or_sample_reps.restype = C.c_int64
+        L.or_value_vector.argtypes = [C.c_void_p, C.c_int64, C.c_uint64, C.c_void_p]
         L.or_free.argtypes = [C.c_void_p]
         L.or_n_choose_k.argtypes = [C.c_int, C.c_int]
         L.or_n_choose_k.restype = C.c_int64
@@ -182,6 +190,38 @@ def build_reps(model, n_threads: int = 0):
     lib().or_free(rp)
     lib().or_free(lp)
     return reps, lid
+
+
+def sample_reps(model, n: int, seed: int = 1):
+    """n allowed representatives (with their stabiliser counts) drawn at random,
+    without building the sector's list."""
+    t = TermLists(model)
+    states = np.empty(n, np.int64)
+    lid = np.empty(n, np.int32)
+    got = lib().or_sample_reps(model.n_sites, model.n_ones, t.T1, t.T2, model.kx, model.ky, int(seed), int(n),
+                               states.ctypes.data, lid.ctypes.data)
+    return states[:got], lid[:got]
+
+
+def value_vector(reps: np.ndarray, seed: int) -> np.ndarray:
+    """The vector hv_rows_listless uses: entry j is a hash of reps[j]."""
+    reps = np.ascontiguousarray(reps, dtype=np.int64)
+    v = np.empty(len(reps), np.complex128)
+    lib().or_value_vector(reps.ctypes.data, len(reps), int(seed), v.ctypes.data)
+    return v
+
+
+def hv_rows_listless(model, rows: np.ndarray, row_lid: np.ndarray, vseed: int, n_threads: int = 0):
+    """Rows of H v for representatives `rows`, with v = value_vector(., vseed),
+    without the sector's representative list (no rank lookups)."""
+    t = TermLists(model)
+    rows = np.ascontiguousarray(rows, dtype=np.int64)
+    row_lid = np.ascontiguousarray(row_lid, dtype=np.int32)
+    out = np.zeros(len(rows), dtype=np.complex128)
+    lib().or_hv_rows_listless(model.n_sites, t.T1, t.T2, model.kx, model.ky, rows.ctypes.data, row_lid.ctypes.data,
+                              len(rows), int(vseed), out.ctypes.data, model.Jz, t.bonds, t.nb, model.Ch, t.tris, t.nt,
+                              model.ChCh, t.bows, t.nbw, int(n_threads))
+    return out
 
 
 def allowed_rep(model, state: int) -> int:

@@ -104,3 +104,22 @@ def test_splitmix_vector_is_deterministic():
     assert np.array_equal(a, b)
     assert np.abs(a.real).max() <= 1 and np.abs(a.imag).max() <= 1
     assert not np.array_equal(a, O.splitmix_vector(1000, 4))
+
+
+def test_listless_rows_equal_list_rows():
+    """The list-free row mode (used where the representative list cannot be
+    built on the host) gives the same rows as the list mode with the same v."""
+    from ed_code_gb300 import lattice as L
+
+    for spec, sec in [(L.TorusSpec("triangular", 4, 3, Jz=0.9, Ch=0.3), (0, 1, 2)),
+                      (L.TorusSpec("square", 4, 4, Jz=1.1, J2=0.4), (1, 1, 3))]:
+        model = L.make_model(spec, *sec)
+        reps, lid = O.build_reps(model)
+        v = O.value_vector(reps, 99)
+        rows = np.arange(0, len(reps), 3)
+        a = O.hv_rows(model, reps, lid, v, rows)
+        b = O.hv_rows_listless(model, reps[rows], lid[rows], 99)
+        assert np.array_equal(a, b)
+        s, sl = O.sample_reps(model, 50, seed=5)
+        assert len(s) == 50 and np.all(np.isin(s, reps))
+        assert np.array_equal(sl, lid[np.searchsorted(reps, s)])
