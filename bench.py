@@ -352,6 +352,232 @@ def run_device(args, world, rank, local_rank):
     return 0
 
 
+def _distinct(levels, tol=1e-9):
+    out = []
+    for x in sorted(levels):
+        if not out or abs(x - out[-1]) > tol * abs(x):
+            out.append(x)
+    return out
+
+
+def _rel_err(got, plain):
+    """Largest |dE|/|E| of the levels in `got` against the plain FP64 levels
+    (each compared with the nearest plain level the plain run reached)."""
+    import numpy as np
+
+    lev = np.array(_distinct(plain))
+    errs = [abs(got[0] - lev[0]) / abs(lev[0])]
+    for x in got[1:]:
+        if x <= lev[-1]:
+            errs.append(float(np.min(np.abs(lev - x))) / abs(x))
+    return float(max(errs))
+
+
+def _plain(sec, n_ev):
+    """The plain FP64 form (lanczos_evecs / exact_evecs replica) on the GPU."""
+    t0 = time.perf_counter()
+    eigs, _, _ = sec.solve_plain(n_ev=n_ev, iterations=200, ncycles=10, tol=1e-11)
+    return list(eigs), time.perf_counter() - t0
+
+
+def run_serve(args):
+    """Serving stream: Poisson arrivals, mixed sizes, continuous batching."""
+    import numpy as np
+    import torch
+
+    from ed_code_gb300 import lattice as L
+    from ed_code_gb300 import serving
+    from ed_code_gb300.sector import GpuSector
+
+    torch.cuda.init()
+    warm = serving.make_stream(4, rate=1e6, seed=99, sizes=(20,))
+    srv = serving.Server(max_iterations=300, res_tol=args.res_tol)
+    srv.run(warm)
+    stream = serving.make_stream(args.requests, rate=args.rate, seed=3)
+    t0 = time.perf_counter()
+    t_create0 = srv.create_seconds
+    served = srv.run(stream)
+    wall = time.perf_counter() - t0
+    timers = srv.batch.timers()
+    t_create = srv.create_seconds - t_create0
+    srv.close()
+    summ = serving.summarize(served)
+    by = {s.rid: s for s in served}
+    # plain FP64, one request after another, on a seeded sample (two per size)
+    rng = np.random.default_rng(5)
+    sample = []
+    for N in (20, 24, 28, 32):
+        ids = [r.rid for r in stream if r.n_sites == N]
+        sample += list(rng.choice(ids, size=min(args.plain_per_size, len(ids)), replace=False)) if ids else []
+    plain_t, errs = {}, []
+    for rid in sample:
+        req = stream[int(rid)]
+        t0 = time.perf_counter()
+        sec = GpuSector(L.make_model(req.spec, req.Sz, req.kx, req.ky))
+        sec.build_targets()
+        eigs, _ = _plain(sec, max(req.n_ev, 4))
+        plain_t.setdefault(req.n_sites, []).append(time.perf_counter() - t0)
+        errs.append(_rel_err(by[req.rid].eigs, eigs))
+        sec.close()
+    seq_plain = sum(float(np.mean(plain_t[r.n_sites])) for r in stream if r.n_sites in plain_t)
+    out = {"metric": "mixed-stream solves/s (serving)", "mode": "serve", "value": summ["solves_per_s"],
+           "unit": "solves/s", "higher_is_better": True, "n_gpus": 1, "data": "synthetic",
+           "p50_s": summ["p50_s"], "p99_s": summ["p99_s"], "makespan_s": summ["makespan_s"], "wall_s": wall,
+           "requests": len(served), "converged": summ["converged"],
+           "max_rel_err_vs_plain_fp64": max(errs) if errs else None, "checked": len(errs),
+           "plain_fp64_seconds_per_request": {str(k): float(np.mean(v)) for k, v in sorted(plain_t.items())},
+           "sequential_plain_solves_per_s": len(stream) / seq_plain if seq_plain else None,
+           "speedup_vs_sequential_plain": (summ["solves_per_s"] * seq_plain / len(stream)) if seq_plain else None,
+           "peak_active": srv.peak_live, "create_seconds": t_create, "batch_timers": timers,
+           "config": {"workload": f"poisson {args.rate}/s, {args.requests} requests, N in 20/24/28/32, seed 3",
+                      "res_tol": args.res_tol, "max_iterations": 300, "vectors": "c64 Krylov, f64 alpha/beta/RQ"}}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def run_batch(args):
+    """64 small Hamiltonians, every momentum at Sz=0, one batch."""
+    import numpy as np
+    import torch
+
+    from ed_code_gb300 import lattice as L
+    from ed_code_gb300.batch import BatchSolver
+    from ed_code_gb300.sector import GpuSector
+
+    torch.cuda.init()
+    rng = np.random.default_rng(2)
+    specs = []
+    for h in range(args.hamiltonians):
+        if rng.random() < 0.5:
+            spec = L.TorusSpec("square", 4, 4, Jz=float(rng.uniform(0.5, 1.5)), J2=float(rng.uniform(0, 0.5)),
+                               Ch=float(rng.uniform(0, 0.4)))
+        else:
+            spec = L.TorusSpec("triangular", 5, 4, Jz=float(rng.uniform(0.5, 1.5)), J2=float(rng.uniform(0, 0.5)),
+                               Ch=float(rng.uniform(0, 0.4)))
+        for kx in range(spec.Lx):
+            for ky in range(spec.Ly):
+                specs.append((spec, kx, ky))
+    t0 = time.perf_counter()
+    secs = []
+    for spec, kx, ky in specs:
+        sec = GpuSector(L.make_model(spec, 0, kx, ky))
+        assert sec.build_targets()
+        secs.append(sec)
+    torch.cuda.synchronize()
+    t_build = time.perf_counter() - t0
+    # autotune the tiles on a few steps of the whole batch
+    trials = {}
+    for rows in (256, 1024, 4096):
+        for lpr in (8, 16):
+            B = BatchSolver(tile_rows=rows, lanes_per_row=lpr)
+            for k, sec in enumerate(secs):
+                B.add(sec, n_ev=3, max_iterations=150, tol=0.0, seed=2, tag=k)
+            B.step(3)
+            t1 = time.perf_counter()
+            B.step(10)
+            trials[(rows, lpr)] = (time.perf_counter() - t1) / 10
+            B.close()
+    best = min(trials, key=trials.get)
+    B = BatchSolver(tile_rows=best[0], lanes_per_row=best[1])
+    t1 = time.perf_counter()
+    for k, sec in enumerate(secs):
+        B.add(sec, n_ev=3, max_iterations=150, tol=0.0, seed=2, tag=k)
+    res = {r["tag"]: r for r in B.run(chunk=10)}
+    t_solve = time.perf_counter() - t1
+    timers = B.timers()
+    # accuracy and the plain FP64 time on a seeded sample
+    pick = rng.choice(len(secs), size=min(args.plain_sample, len(secs)), replace=False)
+    errs, pt = [], []
+    for k in pick:
+        eigs, dt = _plain(secs[int(k)], 3)
+        pt.append(dt)
+        errs.append(_rel_err(res[int(k)]["eigs"], eigs))
+    n = len(secs)
+    out = {"metric": "batched small-sector solves/s", "mode": "batch", "value": n / t_solve, "unit": "solves/s",
+           "higher_is_better": True, "n_gpus": 1, "data": "synthetic", "sectors": n,
+           "dims": [int(min(s.n_p for s in secs)), int(max(s.n_p for s in secs))],
+           "solve_seconds": t_solve, "build_seconds": t_build, "batch_timers": timers, "e2e_solves_per_s": n / (t_solve + t_build),
+           "tiles": {"tile_rows": best[0], "lanes_per_row": best[1],
+                     "ms_per_step": {f"{r}x{l}": round(1e3 * v, 3) for (r, l), v in sorted(trials.items())}},
+           "max_rel_err_vs_plain_fp64": max(errs), "checked": len(errs),
+           "plain_fp64_seconds_per_sector": float(np.mean(pt)),
+           "speedup_vs_sequential_plain": float(np.mean(pt)) * n / t_solve,
+           "config": {"workload": f"{args.hamiltonians} Hamiltonians (4x4 square / 5x4 triangular), all momenta, "
+                                  "Sz=0, seed 2", "iterations": 150, "n_ev": 3}}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def run_precision(args):
+    """Mixed precision against the plain FP64 form: 6x5 triangular, 30 momenta."""
+    import numpy as np
+    import torch
+
+    from ed_code_gb300 import lattice as L
+    from ed_code_gb300.sector import GpuSector
+
+    torch.cuda.init()
+    spec = L.TorusSpec("triangular", 6, 5, Jz=0.8, Ch=0.2)
+    moms = [(kx, ky) for kx in range(6) for ky in range(5)][: args.momenta]
+    mixed = {}
+    t_mixed = 0.0
+    for kx, ky in moms:
+        t0 = time.perf_counter()
+        sec = GpuSector(L.make_model(spec, 0, kx, ky))
+        sec.build_targets()
+        r = sec.solve_mixed(n_ev=6, iterations=300, reorth_every=args.reorth, seed=1)
+        t_mixed += time.perf_counter() - t0
+        mixed[(kx, ky)] = r
+        sec.close()
+    rng = np.random.default_rng(1)
+    pick = [moms[int(i)] for i in rng.choice(len(moms), size=min(args.plain_sample, len(moms)), replace=False)]
+    errs, pt = [], []
+    for kx, ky in pick:
+        t0 = time.perf_counter()
+        sec = GpuSector(L.make_model(spec, 0, kx, ky))
+        sec.build_targets()
+        eigs, _ = _plain(sec, 6)
+        pt.append(time.perf_counter() - t0)
+        errs.append(_rel_err(mixed[(kx, ky)]["eigs"], eigs))
+        sec.close()
+    per_mixed = t_mixed / len(moms)
+    out = {"metric": "precision form vs plain FP64 (solve time ratio)", "mode": "precision",
+           "value": float(np.mean(pt)) / per_mixed, "unit": "x", "higher_is_better": True, "n_gpus": 1,
+           "data": "synthetic", "mixed_seconds_per_sector": per_mixed, "plain_fp64_seconds_per_sector": float(np.mean(pt)),
+           "max_rel_err_vs_plain_fp64": max(errs), "checked": len(errs), "momenta": len(moms),
+           "max_residual": float(max(max(r["residuals"]) for r in mixed.values())),
+           "config": {"workload": "6x5 triangular, Delta=0.8, Jchi=0.2, Sz=0", "iterations": 300, "n_ev": 6,
+                      "reorth_every": args.reorth, "seed": 1}}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def run_solve36(args):
+    """The large single sector: 300 FP32 Lanczos steps, 6 levels, FP64 residuals."""
+    import torch
+
+    from ed_code_gb300.sector import GpuSector
+
+    torch.cuda.init()
+    model = build_model("tri6x6_k00")
+    t0 = time.perf_counter()
+    sec = GpuSector(model)
+    assert sec.build_targets()
+    sec.tune(0)
+    t_build = time.perf_counter() - t0
+    t1 = time.perf_counter()
+    r = sec.solve_mixed(n_ev=6, iterations=300, reorth_every=0, seed=4)
+    t_solve = time.perf_counter() - t1
+    out = {"metric": "36-site sector solve", "mode": "solve36", "value": t_solve, "unit": "s",
+           "higher_is_better": False, "n_gpus": 1, "data": "synthetic", "build_seconds": t_build,
+           "eigs": [float(x) for x in r["eigs"]], "ritz": [float(x) for x in r["ritz"]],
+           "residuals": [float(x) for x in r["residuals"]], "stats": r["stats"],
+           "config": {"workload": "tri6x6_k00", "iterations": 300, "n_ev": 6, "vectors": "3 resident c64",
+                      "seed": 4}}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -366,7 +592,20 @@ def main():
     ap.add_argument("--rows", default=None, help="LANES,POLICY: fix the stored-row kernel instead of timing it")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-step-seconds", type=float, default=4.0)
+    ap.add_argument("--mode", choices=["hv", "serve", "batch", "precision", "solve36"], default="hv",
+                    help="hv: the headline H*v line; the others time the solver configurations")
+    ap.add_argument("--requests", type=int, default=64)
+    ap.add_argument("--rate", type=float, default=200.0)
+    ap.add_argument("--res-tol", type=float, default=1e-6)
+    ap.add_argument("--plain-per-size", type=int, default=2)
+    ap.add_argument("--hamiltonians", type=int, default=64)
+    ap.add_argument("--plain-sample", type=int, default=4)
+    ap.add_argument("--momenta", type=int, default=30)
+    ap.add_argument("--reorth", type=int, default=0)
     args = ap.parse_args()
+    if args.mode != "hv" and args.impl == "gb300":
+        return {"serve": run_serve, "batch": run_batch, "precision": run_precision,
+                "solve36": run_solve36}[args.mode](args)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

@@ -119,6 +119,7 @@ SIGNATURES = {
     "edg_batch_add": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(edg_batch_request)]),
     "edg_batch_step": (C.c_int, [C.c_void_p, C.c_int]),
     "edg_batch_poll": (C.c_int, [C.c_void_p, C.POINTER(edg_batch_result), C.c_int, C.POINTER(C.c_int)]),
+    "edg_batch_timers": (C.c_int, [C.c_void_p, C.c_void_p]),
     "edg_batch_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "edg_hv_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "edg_count_offdiag": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),

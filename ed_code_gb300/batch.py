@@ -71,6 +71,11 @@ class BatchSolver:
         N.check(N.lib().edg_batch_info(self._h, C.byref(a), C.byref(b), C.byref(s)))
         return {"active": a.value, "device_bytes": b.value, "steps": s.value}
 
+    def timers(self) -> dict:
+        t = np.zeros(5, np.float64)
+        N.check(N.lib().edg_batch_timers(self._h, t.ctypes.data))
+        return dict(zip(("add", "step", "finish", "release", "rebuild"), (float(x) for x in t)))
+
     def run(self, chunk: int = 10) -> List[dict]:
         """Step until no segment is left; return every result."""
         out = []

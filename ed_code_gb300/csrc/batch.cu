@@ -34,15 +34,19 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstddef>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/edgpu.h"
 #include "blas1.cuh"
 #include "edg_sector.cuh"
+#include "ff.cuh"
+#include "lanczos_common.cuh"
 #include "tridiag.cuh"
 
 struct edg_sector {
@@ -163,7 +167,8 @@ __global__ void __launch_bounds__(kThreads) k_b_hv(const SegDev* __restrict__ se
   }
 }
 
-// tile partials of <V_j|w> (mode 0) or |w|^2 (mode 1), FP64 compensated
+// tile partials of <V_j|w> (mode 0) or |w|^2 (mode 1): exact products summed
+// in float-float per thread (ff.cuh), FP64 across the CTA
 __global__ void __launch_bounds__(kThreads) k_b_dot(const SegDev* __restrict__ segs, const SegState* __restrict__ ss,
                                                     const TileDev* __restrict__ tiles, double* __restrict__ part,
                                                     int mode) {
@@ -172,16 +177,19 @@ __global__ void __launch_bounds__(kThreads) k_b_dot(const SegDev* __restrict__ s
   if (ss[t.seg].status == kRunning) {
     const SegDev& S = segs[t.seg];
     const float2* v = S.V + (int64_t)ss[t.seg].j * S.n;
-    Acc sr, si;
+    FFAcc sr, si;
     for (int r = threadIdx.x; r < t.rows; r += blockDim.x) {
       const int64_t i = t.row0 + r;
       const float2 y = S.w[i];
       if (mode == 0) {
         const float2 x = v[i];
-        sr.add((double)x.x * y.x + (double)x.y * y.y);
-        si.add((double)x.x * y.y - (double)x.y * y.x);
+        sr.add_prod(x.x, y.x);
+        sr.add_prod(x.y, y.y);
+        si.add_prod(x.x, y.y);
+        si.sub_prod(x.y, y.x);
       } else {
-        sr.add((double)y.x * y.x + (double)y.y * y.y);
+        sr.add_prod(y.x, y.x);
+        sr.add_prod(y.y, y.y);
       }
     }
     a = sr.value();
@@ -220,19 +228,14 @@ __global__ void __launch_bounds__(kThreads) k_b_step(const SegDev* __restrict__ 
   if (ss[t.seg].status != kRunning) return;
   const SegDev& S = segs[t.seg];
   const int j = ss[t.seg].j;
-  const double a = S.alpha[j], b = j > 0 ? S.beta[j] : 0.0;
+  const FFScalar a(S.alpha[j]), b(j > 0 ? S.beta[j] : 0.0);
   const float2* v = S.V + (int64_t)j * S.n;
   const float2* vp = j > 0 ? v - S.n : nullptr;
   for (int r = threadIdx.x; r < t.rows; r += blockDim.x) {
     const int64_t i = t.row0 + r;
     const float2 y = S.w[i], x = v[i];
-    double re = (double)y.x - a * x.x, im = (double)y.y - a * x.y;
-    if (vp) {
-      const float2 p = vp[i];
-      re -= b * p.x;
-      im -= b * p.y;
-    }
-    S.w[i] = make_float2((float)re, (float)im);
+    const float2 p = vp ? vp[i] : make_float2(0.f, 0.f);
+    S.w[i] = make_float2(ff_axpy2(y.x, a, x.x, b, p.x), ff_axpy2(y.y, a, x.y, b, p.y));
   }
 }
 
@@ -246,12 +249,14 @@ __global__ void __launch_bounds__(kThreads) k_b_cgs_dot(const SegDev* __restrict
   const int K = ss[t.seg].status == kRunning ? ss[t.seg].j + 1 : 0;
   for (int k = blockIdx.y; k < K; k += kCgsY) {  // K is the same for every thread of the CTA
     const float2* vk = S.V + (int64_t)k * S.n;
-    Acc sr, si;
+    FFAcc sr, si;
     for (int r = threadIdx.x; r < t.rows; r += blockDim.x) {
       const int64_t i = t.row0 + r;
       const float2 x = vk[i], y = S.w[i];
-      sr.add((double)x.x * y.x + (double)x.y * y.y);
-      si.add((double)x.x * y.y - (double)x.y * y.x);
+      sr.add_prod(x.x, y.x);
+      sr.add_prod(x.y, y.y);
+      si.add_prod(x.x, y.y);
+      si.sub_prod(x.y, y.x);
     }
     double a = sr.value(), b = si.value();
     block_sum2(a, b);
@@ -291,20 +296,21 @@ __global__ void __launch_bounds__(kThreads) k_b_cgs_sub(const SegDev* __restrict
   const TileDev t = tiles[blockIdx.x];
   if (ss[t.seg].status != kRunning) return;
   const SegDev& S = segs[t.seg];
-  __shared__ double sq[2 * (kMaxSteps + 1)];
+  __shared__ float sq[2 * (kMaxSteps + 1)];
   const int K = ss[t.seg].j + 1;
-  for (int k = threadIdx.x; k < 2 * K; k += blockDim.x) sq[k] = S.q[k];
+  for (int k = threadIdx.x; k < 2 * K; k += blockDim.x) sq[k] = (float)S.q[k];
   __syncthreads();
+  // FP32: the q_k are tiny against |w| once the vectors are nearly orthogonal
   for (int r = threadIdx.x; r < t.rows; r += blockDim.x) {
     const int64_t i = t.row0 + r;
     const float2 y = S.w[i];
-    double re = y.x, im = y.y;
+    float re = y.x, im = y.y;
     for (int k = 0; k < K; ++k) {
       const float2 x = S.V[(int64_t)k * S.n + i];
-      re -= sq[2 * k] * x.x - sq[2 * k + 1] * x.y;
-      im -= sq[2 * k] * x.y + sq[2 * k + 1] * x.x;
+      re = fmaf(-sq[2 * k], x.x, fmaf(sq[2 * k + 1], x.y, re));
+      im = fmaf(-sq[2 * k], x.y, fmaf(-sq[2 * k + 1], x.x, im));
     }
-    S.w[i] = make_float2((float)re, (float)im);
+    S.w[i] = make_float2(re, im);
   }
 }
 
@@ -315,12 +321,12 @@ __global__ void __launch_bounds__(kThreads) k_b_scale(const SegDev* __restrict__
   if (ss[t.seg].status != kRunning) return;
   const SegDev& S = segs[t.seg];
   const int j = ss[t.seg].j;
-  const double s = 1.0 / S.beta[j + 1];
+  const FFScalar s(1.0 / S.beta[j + 1]);
   float2* vn = S.V + (int64_t)(j + 1) * S.n;
   for (int r = threadIdx.x; r < t.rows; r += blockDim.x) {
     const int64_t i = t.row0 + r;
     const float2 y = S.w[i];
-    vn[i] = make_float2((float)(y.x * s), (float)(y.y * s));
+    vn[i] = make_float2(fmaf(y.x, s.l, __fmul_rn(y.x, s.h)), fmaf(y.y, s.l, __fmul_rn(y.y, s.h)));
   }
 }
 
@@ -356,16 +362,19 @@ __global__ void __launch_bounds__(128) k_b_check(const SegDev* __restrict__ segs
   if (threadIdx.x == 0 && ok) ss[blockIdx.x].status = kConverged;
 }
 
-// start vector V_0 = x / |x| of one segment (one CTA: the norm is FP64 compensated)
+// start vector V_0 = x / |x| of one segment (one CTA)
 __global__ void __launch_bounds__(kThreads) k_b_start(float2* __restrict__ V0, const float2* __restrict__ x,
                                                       int64_t n) {
-  Acc s;
-  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s.add((double)x[i].x * x[i].x + (double)x[i].y * x[i].y);
+  FFAcc s;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    s.add_prod(x[i].x, x[i].x);
+    s.add_prod(x[i].y, x[i].y);
+  }
   double a = s.value(), b = 0;
   block_sum2(a, b);
-  const double inv = 1.0 / sqrt(a);
+  const FFScalar inv(1.0 / sqrt(a));
   for (int64_t i = threadIdx.x; i < n; i += blockDim.x)
-    V0[i] = make_float2((float)(x[i].x * inv), (float)(x[i].y * inv));
+    V0[i] = make_float2(fmaf(x[i].x, inv.l, __fmul_rn(x[i].x, inv.h)), fmaf(x[i].y, inv.l, __fmul_rn(x[i].y, inv.h)));
 }
 
 struct Segment {
@@ -401,6 +410,9 @@ struct Batch {
   cudaGraphExec_t graph = nullptr;
   int64_t device_bytes = 0, steps = 0;
   MixedFinish fin;
+  // host seconds: add, step (graph replays and waits), finish (T, Ritz
+  // vectors, Rayleigh quotients), release, rebuild (tables and graph capture)
+  double timers[5] = {0, 0, 0, 0, 0};
 
   ~Batch() {
     if (st) cudaStreamSynchronize(st);
@@ -432,42 +444,115 @@ cudaError_t pull_state(Batch& B) {
   return cudaSuccess;
 }
 
-// finish every stopped segment: Ritz values, FP64 Rayleigh quotients, residuals
+using Clock = std::chrono::steady_clock;
+double since(Clock::time_point t0) { return std::chrono::duration<double>(Clock::now() - t0).count(); }
+
+template <class F>
+void parallel_for(int n, F f) {
+  const int nt = std::max(1, std::min<int>(n, (int)std::thread::hardware_concurrency()));
+  if (nt <= 1) {
+    for (int i = 0; i < n; ++i) f(i);
+    return;
+  }
+  std::vector<std::thread> th;
+  for (int t = 0; t < nt; ++t)
+    th.emplace_back([&, t] {
+      for (int i = t; i < n; i += nt) f(i);
+    });
+  for (auto& x : th) x.join();
+}
+
+// Finish every stopped segment: its alpha/beta come back in one wait, the
+// Ritz selection of T runs on host threads, then each segment's FP64 Ritz
+// vectors and Rayleigh quotients are queued and read back in one more wait.
 void finish_stopped(Batch& B) {
-  std::vector<Segment> keep;
-  for (size_t k = 0; k < B.segs.size(); ++k) {
-    Segment& g = B.segs[k];
-    if (g.st.status == kRunning) {
-      keep.push_back(g);
-      continue;
-    }
+  const auto tf = Clock::now();
+  std::vector<int> idx;
+  for (size_t k = 0; k < B.segs.size(); ++k)
+    if (B.segs[k].st.status != kRunning) idx.push_back((int)k);
+  if (idx.empty()) return;
+  const int ns = (int)idx.size();
+  std::vector<std::vector<double>> ah(ns), bh(ns);
+  for (int i = 0; i < ns; ++i) {
+    const Segment& g = B.segs[idx[i]];
+    ah[i].resize(g.st.j);
+    bh[i].resize(g.st.j + 1);
+    cudaMemcpyAsync(ah[i].data(), g.d.alpha, sizeof(double) * g.st.j, cudaMemcpyDeviceToHost, B.st);
+    cudaMemcpyAsync(bh[i].data(), g.d.beta, sizeof(double) * (g.st.j + 1), cudaMemcpyDeviceToHost, B.st);
+  }
+  std::vector<int> status(ns, EDG_OK);
+  cudaError_t e = cudaStreamSynchronize(B.st);
+  if (e != cudaSuccess) std::fill(status.begin(), status.end(), cuda_fail(e, "batch: T"));
+  std::vector<RitzSel> sel(ns);
+  parallel_for(ns, [&](int i) {
+    const Segment& g = B.segs[idx[i]];
+    const int m = g.st.j, n_try = std::min(kMaxEv, std::min(g.req.n_ev + 4, m));
+    if (status[i] == EDG_OK) ritz_select(ah[i].data(), bh[i].data(), m, n_try, 2 * n_try + 8, sel[i]);
+  });
+  int64_t n_max = 1, x_max = 1;
+  int m_max = 1, total = 0;
+  std::vector<int> off(ns, 0);
+  for (int i = 0; i < ns; ++i) {
+    const Segment& g = B.segs[idx[i]];
+    const int na = (int)sel[i].acc.size();
+    if (status[i] == EDG_OK && na == 0)
+      status[i] = fail(EDG_ERR_NOT_CONVERGED, "batch: no Ritz value survived the copy test");
+    n_max = std::max(n_max, g.d.n);
+    x_max = std::max(x_max, g.d.n * na);
+    m_max = std::max(m_max, g.st.j);
+    off[i] = total;
+    total += na;
+  }
+  if (B.fin.reserve(n_max, m_max, total) != cudaSuccess || B.fin.reserve_x(x_max, 1) != cudaSuccess) {
+    cudaGetLastError();
+    for (int& s : status)
+      if (s == EDG_OK) s = fail(EDG_ERR_NOMEM, "batch: finishing scratch");
+  }
+  for (int i = 0; i < ns; ++i) {
+    if (status[i] != EDG_OK) continue;
+    Segment& g = B.segs[idx[i]];
+    const int m = g.st.j, na = (int)sel[i].acc.size();
+    cudaMemcpyAsync(B.fin.y, sel[i].y.data(), sizeof(double) * na * m, cudaMemcpyHostToDevice, B.st);
+    status[i] = B.fin.ritz_stored(B.st, g.d.V, g.d.n, m, na);
+    if (status[i] == EDG_OK && (e = B.fin.rayleigh_async(g.sec->s, B.st, g.d.n, na, B.fin.res + 4 * off[i])) != cudaSuccess)
+      status[i] = cuda_fail(e, "batch: FP64 H*v");
+  }
+  std::vector<double> rr(4 * (size_t)std::max(total, 1));
+  cudaMemcpyAsync(rr.data(), B.fin.res, sizeof(double) * 4 * total, cudaMemcpyDeviceToHost, B.st);
+  if ((e = cudaStreamSynchronize(B.st)) != cudaSuccess) {
+    const int rc = cuda_fail(e, "batch: residuals");
+    for (int& s : status) s = rc;
+  }
+  for (int i = 0; i < ns; ++i) {
+    Segment& g = B.segs[idx[i]];
     edg_batch_result r{};
     r.tag = g.req.tag;
     r.iterations = g.st.j;
     r.converged = g.st.status == kConverged;
-    const int m = g.st.j, n_try = std::min(kBatchMaxEv, std::min(g.req.n_ev + 4, m));
-    const int64_t n = g.d.n;
-    int na = 0, rc = EDG_OK;
-    std::vector<int> acc_h;
-    std::vector<double> th, rr;
-    if (B.fin.reserve(n, m) != cudaSuccess) rc = fail(EDG_ERR_NOMEM, "batch: finishing scratch");
-    if (rc == EDG_OK) rc = B.fin.tridiag(B.st, g.d.alpha, g.d.beta, m, n_try, &na, acc_h, th);
-    if (rc == EDG_OK && na == 0) rc = fail(EDG_ERR_NOT_CONVERGED, "batch: no Ritz value survived the copy test");
-    if (rc == EDG_OK && B.fin.reserve_x(n, na) != cudaSuccess) rc = fail(EDG_ERR_NOMEM, "batch: FP64 Ritz vectors");
-    if (rc == EDG_OK) rc = B.fin.ritz_stored(B.st, g.d.V, n, m, na);
-    if (rc == EDG_OK) rc = B.fin.rayleigh(g.sec->s, B.st, n, na, rr);
-    if (rc == EDG_OK) {
-      std::vector<int> sel;
-      pick_levels(rr, th, acc_h, na, g.req.n_ev, r.eigs, r.ritz, r.residuals, sel);
-      r.n_found = (int)sel.size();
+    r.status = status[i];
+    if (status[i] == EDG_OK) {
+      const int na = (int)sel[i].acc.size();
+      std::vector<double> ri(rr.begin() + 4 * off[i], rr.begin() + 4 * (off[i] + na));
+      std::vector<int> keep;
+      pick_levels(ri, sel[i].theta, sel[i].acc, na, g.req.n_ev, r.eigs, r.ritz, r.residuals, keep);
+      r.n_found = (int)keep.size();
     }
-    r.status = rc;
     B.done.push_back(r);
+  }
+  B.timers[2] += since(tf);
+  const auto tr = Clock::now();
+  std::vector<Segment> keep;
+  for (Segment& g : B.segs) {
+    if (g.st.status == kRunning) {
+      keep.push_back(g);
+      continue;
+    }
     B.device_bytes -= g.bytes;
     release(g);
-    B.dirty = true;
   }
   B.segs.swap(keep);
+  B.dirty = true;
+  B.timers[3] += since(tr);
 }
 
 // upload the tables of the current segments and capture one step as a graph
@@ -557,7 +642,9 @@ int settle(Batch& B) {
     if (B.segs[k].st.status != kRunning) B.dirty = true;
   if (!B.dirty) return EDG_OK;
   finish_stopped(B);
+  const auto t0 = Clock::now();
   const int rc = rebuild(B);
+  B.timers[4] += since(t0);
   return rc == EDG_OK ? EDG_OK : fail(rc, "batch: rebuilding the step graph failed");
 }
 
@@ -605,6 +692,7 @@ int edg_batch_footprint(const edg_sector* s, const edg_batch_request* req, int64
 int edg_batch_add(edg_batch* bh, edg_sector* sec, const edg_batch_request* req) {
   if (!bh || !sec || !req) return fail(EDG_ERR_INVALID, "NULL argument");
   Batch& B = bh->b;
+  const auto t_add = Clock::now();
   Sector& S = sec->s;
   if (!S.col) return fail(EDG_ERR_INVALID, "batch segments need stored rows (edg_sector_build_targets)");
   if (req->n_ev < 1 || req->n_ev > kBatchMaxEv) return fail(EDG_ERR_INVALID, "n_ev must be in [1, 32]");
@@ -659,6 +747,7 @@ int edg_batch_add(edg_batch* bh, edg_sector* sec, const edg_batch_request* req) 
   B.segs.push_back(g);
   B.device_bytes += g.bytes;
   B.dirty = true;
+  B.timers[0] += since(t_add);
   return EDG_OK;
 }
 
@@ -669,10 +758,18 @@ int edg_batch_step(edg_batch* bh, int n_steps) {
   for (int s = 0; s < n_steps && rc == EDG_OK; ++s) {
     if (B.dirty && (rc = settle(B)) != EDG_OK) break;
     if (B.n_dev == 0) break;
+    const auto t0 = Clock::now();
     const cudaError_t e = cudaGraphLaunch(B.graph, B.st);
     if (e != cudaSuccess) return cuda_fail(e, "batch step");
     ++B.steps;
-    if (B.steps % B.opts.check_every == 0) rc = settle(B);
+    if (B.steps % B.opts.check_every == 0) {
+      const cudaError_t es = cudaStreamSynchronize(B.st);
+      if (es != cudaSuccess) return cuda_fail(es, "batch step");
+      B.timers[1] += since(t0);
+      rc = settle(B);
+    } else {
+      B.timers[1] += since(t0);
+    }
   }
   if (rc == EDG_OK) rc = settle(B);
   return rc;
@@ -685,6 +782,12 @@ int edg_batch_poll(edg_batch* bh, edg_batch_result* out, int cap, int* n_out) {
   for (int k = 0; k < n; ++k) out[k] = B.done[k];
   B.done.erase(B.done.begin(), B.done.begin() + n);
   *n_out = n;
+  return EDG_OK;
+}
+
+int edg_batch_timers(const edg_batch* bh, double* seconds) {
+  if (!bh || !seconds) return fail(EDG_ERR_INVALID, "NULL argument");
+  for (int k = 0; k < 5; ++k) seconds[k] = bh->b.timers[k];
   return EDG_OK;
 }
 

@@ -113,26 +113,23 @@ int solve_plain(Sector& S, const edg_solver_opts& o, double* eigs, int64_t cap, 
 int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, double* resid, int64_t* n_out,
                 double* evecs, edg_mixed_stats* stats);
 // lanczos_mixed.cu: the end of a mixed-precision Lanczos run, shared by the
-// single-sector solver and the batch: T's Ritz pairs (with the copy test),
-// FP64 Ritz vectors, and one FP64 H*v per Ritz vector for its Rayleigh
-// quotient and residual.  Device scratch grows on demand and is reused.
+// single-sector solver and the batch: FP64 Ritz vectors from the host-chosen
+// Ritz coefficients (lanczos_common.cuh), and one FP64 H*v per Ritz vector
+// for its Rayleigh quotient and residual.  Device scratch grows on demand.
 struct MixedFinish {
-  double *theta = nullptr, *theta_hat = nullptr, *y = nullptr, *work = nullptr;
-  int *acc = nullptr, *nacc = nullptr;
+  double* y = nullptr;    // Ritz coefficients, na x m
   double2 *X = nullptr, *HX = nullptr;
-  double *part = nullptr, *res = nullptr;
-  size_t y_bytes = 0, work_bytes = 0, hx_bytes = 0, x_bytes = 0;
+  double* part = nullptr;
+  double* res = nullptr;  // 4 doubles per Ritz vector
+  size_t y_bytes = 0, hx_bytes = 0, x_bytes = 0, res_bytes = 0;
   ~MixedFinish();
-  cudaError_t reserve(int64_t n, int m);
+  cudaError_t reserve(int64_t n, int m, int n_res);
   cudaError_t reserve_x(int64_t n, int na);
-  // k_tridiag on alpha[0..m-1], beta[1..m-1]; na accepted Ritz values,
-  // acc_h their indices into th (T's lowest eigenvalues); Ritz coefficients in y
-  int tridiag(cudaStream_t st, const double* alpha, const double* beta, int m, int n_try, int* na,
-              std::vector<int>& acc_h, std::vector<double>& th);
   // X_q = sum_j y_q[j] V_j from m stored FP32 vectors (leading dimension n)
   int ritz_stored(cudaStream_t st, const float2* V, int64_t n, int m, int na);
-  // out[4q..4q+3] = |x_q|^2, <x_q|H x_q>, Rayleigh quotient, residual
-  int rayleigh(Sector& S, cudaStream_t st, int64_t n, int na, std::vector<double>& out);
+  // res[4q..4q+3] = |x_q|^2, <x_q|H x_q>, Rayleigh quotient, residual, queued
+  // on st (no wait)
+  cudaError_t rayleigh_async(Sector& S, cudaStream_t st, int64_t n, int na, double* res_dev);
 };
 void pick_levels(const std::vector<double>& rr, const std::vector<double>& th, const std::vector<int>& acc_h, int na,
                  int want, double* eigs, double* ritz, double* resid, std::vector<int>& keep);

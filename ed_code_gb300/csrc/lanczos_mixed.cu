@@ -11,7 +11,8 @@
 //    vectors orthogonality decays within a few steps once a level converges:
 //    every step (1) or every few steps keeps T exact; every 20 steps does not;
 //    reorth_every = 0 keeps three vectors resident (the 36-site case: 2 GB
-//    each) and removes the copies of converged levels afterwards;
+//    each), reorthogonalises w locally against the two latest vectors each
+//    step, and removes the copies of converged levels afterwards;
 //  * T's lowest eigenvalues by bisection and their eigenvectors by inverse
 //    iteration, in FP64 in one CTA on the GPU; Ritz values that T shares with
 //    T-without-its-first-row are copies produced by lost orthogonality and are
@@ -32,6 +33,7 @@
 #include "../../include/edgpu.h"
 #include "blas1.cuh"
 #include "edg_sector.cuh"
+#include "ff.cuh"
 #include "tridiag.cuh"
 #include "lanczos_common.cuh"
 
@@ -43,17 +45,20 @@ int cuda_fail(cudaError_t e, const char* what);
 namespace {
 
 
-// partial sums of sum conj(a) b over FP32 vectors, FP64 compensated;
+// partial sums of sum conj(a) b over FP32 vectors: exact products summed in
+// float-float per thread, FP64 across threads;
 // part[(k*gridDim.x + b)*2 + {0,1}], k = blockIdx.y selects a = V + k*ld
 __global__ void __launch_bounds__(kRedThreads) k_dot32(const float2* __restrict__ V, int64_t ld,
                                                        const float2* __restrict__ x, int64_t n,
                                                        double* __restrict__ part) {
   const float2* a = V + (int64_t)blockIdx.y * ld;
-  Acc sr, si;
+  FFAcc sr, si;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const float2 p = a[i], q = x[i];
-    sr.add((double)p.x * q.x + (double)p.y * q.y);
-    si.add((double)p.x * q.y - (double)p.y * q.x);
+    sr.add_prod(p.x, q.x);
+    sr.add_prod(p.y, q.y);
+    si.add_prod(p.x, q.y);
+    si.sub_prod(p.y, q.x);
   }
   __shared__ double rr[kRedThreads], ri[kRedThreads];
   rr[threadIdx.x] = sr.value();
@@ -106,26 +111,22 @@ __global__ void __launch_bounds__(kRedThreads) k_finish(const double* __restrict
   }
 }
 
-// w = w - alpha v - beta vprev (FP64 arithmetic, FP32 storage), and partial
-// sums of |w|^2 of the stored values.
+// w = w - alpha v - beta vprev (float-float with FP64 alpha/beta, one final
+// rounding to the FP32 storage), and partial sums of |w|^2 of the stored values.
 __global__ void __launch_bounds__(kRedThreads) k_step(float2* __restrict__ w, const float2* __restrict__ v,
                                                       const float2* __restrict__ vprev,
                                                       const double* __restrict__ alpha,
                                                       const double* __restrict__ beta, int64_t n,
                                                       double* __restrict__ part) {
-  const double a = *alpha, b = vprev ? *beta : 0.0;
-  Acc s;
+  const FFScalar a(*alpha), b(vprev ? *beta : 0.0);
+  FFAcc s;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const float2 wi = w[i], vi = v[i];
-    double re = (double)wi.x - a * vi.x, im = (double)wi.y - a * vi.y;
-    if (vprev) {
-      const float2 pi = vprev[i];
-      re -= b * pi.x;
-      im -= b * pi.y;
-    }
-    const float2 o = make_float2((float)re, (float)im);
+    const float2 pi = vprev ? vprev[i] : make_float2(0.f, 0.f);
+    const float2 o = make_float2(ff_axpy2(wi.x, a, vi.x, b, pi.x), ff_axpy2(wi.y, a, vi.y, b, pi.y));
     w[i] = o;
-    s.add((double)o.x * o.x + (double)o.y * o.y);
+    s.add_prod(o.x, o.x);
+    s.add_prod(o.y, o.y);
   }
   __shared__ double rr[kRedThreads];
   rr[threadIdx.x] = s.value();
@@ -140,30 +141,33 @@ __global__ void __launch_bounds__(kRedThreads) k_step(float2* __restrict__ w, co
   }
 }
 
-// dst = src / beta (dst may be src)
+// dst = src / beta (dst may be src); 1/beta as an FP32 head and tail
 __global__ void k_scale_inv(float2* dst, const float2* src, const double* __restrict__ beta, int64_t n) {
-  const double s = 1.0 / *beta;
+  const FFScalar s(1.0 / *beta);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const float2 x = src[i];
-    dst[i] = make_float2((float)(x.x * s), (float)(x.y * s));
+    dst[i] = make_float2(fmaf(x.x, s.l, __fmul_rn(x.x, s.h)), fmaf(x.y, s.l, __fmul_rn(x.y, s.h)));
   }
 }
 
-// y -= sum_k q_k V_k with q (complex, device) read into shared memory
+// y -= sum_k q_k V_k with q (complex, device) read into shared memory.  The
+// q_k are tiny against |y| once the vectors are nearly orthogonal, so FP32
+// arithmetic adds errors far below the FP32 rounding of y itself.
 __global__ void k_sub32(float2* __restrict__ y, const float2* __restrict__ V, int64_t ld,
                         const double* __restrict__ q, int K, int64_t n) {
-  extern __shared__ double sq[];
-  for (int k = threadIdx.x; k < 2 * K; k += blockDim.x) sq[k] = q[k];
+  extern __shared__ float sqf[];
+  for (int k = threadIdx.x; k < 2 * K; k += blockDim.x) sqf[k] = (float)q[k];
   __syncthreads();
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const float2 y0 = y[i];
-    double re = y0.x, im = y0.y;
+    float re = y0.x, im = y0.y;
     for (int k = 0; k < K; ++k) {
       const float2 vv = V[(int64_t)k * ld + i];
-      re -= sq[2 * k] * vv.x - sq[2 * k + 1] * vv.y;
-      im -= sq[2 * k] * vv.y + sq[2 * k + 1] * vv.x;
+      const float qr = sqf[2 * k], qi = sqf[2 * k + 1];
+      re = fmaf(-qr, vv.x, fmaf(qi, vv.y, re));
+      im = fmaf(-qr, vv.y, fmaf(-qi, vv.x, im));
     }
-    y[i] = make_float2((float)re, (float)im);
+    y[i] = make_float2(re, im);
   }
 }
 
@@ -298,56 +302,31 @@ struct Dev {
 }  // namespace
 
 MixedFinish::~MixedFinish() {
-  void* p[] = {theta, theta_hat, y, work, acc, nacc, X, HX, part, res};
+  void* p[] = {y, X, HX, part, res};
   for (void* q : p)
     if (q) cudaFree(q);
 }
 
-cudaError_t MixedFinish::reserve(int64_t n, int m) {
-  auto grow = [](void** p, size_t bytes, size_t& have) -> cudaError_t {
-    if (bytes <= have) return cudaSuccess;
-    if (*p) cudaFree(*p);
-    *p = nullptr;
-    have = 0;
-    cudaError_t e = cudaMalloc(p, bytes);
-    if (e == cudaSuccess) have = bytes;
-    return e;
-  };
-  cudaError_t e = cudaSuccess;
-  if (!theta) {
-    if ((e = cudaMalloc(&theta, sizeof(double) * kCand)) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&theta_hat, sizeof(double) * kCand)) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&acc, sizeof(int) * kMaxEv)) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&nacc, sizeof(int))) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&part, sizeof(double) * 3 * kRedBlocks)) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&res, sizeof(double) * 4 * kMaxEv)) != cudaSuccess) return e;
-  }
-  if ((e = grow((void**)&y, sizeof(double) * kMaxEv * m, y_bytes)) != cudaSuccess) return e;
-  if ((e = grow((void**)&work, sizeof(double) * kMaxEv * 5 * m, work_bytes)) != cudaSuccess) return e;
-  if ((e = grow((void**)&HX, sizeof(double2) * n, hx_bytes)) != cudaSuccess) return e;
-  return cudaSuccess;
-}
-
-cudaError_t MixedFinish::reserve_x(int64_t n, int na) {
-  if (sizeof(double2) * n * na <= x_bytes) return cudaSuccess;
-  if (X) cudaFree(X);
-  X = nullptr;
-  x_bytes = 0;
-  cudaError_t e = cudaMalloc(&X, sizeof(double2) * n * na);
-  if (e == cudaSuccess) x_bytes = sizeof(double2) * n * na;
+static cudaError_t grow(void** p, size_t bytes, size_t& have) {
+  if (bytes <= have) return cudaSuccess;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  have = 0;
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e == cudaSuccess) have = bytes;
   return e;
 }
 
-int MixedFinish::tridiag(cudaStream_t st, const double* alpha, const double* beta, int m, int n_try, int* na,
-                         std::vector<int>& acc_h, std::vector<double>& th) {
-  k_tridiag<<<1, 128, sizeof(double) * 2 * m, st>>>(alpha, beta, m, n_try, theta, theta_hat, y, work, acc, nacc);
-  acc_h.assign(kMaxEv, 0);
-  th.assign(kCand, 0.0);
-  cudaMemcpyAsync(na, nacc, sizeof(int), cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(acc_h.data(), acc, sizeof(int) * kMaxEv, cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(th.data(), theta, sizeof(double) * std::min(kCand, m), cudaMemcpyDeviceToHost, st);
-  const cudaError_t e = cudaStreamSynchronize(st);
-  return e == cudaSuccess ? EDG_OK : cuda_fail(e, "mixed Lanczos: T");
+cudaError_t MixedFinish::reserve(int64_t n, int m, int n_res) {
+  cudaError_t e = cudaSuccess;
+  if (!part && (e = cudaMalloc(&part, sizeof(double) * 3 * kRedBlocks)) != cudaSuccess) return e;
+  if ((e = grow((void**)&y, sizeof(double) * kMaxEv * m, y_bytes)) != cudaSuccess) return e;
+  if ((e = grow((void**)&HX, sizeof(double2) * n, hx_bytes)) != cudaSuccess) return e;
+  return grow((void**)&res, sizeof(double) * 4 * std::max(n_res, kMaxEv), res_bytes);
+}
+
+cudaError_t MixedFinish::reserve_x(int64_t n, int na) {
+  return grow((void**)&X, sizeof(double2) * n * na, x_bytes);
 }
 
 int MixedFinish::ritz_stored(cudaStream_t st, const float2* V, int64_t n, int m, int na) {
@@ -359,20 +338,17 @@ int MixedFinish::ritz_stored(cudaStream_t st, const float2* V, int64_t n, int m,
   return e == cudaSuccess ? EDG_OK : cuda_fail(e, "mixed Lanczos: Ritz vectors");
 }
 
-int MixedFinish::rayleigh(Sector& S, cudaStream_t st, int64_t n, int na, std::vector<double>& out) {
+cudaError_t MixedFinish::rayleigh_async(Sector& S, cudaStream_t st, int64_t n, int na, double* res_dev) {
   for (int q = 0; q < na; ++q) {
     double2* x = X + (int64_t)q * n;
     cudaError_t e = launch_hv(S, x, HX, true, st);
-    if (e != cudaSuccess) return cuda_fail(e, "mixed Lanczos: FP64 H*v");
+    if (e != cudaSuccess) return e;
     k_rq_partial<<<kRedBlocks, kRedThreads, 0, st>>>(x, HX, n, nullptr, part);
-    k_rq_sum<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, res + 4 * q, 0);
-    k_rq_partial<<<kRedBlocks, kRedThreads, 0, st>>>(x, HX, n, res + 4 * q + 2, part);
-    k_rq_sum<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, res + 4 * q, 1);
+    k_rq_sum<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, res_dev + 4 * q, 0);
+    k_rq_partial<<<kRedBlocks, kRedThreads, 0, st>>>(x, HX, n, res_dev + 4 * q + 2, part);
+    k_rq_sum<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, res_dev + 4 * q, 1);
   }
-  out.assign(4 * (size_t)na, 0.0);
-  cudaMemcpyAsync(out.data(), res, sizeof(double) * 4 * na, cudaMemcpyDeviceToHost, st);
-  const cudaError_t e = cudaStreamSynchronize(st);
-  return e == cudaSuccess ? EDG_OK : cuda_fail(e, "mixed Lanczos: residual");
+  return cudaGetLastError();
 }
 
 // A Rayleigh quotient within 1e-8 relative of an earlier one is the same level
@@ -406,7 +382,7 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
   const auto t_start = clk::now();
   Dev D;
   float2 *V = nullptr, *w = nullptr, *buf[3] = {nullptr, nullptr, nullptr};
-  double *alpha, *beta, *part, *scal;
+  double *alpha, *beta, *part, *scal, *lq;
   cudaError_t e = cudaSuccess;
   if (store) {
     if ((e = D.alloc(&V, (size_t)n * (m + 1))) != cudaSuccess)
@@ -418,7 +394,8 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
   if ((e = D.alloc(&w, (size_t)n)) != cudaSuccess) return fail(EDG_ERR_NOMEM, "mixed Lanczos: w");
   const int64_t kparts = (int64_t)std::max(m + 1, 4) * kRedBlocks * 2;
   if ((e = D.alloc(&alpha, m + 1)) != cudaSuccess || (e = D.alloc(&beta, m + 2)) != cudaSuccess ||
-      (e = D.alloc(&part, kparts)) != cudaSuccess || (e = D.alloc(&scal, 2 * (m + 2) + 2)) != cudaSuccess)
+      (e = D.alloc(&part, kparts)) != cudaSuccess || (e = D.alloc(&scal, 2 * (m + 2) + 2)) != cudaSuccess ||
+      (e = D.alloc(&lq, 2)) != cudaSuccess)
     return fail(EDG_ERR_NOMEM, "mixed Lanczos: scratch");
   cudaMemsetAsync(beta, 0, sizeof(double) * (m + 2), st);
 
@@ -465,7 +442,7 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
               const int kk = std::min(512, K - k0);
               k_dot32<<<dim3(kRedBlocks, kk), kRedThreads, 0, st>>>(V + (int64_t)k0 * n, n, x, n, part);
               k_finish<<<kk, kRedThreads, 0, st>>>(part, kRedBlocks, scal, 0);
-              k_sub32<<<grid_n(n), 256, sizeof(double) * 2 * kk, st>>>(x, V + (int64_t)k0 * n, n, scal, kk, n);
+              k_sub32<<<grid_n(n), 256, sizeof(float) * 2 * kk, st>>>(x, V + (int64_t)k0 * n, n, scal, kk, n);
             }
         };
         if (o.reorth_every > 1 && j > 0) {
@@ -475,6 +452,18 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
         }
         cgs2(w, j + 1);
         norm_into(w, beta + j + 1);
+      } else if (!store) {
+        // Local reorthogonalisation of w against v_j and v_{j-1}, the vectors
+        // still resident: it slows the growth of the copies that FP32 vectors
+        // make without full reorthogonalisation.  The second pass repeats it
+        // (the kernels are deterministic, so with the same coefficients).
+        for (int b = 0; b < (j > 0 ? 2 : 1); ++b) {
+          const float2* vb = vec(j - b);
+          k_dot32<<<dim3(kRedBlocks, 1), kRedThreads, 0, st>>>(vb, 0, w, n, part);
+          k_finish<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, lq, 0);
+          k_sub32<<<grid_n(n), 256, sizeof(float) * 2, st>>>(w, vb, n, lq, 1, n);
+        }
+        if (!second) norm_into(w, beta + j + 1);
       } else if (!second) {
         k_finish<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, beta + j + 1, 2);
       }
@@ -485,32 +474,37 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
     return cudaStreamSynchronize(st);
   };
   if ((e = run(false, nullptr, 0, {})) != cudaSuccess) return cuda_fail(e, "mixed Lanczos");
-  // eigenvalues and Ritz coefficients of T on the device
+  // Ritz values and coefficients of T on the host
   MixedFinish F;
-  if ((e = F.reserve(n, m)) != cudaSuccess) return fail(EDG_ERR_NOMEM, "mixed Lanczos: scratch");
   const int n_try = std::min(kMaxEv, std::min(want + 4, m));
-  int na = 0;
-  std::vector<int> acc_h;
-  std::vector<double> th;
-  int rc = F.tridiag(st, alpha, beta, m, n_try, &na, acc_h, th);
-  if (rc != EDG_OK) return rc;
+  if ((e = F.reserve(n, m, n_try)) != cudaSuccess) return fail(EDG_ERR_NOMEM, "mixed Lanczos: scratch");
+  std::vector<double> ah(m), bh(m + 1);
+  cudaMemcpyAsync(ah.data(), alpha, sizeof(double) * m, cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(bh.data(), beta, sizeof(double) * (m + 1), cudaMemcpyDeviceToHost, st);
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "mixed Lanczos: T");
+  RitzSel sel;
+  ritz_select(ah.data(), bh.data(), m, n_try, kCand, sel);
+  const int na = (int)sel.acc.size();
+  const std::vector<int>& acc_h = sel.acc;
+  const std::vector<double>& th = sel.theta;
   if (na == 0) return fail(EDG_ERR_NOT_CONVERGED, "mixed Lanczos: no Ritz value survived the copy test");
+  cudaMemcpyAsync(F.y, sel.y.data(), sizeof(double) * na * m, cudaMemcpyHostToDevice, st);
   // Ritz vectors in FP64
   if ((e = F.reserve_x(n, na)) != cudaSuccess) return fail(EDG_ERR_NOMEM, "mixed Lanczos: FP64 Ritz vectors do not fit");
   int passes = 1;
+  int rc = EDG_OK;
   if (store) {
     if ((rc = F.ritz_stored(st, V, n, m, na)) != EDG_OK) return rc;
   } else {
     passes = 2;
-    std::vector<double> yh((size_t)na * m);
-    cudaMemcpyAsync(yh.data(), F.y, sizeof(double) * na * m, cudaMemcpyDeviceToHost, st);
     cudaMemsetAsync(F.X, 0, sizeof(double2) * na * n, st);
-    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "mixed Lanczos: T");
-    if ((e = run(true, F.X, na, yh)) != cudaSuccess) return cuda_fail(e, "mixed Lanczos: second pass");
+    if ((e = run(true, F.X, na, sel.y)) != cudaSuccess) return cuda_fail(e, "mixed Lanczos: second pass");
   }
   // FP64 Rayleigh quotient and residual of each Ritz vector
-  std::vector<double> rr;
-  if ((rc = F.rayleigh(S, st, n, na, rr)) != EDG_OK) return rc;
+  std::vector<double> rr(4 * (size_t)na);
+  if ((e = F.rayleigh_async(S, st, n, na, F.res)) != cudaSuccess) return cuda_fail(e, "mixed Lanczos: FP64 H*v");
+  cudaMemcpyAsync(rr.data(), F.res, sizeof(double) * 4 * na, cudaMemcpyDeviceToHost, st);
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "mixed Lanczos: residual");
   std::vector<int> keep;
   pick_levels(rr, th, acc_h, na, want, eigs, ritz, resid, keep);
   if (evecs) {

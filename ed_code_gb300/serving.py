@@ -115,6 +115,7 @@ class Server:
         self.batch = BatchSolver(tile_rows=tile_rows, lanes_per_row=lanes_per_row, check_every=check_every)
         self.peak_live = 0
         self.peak_bytes = 0
+        self.create_seconds = 0.0   # sector construction (basis and stored rows)
 
     def run(self, requests: Sequence[Request], clock: Callable[[], float] = time.perf_counter,
             on_result: Optional[Callable[[Served], None]] = None) -> List[Served]:
@@ -137,10 +138,12 @@ class Server:
                 if live and used + need > self.budget:
                     break
                 queue.pop(0)
+                tc = clock()
                 model = L.make_model(req.spec, req.Sz, req.kx, req.ky)
                 sec = GpuSector(model)
                 if not sec.build_targets():
                     raise MemoryError(f"request {req.rid}: stored rows do not fit")
+                self.create_seconds += clock() - tc
                 self.batch.add(sec, n_ev=req.n_ev, max_iterations=min(self.max_iterations, sec.n_p),
                                tol=self.res_tol, seed=1 + req.rid, tag=req.rid)
                 live[req.rid] = (req, sec, need, clock() - t0)

@@ -259,6 +259,10 @@ int edg_batch_step(edg_batch* b, int n_steps);
 /* Move up to cap finished results into out; *n_out receives how many. */
 int edg_batch_poll(edg_batch* b, edg_batch_result* out, int cap, int* n_out);
 int edg_batch_info(const edg_batch* b, int* n_active, int64_t* device_bytes, int64_t* steps);
+/* Host seconds spent so far, seconds[0..4]: adding segments, stepping (graph
+ * replays up to the waits of the convergence tests), finishing segments,
+ * releasing their memory, rebuilding the step graph. */
+int edg_batch_timers(const edg_batch* b, double* seconds);
 
 /* Deterministic complex test vector (splitmix64, entries uniform in [-1,1)^2)
  * written to device memory; the same generator as the test suite's. */
