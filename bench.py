@@ -413,7 +413,7 @@ def run_serve(args):
     for rid in sample:
         req = stream[int(rid)]
         t0 = time.perf_counter()
-        sec = GpuSector(L.make_model(req.spec, req.Sz, req.kx, req.ky))
+        sec = GpuSector(L.make_model(req.spec, req.Sz, req.kx, req.ky, bowties=False))
         sec.build_targets()
         eigs, _ = _plain(sec, max(req.n_ev, 4))
         plain_t.setdefault(req.n_sites, []).append(time.perf_counter() - t0)
@@ -459,10 +459,16 @@ def run_batch(args):
                 specs.append((spec, kx, ky))
     t0 = time.perf_counter()
     secs = []
+    t_model = t_create = 0.0
     for spec, kx, ky in specs:
-        sec = GpuSector(L.make_model(spec, 0, kx, ky))
+        ta = time.perf_counter()
+        model = L.make_model(spec, 0, kx, ky, bowties=False)
+        tb = time.perf_counter()
+        sec = GpuSector(model)
         assert sec.build_targets()
         secs.append(sec)
+        t_model += tb - ta
+        t_create += time.perf_counter() - tb
     torch.cuda.synchronize()
     t_build = time.perf_counter() - t0
     # autotune the tiles on a few steps of the whole batch
@@ -496,7 +502,8 @@ def run_batch(args):
     out = {"metric": "batched small-sector solves/s", "mode": "batch", "value": n / t_solve, "unit": "solves/s",
            "higher_is_better": True, "n_gpus": 1, "data": "synthetic", "sectors": n,
            "dims": [int(min(s.n_p for s in secs)), int(max(s.n_p for s in secs))],
-           "solve_seconds": t_solve, "build_seconds": t_build, "batch_timers": timers, "e2e_solves_per_s": n / (t_solve + t_build),
+           "solve_seconds": t_solve, "build_seconds": t_build, "batch_timers": timers,
+           "build_split": {"term_lists": t_model, "sector_and_rows": t_create}, "e2e_solves_per_s": n / (t_solve + t_build),
            "tiles": {"tile_rows": best[0], "lanes_per_row": best[1],
                      "ms_per_step": {f"{r}x{l}": round(1e3 * v, 3) for (r, l), v in sorted(trials.items())}},
            "max_rel_err_vs_plain_fp64": max(errs), "checked": len(errs),

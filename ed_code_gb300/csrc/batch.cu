@@ -239,7 +239,32 @@ __global__ void __launch_bounds__(kThreads) k_b_step(const SegDev* __restrict__ 
   }
 }
 
-// tile partials of <V_k|w> for k <= j; CTA (tile, y) takes k = y, y + kCgsY, ...
+// Sum v[0..2*kQ-1] over the CTA; thread 0 returns the sums in v.
+template <int kQ>
+__device__ __forceinline__ void block_sum_n(double* v) {
+  __shared__ double sm[kThreads / 32][2 * kQ];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < 2 * kQ; ++q)
+    for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_down_sync(0xffffffffu, v[q], o);
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < 2 * kQ; ++q) sm[wid][q] = v[q];
+  __syncthreads();
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int q = 0; q < 2 * kQ; ++q) {
+      double s = 0;
+      for (int w = 0; w < kThreads / 32; ++w) s += sm[w][q];
+      v[q] = s;
+    }
+  __syncthreads();
+}
+
+// tile partials of <V_k|w> for k <= j: CTA (tile, y) takes the groups of
+// kCgsQ consecutive k starting at kCgsQ*y, kCgsQ*(y + kCgsY), ..., reading
+// kCgsQ vectors per pass over its rows
+constexpr int kCgsQ = 4;
 __global__ void __launch_bounds__(kThreads) k_b_cgs_dot(const SegDev* __restrict__ segs,
                                                         const SegState* __restrict__ ss,
                                                         const TileDev* __restrict__ tiles, int n_tiles,
@@ -247,24 +272,34 @@ __global__ void __launch_bounds__(kThreads) k_b_cgs_dot(const SegDev* __restrict
   const TileDev t = tiles[blockIdx.x];
   const SegDev& S = segs[t.seg];
   const int K = ss[t.seg].status == kRunning ? ss[t.seg].j + 1 : 0;
-  for (int k = blockIdx.y; k < K; k += kCgsY) {  // K is the same for every thread of the CTA
-    const float2* vk = S.V + (int64_t)k * S.n;
-    FFAcc sr, si;
+  for (int k0 = blockIdx.y * kCgsQ; k0 < K; k0 += kCgsY * kCgsQ) {  // K is the same for the whole CTA
+    FFAcc sr[kCgsQ], si[kCgsQ];
     for (int r = threadIdx.x; r < t.rows; r += blockDim.x) {
       const int64_t i = t.row0 + r;
-      const float2 x = vk[i], y = S.w[i];
-      sr.add_prod(x.x, y.x);
-      sr.add_prod(x.y, y.y);
-      si.add_prod(x.x, y.y);
-      si.sub_prod(x.y, y.x);
+      const float2 y = S.w[i];
+#pragma unroll
+      for (int q = 0; q < kCgsQ; ++q)
+        if (k0 + q < K) {
+          const float2 x = S.V[(int64_t)(k0 + q) * S.n + i];
+          sr[q].add_prod(x.x, y.x);
+          sr[q].add_prod(x.y, y.y);
+          si[q].add_prod(x.x, y.y);
+          si[q].sub_prod(x.y, y.x);
+        }
     }
-    double a = sr.value(), b = si.value();
-    block_sum2(a, b);
-    if (threadIdx.x == 0) {
-      const int64_t o = ((int64_t)k * n_tiles + blockIdx.x) * 2;
-      part[o] = a;
-      part[o + 1] = b;
+    double v[2 * kCgsQ];
+#pragma unroll
+    for (int q = 0; q < kCgsQ; ++q) {
+      v[2 * q] = sr[q].value();
+      v[2 * q + 1] = si[q].value();
     }
+    block_sum_n<kCgsQ>(v);
+    if (threadIdx.x == 0)
+      for (int q = 0; q < kCgsQ && k0 + q < K; ++q) {
+        const int64_t o = ((int64_t)(k0 + q) * n_tiles + blockIdx.x) * 2;
+        part[o] = v[2 * q];
+        part[o + 1] = v[2 * q + 1];
+      }
   }
 }
 

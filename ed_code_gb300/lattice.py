@@ -279,7 +279,7 @@ def bowties_from_triangles(tris: Sequence[Triangle], adj: Sequence[Bond]) -> Lis
     return out
 
 
-def parse_input_text(text: str) -> Model:
+def parse_input_text(text: str, bowties: bool = True) -> Model:
     """Parse the reference input format into a :class:`Model`.
 
     Follows routine_parameters (read_input_file.cpp:59-108) and
@@ -330,7 +330,7 @@ def parse_input_text(text: str) -> Model:
             kw["Vector_File_Path"] = rest
     if len(T1) != len(T2):
         raise ValueError("ERROR: input T1 != T2")   # read_input_file.cpp:423-427
-    chch = bowties_from_triangles(tri_first, adj) if tri_first else []
+    chch = bowties_from_triangles(tri_first, adj) if (tri_first and bowties) else []
     return Model(
         n_sites=len(T1), T1=T1, T2=T2, adj_list=adj, ch_list=ch, chch_list=chch,
         Jz=vals["Jz"], J1=vals["J1"], J2=vals["J2"], Ch=vals["Ch"], ChCh=vals["ChCh"],
@@ -342,8 +342,10 @@ def parse_input_text(text: str) -> Model:
     )
 
 
-def make_model(spec: TorusSpec, Sz: float = 0.0, kx: int = 0, ky: int = 0, **kw) -> Model:
-    """Build the term lists for ``spec`` exactly as the reference parser would."""
-    m = parse_input_text(input_file_text(spec, Sz, kx, ky, **kw))
+def make_model(spec: TorusSpec, Sz: float = 0.0, kx: int = 0, ky: int = 0, bowties: bool = True, **kw) -> Model:
+    """Build the term lists for ``spec`` exactly as the reference parser would.
+    ``bowties=False`` leaves the ChCh bowtie list empty (it is O(triangles^2)
+    to build and unused when ChCh is 0)."""
+    m = parse_input_text(input_file_text(spec, Sz, kx, ky, **kw), bowties=bowties)
     m.lattice, m.Lx, m.Ly = spec.lattice, spec.Lx, spec.Ly
     return m

@@ -26,10 +26,11 @@ def _model_struct(model: Model):
         *[N.edg_bond(b.x, b.y, b.J, b.expphase.real, b.expphase.imag) for b in model.adj_list])
     tris = (N.edg_triangle * max(1, len(model.ch_list)))(
         *[N.edg_triangle(t.i, t.j, t.k, t.expphase.real, t.expphase.imag) for t in model.ch_list])
-    bows = (N.edg_bowtie * max(1, len(model.chch_list)))(
-        *[N.edg_bowtie(b.x, b.y, b.z, b.p, b.q, b.r) for b in model.chch_list])
+    # the library ignores the bowties when ChCh is 0, so they are not copied then
+    chch = model.chch_list if abs(model.ChCh) > 1e-16 else []
+    bows = (N.edg_bowtie * max(1, len(chch)))(*[N.edg_bowtie(b.x, b.y, b.z, b.p, b.q, b.r) for b in chch])
     m = N.edg_model(n, T1, T2, model.Jz, bonds, len(model.adj_list), model.Ch, tris, len(model.ch_list),
-                    model.ChCh, bows, len(model.chch_list))
+                    model.ChCh, bows, len(chch))
     return m, [T1, T2, bonds, tris, bows]
 
 

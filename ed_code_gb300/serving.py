@@ -139,7 +139,7 @@ class Server:
                     break
                 queue.pop(0)
                 tc = clock()
-                model = L.make_model(req.spec, req.Sz, req.kx, req.ky)
+                model = L.make_model(req.spec, req.Sz, req.kx, req.ky, bowties=req.spec.ChCh != 0)
                 sec = GpuSector(model)
                 if not sec.build_targets():
                     raise MemoryError(f"request {req.rid}: stored rows do not fit")
