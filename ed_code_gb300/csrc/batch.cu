@@ -17,7 +17,8 @@
 //                                   its own tiles in order: deterministic, and
 //                                   independent of the other segments)
 //   step    w -= alpha_j V_j + beta_j V_{j-1}
-//   cgs     w -= sum_k <V_k|w> V_k over k <= j, twice (FP64 coefficients)
+//   cgs     w -= sum_k <V_k|w> V_k over k <= j (FP64 coefficients); a second
+//           pass only when the first removed more than 1e-4 of |w|^2
 //   norm    beta_{j+1} = |w|
 //   scale   V_{j+1} = w / beta_{j+1};  j += 1
 //   check   every check_every steps: the wanted Ritz pairs of T_j (bisection
@@ -83,6 +84,7 @@ struct SegDev {
   double* beta;           // m_max + 2
   double* q;              // 2 (m_max + 1): reorthogonalisation coefficients
   double* ywork;          // want x 6 m_max: Ritz coefficients + inverse-iteration work
+  double* aux;            // [0]: |w|^2 before reorthogonalisation
   int64_t n;
   int m_max, want, check_every, pad;
   double tol;
@@ -91,6 +93,8 @@ struct SegDev {
 struct SegState {
   int j;       // steps taken
   int status;  // kRunning, kConverged, kMaxedOut
+  int redo;    // this step's second Gram-Schmidt pass is needed
+  int pad;
 };
 
 struct TileDev {
@@ -203,7 +207,7 @@ __global__ void __launch_bounds__(kThreads) k_b_dot(const SegDev* __restrict__ s
 }
 
 // one CTA per segment sums its tiles' partials in order:
-// mode 0 -> alpha_j, mode 1 -> beta_{j+1} = sqrt
+// mode 0 -> alpha_j, mode 1 -> beta_{j+1} = sqrt, mode 2 -> aux[0] = |w|^2
 __global__ void __launch_bounds__(kThreads) k_b_finish(const SegDev* __restrict__ segs,
                                                        const SegState* __restrict__ ss, const int* __restrict__ tb,
                                                        const double* __restrict__ part, int mode) {
@@ -218,7 +222,8 @@ __global__ void __launch_bounds__(kThreads) k_b_finish(const SegDev* __restrict_
   block_sum2(a, b);
   if (threadIdx.x == 0) {
     if (mode == 0) S.alpha[j] = a;
-    else S.beta[j + 1] = sqrt(a);
+    else if (mode == 1) S.beta[j + 1] = sqrt(a);
+    else S.aux[0] = a;
   }
 }
 
@@ -268,10 +273,11 @@ constexpr int kCgsQ = 4;
 __global__ void __launch_bounds__(kThreads) k_b_cgs_dot(const SegDev* __restrict__ segs,
                                                         const SegState* __restrict__ ss,
                                                         const TileDev* __restrict__ tiles, int n_tiles,
-                                                        double* __restrict__ part) {
+                                                        double* __restrict__ part, int pass) {
   const TileDev t = tiles[blockIdx.x];
   const SegDev& S = segs[t.seg];
-  const int K = ss[t.seg].status == kRunning ? ss[t.seg].j + 1 : 0;
+  const bool run = ss[t.seg].status == kRunning && (pass == 0 || ss[t.seg].redo);
+  const int K = run ? ss[t.seg].j + 1 : 0;
   for (int k0 = blockIdx.y * kCgsQ; k0 < K; k0 += kCgsY * kCgsQ) {  // K is the same for the whole CTA
     FFAcc sr[kCgsQ], si[kCgsQ];
     for (int r = threadIdx.x; r < t.rows; r += blockDim.x) {
@@ -307,8 +313,8 @@ __global__ void __launch_bounds__(kThreads) k_b_cgs_dot(const SegDev* __restrict
 __global__ void __launch_bounds__(kThreads) k_b_cgs_finish(const SegDev* __restrict__ segs,
                                                            const SegState* __restrict__ ss,
                                                            const int* __restrict__ tb, int n_tiles,
-                                                           const double* __restrict__ part) {
-  if (ss[blockIdx.x].status != kRunning) return;
+                                                           const double* __restrict__ part, int pass) {
+  if (ss[blockIdx.x].status != kRunning || (pass == 1 && !ss[blockIdx.x].redo)) return;
   const SegDev& S = segs[blockIdx.x];
   const int K = ss[blockIdx.x].j + 1;
   for (int k = blockIdx.y; k < K; k += kCgsY) {
@@ -327,9 +333,9 @@ __global__ void __launch_bounds__(kThreads) k_b_cgs_finish(const SegDev* __restr
 
 __global__ void __launch_bounds__(kThreads) k_b_cgs_sub(const SegDev* __restrict__ segs,
                                                         const SegState* __restrict__ ss,
-                                                        const TileDev* __restrict__ tiles) {
+                                                        const TileDev* __restrict__ tiles, int pass) {
   const TileDev t = tiles[blockIdx.x];
-  if (ss[t.seg].status != kRunning) return;
+  if (ss[t.seg].status != kRunning || (pass == 1 && !ss[t.seg].redo)) return;
   const SegDev& S = segs[t.seg];
   __shared__ float sq[2 * (kMaxSteps + 1)];
   const int K = ss[t.seg].j + 1;
@@ -363,6 +369,21 @@ __global__ void __launch_bounds__(kThreads) k_b_scale(const SegDev* __restrict__
     const float2 y = S.w[i];
     vn[i] = make_float2(fmaf(y.x, s.l, __fmul_rn(y.x, s.h)), fmaf(y.y, s.l, __fmul_rn(y.y, s.h)));
   }
+}
+
+// Whether the second Gram-Schmidt pass is needed (Daniel, Gragg, Kaufman and
+// Stewart's test): the first pass removed sum |q_k|^2 from |w|^2; when that
+// is below 1e-4 |w|^2 (the norm changed by less than 0.005%) w is already
+// orthogonal to the working precision and the second pass is skipped.
+__global__ void __launch_bounds__(kThreads) k_b_cgs_decide(const SegDev* __restrict__ segs,
+                                                           SegState* __restrict__ ss) {
+  if (ss[blockIdx.x].status != kRunning) return;
+  const SegDev& S = segs[blockIdx.x];
+  const int K = ss[blockIdx.x].j + 1;
+  double a = 0, b = 0;
+  for (int k = threadIdx.x; k < K; k += blockDim.x) a += S.q[2 * k] * S.q[2 * k] + S.q[2 * k + 1] * S.q[2 * k + 1];
+  block_sum2(a, b);
+  if (threadIdx.x == 0) ss[blockIdx.x].redo = a > 1e-4 * S.aux[0] ? 1 : 0;
 }
 
 __global__ void k_b_advance(const SegDev* __restrict__ segs, SegState* __restrict__ ss, int n_seg) {
@@ -421,7 +442,7 @@ struct Segment {
 };
 
 void release(Segment& g) {
-  void* p[] = {g.d.V, g.d.w, g.d.u, g.d.alpha, g.d.beta, g.d.q, g.d.ywork};
+  void* p[] = {g.d.V, g.d.w, g.d.u, g.d.alpha, g.d.beta, g.d.q, g.d.ywork, g.d.aux};
   for (void* x : p)
     if (x) cudaFree(x);
   g.d = SegDev{};
@@ -652,10 +673,13 @@ int rebuild(Batch& B) {
   k_b_dot<<<nt, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles, B.d_part, 0);
   k_b_finish<<<ns, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tb, B.d_part, 0);
   k_b_step<<<nt, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles);
+  k_b_dot<<<nt, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles, B.d_part, 1);
+  k_b_finish<<<ns, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tb, B.d_part, 2);
   for (int pass = 0; pass < 2; ++pass) {
-    k_b_cgs_dot<<<dim3(nt, kCgsY), kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles, nt, B.d_part);
-    k_b_cgs_finish<<<dim3(ns, kCgsY), kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tb, nt, B.d_part);
-    k_b_cgs_sub<<<nt, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles);
+    k_b_cgs_dot<<<dim3(nt, kCgsY), kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles, nt, B.d_part, pass);
+    k_b_cgs_finish<<<dim3(ns, kCgsY), kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tb, nt, B.d_part, pass);
+    k_b_cgs_sub<<<nt, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles, pass);
+    if (pass == 0) k_b_cgs_decide<<<ns, kThreads, 0, B.st>>>(B.d_segs, B.d_state);
   }
   k_b_dot<<<nt, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles, B.d_part, 1);
   k_b_finish<<<ns, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tb, B.d_part, 1);
@@ -761,6 +785,7 @@ int edg_batch_add(edg_batch* bh, edg_sector* sec, const edg_batch_request* req) 
   if (e == cudaSuccess) e = cudaMalloc(&d.beta, sizeof(double) * (m + 2));
   if (e == cudaSuccess) e = cudaMalloc(&d.q, sizeof(double) * 2 * (m + 1));
   if (e == cudaSuccess) e = cudaMalloc(&d.ywork, sizeof(double) * 6 * (size_t)d.want * m);
+  if (e == cudaSuccess) e = cudaMalloc(&d.aux, sizeof(double) * 2);
   if (e != cudaSuccess) {
     cudaGetLastError();
     release(g);
