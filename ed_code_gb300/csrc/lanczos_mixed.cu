@@ -171,19 +171,43 @@ __global__ void k_sub32(float2* __restrict__ y, const float2* __restrict__ V, in
   }
 }
 
-// X_e += c[e][j] * v (FP64 accumulators, E Ritz vectors)
-__global__ void k_accumulate(double2* __restrict__ X, int64_t ldx, const float2* __restrict__ v,
-                             const double* __restrict__ c, int E, int64_t n) {
-  extern __shared__ double sc[];
-  for (int e = threadIdx.x; e < E; e += blockDim.x) sc[e] = c[e];
+// Second pass of the resident-vector mode: X_e += sum_t y[e*m + j0 + t] V_{j0+t}
+// over a window of cnt <= kRing vectors still resident in the ring, so each
+// FP64 Ritz vector is read and written once per window instead of once per
+// step.  The window sum is float-float; the add to X is FP64.
+constexpr int kRing = 8;
+struct RingPtrs {
+  const float2* v[kRing];
+};
+__global__ void __launch_bounds__(256) k_ritz_window(double2* __restrict__ X, int64_t n, RingPtrs ring, int cnt,
+                                                     const double* __restrict__ y, int m, int j0, int E) {
+  __shared__ float2 sc[kMaxEv * kRing];  // (head, tail) of y[e*m + j0 + t] at e*kRing + t
+  for (int k = threadIdx.x; k < E * cnt; k += blockDim.x) {
+    const int e = k / cnt, t = k % cnt;
+    const FFScalar c(y[(int64_t)e * m + j0 + t]);
+    sc[e * kRing + t] = make_float2(c.h, c.l);
+  }
   __syncthreads();
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const float2 vv = v[i];
+    float2 v[kRing];
+#pragma unroll
+    for (int t = 0; t < kRing; ++t)
+      if (t < cnt) v[t] = ring.v[t][i];
     for (int e = 0; e < E; ++e) {
-      double2 x = X[(int64_t)e * ldx + i];
-      x.x += sc[e] * vv.x;
-      x.y += sc[e] * vv.y;
-      X[(int64_t)e * ldx + i] = x;
+      FFAcc ar, ai;
+#pragma unroll
+      for (int t = 0; t < kRing; ++t)
+        if (t < cnt) {
+          const float2 c = sc[e * kRing + t];
+          ar.add_prod(c.x, v[t].x);
+          ar.lo = fmaf(c.y, v[t].x, ar.lo);
+          ai.add_prod(c.x, v[t].y);
+          ai.lo = fmaf(c.y, v[t].y, ai.lo);
+        }
+      double2 x = X[(int64_t)e * n + i];
+      x.x += ar.value();
+      x.y += ai.value();
+      X[(int64_t)e * n + i] = x;
     }
   }
 }
@@ -222,31 +246,37 @@ __global__ void __launch_bounds__(kRedThreads) k_rq_partial(const double2* __res
   }
 }
 
-// X_q = sum_j y[q*m + j] V_j for q in [q0, q0 + qn), qn <= kRitzChunk, in FP64:
-// each V_j is read once per chunk of Ritz vectors.
+// X_q = sum_j y[q*m + j] V_j for q in [q0, q0 + qn), qn <= kRitzChunk: each
+// V_j is read once per chunk of Ritz vectors.  The coefficients are split into
+// FP32 heads and tails and the sums kept in float-float (ff.cuh), written out
+// in FP64.
 constexpr int kRitzChunk = 8;
 __global__ void __launch_bounds__(256) k_ritz_vectors(double2* __restrict__ X, int64_t n,
                                                       const float2* __restrict__ V, int64_t ldv,
                                                       const double* __restrict__ y, int m, int q0, int qn) {
-  extern __shared__ double sy[];  // qn * m
-  for (int k = threadIdx.x; k < qn * m; k += blockDim.x) sy[k] = y[(int64_t)q0 * m + k];
+  extern __shared__ float2 sy2[];  // qn * m (head, tail)
+  for (int k = threadIdx.x; k < qn * m; k += blockDim.x) {
+    const FFScalar c(y[(int64_t)q0 * m + k]);
+    sy2[k] = make_float2(c.h, c.l);
+  }
   __syncthreads();
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    double ar[kRitzChunk], ai[kRitzChunk];
-#pragma unroll
-    for (int q = 0; q < kRitzChunk; ++q) ar[q] = ai[q] = 0.0;
+    FFAcc ar[kRitzChunk], ai[kRitzChunk];
     for (int j = 0; j < m; ++j) {
       const float2 v = V[(int64_t)j * ldv + i];
 #pragma unroll
       for (int q = 0; q < kRitzChunk; ++q)
         if (q < qn) {
-          ar[q] += sy[q * m + j] * v.x;
-          ai[q] += sy[q * m + j] * v.y;
+          const float2 c = sy2[q * m + j];
+          ar[q].add_prod(c.x, v.x);
+          ar[q].lo = fmaf(c.y, v.x, ar[q].lo);
+          ai[q].add_prod(c.x, v.y);
+          ai[q].lo = fmaf(c.y, v.y, ai[q].lo);
         }
     }
 #pragma unroll
     for (int q = 0; q < kRitzChunk; ++q)
-      if (q < qn) X[(int64_t)(q0 + q) * n + i] = make_double2(ar[q], ai[q]);
+      if (q < qn) X[(int64_t)(q0 + q) * n + i] = make_double2(ar[q].value(), ai[q].value());
   }
 }
 
@@ -332,7 +362,7 @@ cudaError_t MixedFinish::reserve_x(int64_t n, int na) {
 int MixedFinish::ritz_stored(cudaStream_t st, const float2* V, int64_t n, int m, int na) {
   for (int q0 = 0; q0 < na; q0 += kRitzChunk) {
     const int qn = std::min(kRitzChunk, na - q0);
-    k_ritz_vectors<<<grid_n(n), 256, sizeof(double) * qn * m, st>>>(X, n, V, n, y, m, q0, qn);
+    k_ritz_vectors<<<grid_n(n), 256, sizeof(float2) * qn * m, st>>>(X, n, V, n, y, m, q0, qn);
   }
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? EDG_OK : cuda_fail(e, "mixed Lanczos: Ritz vectors");
@@ -381,7 +411,8 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
   using clk = std::chrono::steady_clock;
   const auto t_start = clk::now();
   Dev D;
-  float2 *V = nullptr, *w = nullptr, *buf[3] = {nullptr, nullptr, nullptr};
+  float2 *V = nullptr, *w = nullptr, *buf[kRing] = {};
+  int ring = 3;  // resident vectors without storage: the recurrence needs 3
   double *alpha, *beta, *part, *scal, *lq;
   cudaError_t e = cudaSuccess;
   if (store) {
@@ -390,6 +421,15 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
   } else {
     for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = D.alloc(&buf[k], (size_t)n);
     if (e != cudaSuccess) return fail(EDG_ERR_NOMEM, "mixed Lanczos: vectors do not fit");
+    // up to kRing - 3 more when they fit with room to spare: the second pass
+    // then adds them to the Ritz vectors a window at a time
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    const size_t vb = sizeof(float2) * (size_t)n;
+    while (ring < kRing && free_b > vb * (size_t)(kRing - ring + 8) &&
+           D.alloc(&buf[ring], (size_t)n) == cudaSuccess)
+      ++ring;
+    cudaGetLastError();
   }
   if ((e = D.alloc(&w, (size_t)n)) != cudaSuccess) return fail(EDG_ERR_NOMEM, "mixed Lanczos: w");
   const int64_t kparts = (int64_t)std::max(m + 1, 4) * kRedBlocks * 2;
@@ -399,27 +439,30 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
     return fail(EDG_ERR_NOMEM, "mixed Lanczos: scratch");
   cudaMemsetAsync(beta, 0, sizeof(double) * (m + 2), st);
 
-  auto vec = [&](int j) -> float2* { return store ? V + (int64_t)j * n : buf[j % 3]; };
+  auto vec = [&](int j) -> float2* { return store ? V + (int64_t)j * n : buf[j % ring]; };
   auto norm_into = [&](const float2* x, double* dst) {  // dst = |x| in FP64
     k_dot32<<<dim3(kRedBlocks, 1), kRedThreads, 0, st>>>(x, 0, x, n, part);
     k_finish<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, dst, 2);
   };
   double t_hv = 0;
   int64_t hv_calls = 0;
-  // one Lanczos pass; with acc_X non-null the Ritz vectors are accumulated
-  // instead of alpha/beta being computed (second pass, same recurrence)
-  auto run = [&](bool second, double2* X, int E, const std::vector<double>& yh) -> cudaError_t {
+  // one Lanczos pass; in the second pass (same recurrence, same alpha/beta)
+  // the Ritz vectors X are accumulated from the device coefficients yd
+  auto run = [&](bool second, double2* X, int E, const double* yd) -> cudaError_t {
     cudaError_t ce = edg_fill_random(w, n, EDG_C64, o.seed, st) == EDG_OK ? cudaSuccess : cudaErrorUnknown;
     if (ce != cudaSuccess) return ce;
     norm_into(w, scal);                                     // |v0 unnormalised|
     k_scale_inv<<<grid_n(n), 256, 0, st>>>(vec(0), w, scal, n);
+    const int win = std::max(1, ring - 2);  // vectors V_j0..V_j still resident at step j
+    int acc_from = 0;
     for (int j = 0; j < m; ++j) {
       if (second) {
-        std::vector<double> c(E);
-        for (int q = 0; q < E; ++q) c[q] = yh[(size_t)q * m + j];
-        cudaMemcpyAsync(scal, c.data(), sizeof(double) * E, cudaMemcpyHostToDevice, st);
-        k_accumulate<<<grid_n(n), 256, sizeof(double) * E, st>>>(X, n, vec(j), scal, E, n);
-        if ((ce = cudaStreamSynchronize(st)) != cudaSuccess) return ce;  // c must outlive the copy
+        if (j - acc_from + 1 == win || j + 1 == m) {
+          RingPtrs rp{};
+          for (int t = 0; t <= j - acc_from; ++t) rp.v[t] = vec(acc_from + t);
+          k_ritz_window<<<grid_n(n), 256, 0, st>>>(X, n, rp, j - acc_from + 1, yd, m, acc_from, E);
+          acc_from = j + 1;
+        }
         if (j + 1 == m) break;
       }
       auto t0 = clk::now();
@@ -473,7 +516,7 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
     }
     return cudaStreamSynchronize(st);
   };
-  if ((e = run(false, nullptr, 0, {})) != cudaSuccess) return cuda_fail(e, "mixed Lanczos");
+  if ((e = run(false, nullptr, 0, nullptr)) != cudaSuccess) return cuda_fail(e, "mixed Lanczos");
   // Ritz values and coefficients of T on the host
   MixedFinish F;
   const int n_try = std::min(kMaxEv, std::min(want + 4, m));
@@ -498,7 +541,7 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
   } else {
     passes = 2;
     cudaMemsetAsync(F.X, 0, sizeof(double2) * na * n, st);
-    if ((e = run(true, F.X, na, sel.y)) != cudaSuccess) return cuda_fail(e, "mixed Lanczos: second pass");
+    if ((e = run(true, F.X, na, F.y)) != cudaSuccess) return cuda_fail(e, "mixed Lanczos: second pass");
   }
   // FP64 Rayleigh quotient and residual of each Ritz vector
   std::vector<double> rr(4 * (size_t)na);

@@ -32,9 +32,12 @@ def test_mixed_matches_reference(gpu, name, n_ev, reorth):
     assert out["stats"]["passes"] == (1 if reorth else 2)
 
 
-def test_mixed_eigenvectors(gpu):
+@pytest.mark.parametrize("reorth", [1, 0])
+def test_mixed_eigenvectors(gpu, reorth):
+    """Stored vectors (reorth 1) or the second pass over resident vectors (0)."""
     sec = gpu.GpuSector(golden_model("tri6x4_k10", 0))
-    out = sec.solve_mixed(n_ev=2, iterations=250, reorth_every=1, want_vectors=True)
+    out = sec.solve_mixed(n_ev=2, iterations=250, reorth_every=reorth, want_vectors=True)
+    assert out["stats"]["passes"] == (1 if reorth else 2)
     X = out["evecs"]
     for k in range(len(out["eigs"])):
         assert abs(np.vdot(X[k], X[k]).real - 1.0) < 1e-12
