@@ -247,7 +247,7 @@ def run_device(args, world, rank, local_rank):
     # stored targets: the search done once, its results streamed every H*v
     mode = "matrix-free"
     t_tgt = None
-    lpr, tune_ms = None, None
+    lpr, tune_ms, t_pack = None, None, None
     if not args.matrix_free:
         t0 = time.perf_counter()
         if sec.build_targets():
@@ -261,6 +261,14 @@ def run_device(args, world, rank, local_rank):
                 lpr = lanes
             else:
                 lpr, tune_ms = sec.tune(0)
+            # column panels on request (measured slower than the tuned row
+            # kernel at 32 and 36 sites)
+            if args.panels > 0:
+                t0 = time.perf_counter()
+                sec.pack_panels(max(args.panels, 0))
+                torch.cuda.synchronize()
+                t_pack = time.perf_counter() - t0
+                mode = "panels"
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
             sec.hv(v, w, stream)
@@ -336,6 +344,8 @@ def run_device(args, world, rank, local_rank):
                    "stored_row_bytes": 6 * sec.info.get("n_targets", 0) + 16 * sec.n_p,
                    "matrix_free_ms_per_step": mf_ms,
                    "lanes_per_row": lpr, "cache_policy": sec.info.get("cache_policy"),
+                   "panels": sec.info.get("panels"), "panel_pack_seconds": None if t_pack is None else round(t_pack, 3),
+                   "row_kernel_ms": None if tune_ms is None else round(float(min(x for x in tune_ms if x > 0)), 3),
                    "tune_ms_lpr_8_16_32": None if tune_ms is None else [round(float(x), 3) for x in tune_ms],
                    "matrix_free_GBps": B_mf / (mf_ms / 1e3) / 1e9,
                    "l2": "inputs larger than L2 (no flush needed)", "orbit_search": "torus" if sec.info["torus"] else "walk"},
@@ -344,8 +354,9 @@ def run_device(args, world, rank, local_rank):
         "cpu_baseline": cpu,
         "e2e": e2e,
         "clocks": clocks,
-        # one H*v kernel per step; the stored-target path adds the u = v/norm pass
-        "gpu_launches": args.steps * (2 if mode == "stored-rows" else 1),
+        # per step: the u = v/norm pass plus one row kernel, or one launch per
+        # panel; the matrix-free kernel is one launch
+        "gpu_launches": args.steps * ({"stored-rows": 2, "panels": 1 + (sec.info.get("panels") or 0)}.get(mode, 1)),
     }
     if rank == 0:
         print(json.dumps(out), flush=True)
@@ -597,6 +608,8 @@ def main():
     ap.add_argument("--matrix-free", action="store_true", help="do not store the searched targets")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--rows", default=None, help="LANES,POLICY: fix the stored-row kernel instead of timing it")
+    ap.add_argument("--panels", type=int, default=0,
+                    help="regroup the stored rows into this many column panels (0: keep the row kernel)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-step-seconds", type=float, default=4.0)
     ap.add_argument("--mode", choices=["hv", "serve", "batch", "precision", "solve36"], default="hv",

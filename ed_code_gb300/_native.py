@@ -54,7 +54,7 @@ class edg_sector_info(C.Structure):
         ("n_sites", C.c_int), ("n_ones", C.c_int), ("L1", C.c_int), ("L2", C.c_int), ("kx", C.c_int),
         ("ky", C.c_int), ("torus", C.c_int), ("n_groups", C.c_int), ("n_p", C.c_int64), ("n_configs", C.c_int64),
         ("device_bytes", C.c_int64), ("n_targets", C.c_int64), ("lanes_per_row", C.c_int),
-        ("cache_policy", C.c_int),
+        ("cache_policy", C.c_int), ("panels", C.c_int),
     ]
 
 
@@ -113,6 +113,7 @@ SIGNATURES = {
     "edg_hv": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "edg_hv_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
     "edg_sector_set_rows": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "edg_sector_pack_panels": (C.c_int, [C.c_void_p, C.c_int]),
     "edg_batch_create": (C.c_int, [C.POINTER(edg_batch_opts), C.POINTER(C.c_void_p)]),
     "edg_batch_destroy": (C.c_int, [C.c_void_p]),
     "edg_batch_footprint": (C.c_int, [C.c_void_p, C.POINTER(edg_batch_request), C.POINTER(C.c_int64)]),

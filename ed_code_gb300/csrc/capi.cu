@@ -487,6 +487,7 @@ int edg_sector_get_info(const edg_sector* s, edg_sector_info* info) {
   info->n_targets = P.n_targets;
   info->lanes_per_row = s->s.col ? s->s.csr_lpr : 0;
   info->cache_policy = s->s.col ? s->s.csr_pol : 0;
+  info->panels = s->s.pan_p;
   return EDG_OK;
 }
 
@@ -637,6 +638,14 @@ int edg_sector_tune(edg_sector* s, int lanes_per_row, int* chosen, double* ms) {
   if (!s) return fail(EDG_ERR_INVALID, "NULL sector");
   const int rc = tune_rows(s->s, lanes_per_row, chosen, ms);
   if (rc != EDG_OK) return fail(rc, "tuning the stored-row kernel failed");
+  return EDG_OK;
+}
+
+int edg_sector_pack_panels(edg_sector* s, int n_panels) {
+  if (!s) return fail(EDG_ERR_INVALID, "NULL sector");
+  std::string err;
+  const int rc = pack_panels(s->s, n_panels, err);
+  if (rc != EDG_OK) return fail(rc, err);
   return EDG_OK;
 }
 

@@ -99,6 +99,14 @@ struct Sector {
   size_t targets_bytes = 0;
   int csr_lpr = 16;             // lanes per CSR row (8, 16 or 32): edg_sector_tune
   int csr_pol = 1;              // cache policy of the CSR loads (1 or 2): edg_sector_tune
+  // column panels (edg_sector_pack_panels): the stored rows regrouped so that
+  // one H*v launch per panel gathers from one L2-sized slice of u
+  uint32_t* pan_ent = nullptr;  // (column - p*pan_c) | local row << 23
+  uint16_t* pan_vid = nullptr;
+  uint64_t* pan_off = nullptr;  // pan_p * pan_nb + 1 segment offsets, panel-major
+  int pan_p = 0;                // panels
+  int64_t pan_c = 0;            // columns per panel (< 2^23)
+  int64_t pan_nb = 0;           // row blocks of kPanRows rows
 };
 
 // basis.cu
@@ -139,6 +147,7 @@ cudaError_t count_offdiag(const Sector& S, unsigned long long* nnz_dev, cudaStre
 int build_targets(Sector& S, int64_t max_bytes, std::string& err);
 void free_targets(Sector& S);
 cudaError_t launch_hv_stored(const Sector& S, const void* v, void* w, bool fp64, cudaStream_t st);
+int pack_panels(Sector& S, int n_panels, std::string& err);
 int tune_rows(Sector& S, int lpr, int* chosen, double* ms_out);
 int hv_grid_blocks(bool fp64, bool torus, bool chch);
 

@@ -17,7 +17,7 @@
 extern "C" {
 #endif
 
-#define EDGPU_ABI_VERSION 2
+#define EDGPU_ABI_VERSION 3
 
 enum {
   EDG_OK = 0,
@@ -67,6 +67,7 @@ typedef struct {
   int64_t n_targets;     /* stored nonzeros (0: H*v searches on the fly) */
   int lanes_per_row;     /* stored-row H*v: lanes of a warp per row (edg_sector_tune) */
   int cache_policy;      /* stored-row H*v: 1 streaming row loads, 2 L2 evict-first row loads */
+  int panels;            /* column panels of the stored rows (0: row order) */
 } edg_sector_info;
 
 const char* edg_last_error(void);
@@ -126,6 +127,17 @@ int edg_sector_tune(edg_sector* s, int lanes_per_row, int* chosen, double* ms);
 /* Set both choices without timing: lanes_per_row 8, 16 or 32, cache_policy 1
  * or 2.  Results do not depend on either; only the speed does. */
 int edg_sector_set_rows(edg_sector* s, int lanes_per_row, int cache_policy);
+
+/* Regroup the stored rows into column panels: rows in blocks of 64, columns
+ * in n_panels slices (<= 0: enough for each slice of u to fit in 64 MB of L2
+ * at complex64), entries stored per (block, panel), in row order.  edg_hv
+ * then makes one pass per panel, gathering from one L2-resident slice of u
+ * and adding the row sums into w.  Same bytes per nonzero as the rows; the
+ * row arrays are freed.  Measured slower than the tuned row kernel at 32 and
+ * 36 sites (a panel holds ~2 entries per row, so the per-entry segmented
+ * reduction and the per-panel pass over w outweigh the L2 hits); kept as an
+ * option.  Batch segments and edg_hv_noalloc need the row form. */
+int edg_sector_pack_panels(edg_sector* s, int n_panels);
 
 /* Same with host buffers: copies v in, applies H, copies w out, synchronises.
  * This is the call the reference's sHv(v, w, ...) adapter makes. */

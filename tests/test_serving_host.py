@@ -35,3 +35,22 @@ def test_footprint_estimate_grows_with_size_and_steps():
     # at least the FP32 Krylov vectors of 300 steps
     assert serving.estimate_bytes(big, 300) > n_p * 8 * 300
     assert serving.estimate_bytes(r, 300) > 0
+
+
+def test_sweep_sort_matches_the_reference_rules():
+    from ed_code_gb300 import sweep as W
+
+    mk = lambda i, E, Sz: W.Level(i, E, 0.0, 0.0, Sz, 0, 0)
+    lv = [mk(0, -1.0, 1.0), mk(1, -2.0, 0.0), mk(2, -1.0, 0.0), mk(3, -1.0 + 4e-16, 2.0), mk(4, -1.0 + 4e-16, 0.5),
+          mk(5, -3.0, 3.0)]
+    out = W.sort_levels(lv)
+    assert [q.id for q in out][:2] == [5, 1]
+    assert all(a.En <= b.En + 1e-15 for a, b in zip(out, out[1:]))
+    # within 1e-15 of each other the lowest Sz comes first
+    tied = out[2:]
+    assert tied[0].Sz == 0.0
+    assert W.sector_list(W.L.TorusSpec("square", 4, 2))[:3] == [(4, 0, 0), (4, 0, 1), (4, 1, 0)]
+    assert {s[0] for s in W.sector_list(W.L.TorusSpec("square", 4, 2))} == set(range(4, 9))
+    assert {s[0] for s in W.sector_list(W.L.TorusSpec("square", 4, 2), Sz=1.0)} == {5}
+    txt = W.table(out, 8, 1.0, 0.0)
+    assert "ID\tEnergies\tEnergies/site\tSz\tpx\tpy\tJz\tJ2\tEnergies-E0" in txt
