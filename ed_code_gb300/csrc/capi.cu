@@ -42,6 +42,9 @@ static void free_sector(Sector& S) {
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (S.stream) cudaStreamDestroy(S.stream);
+  if (S.copy_stream) cudaStreamDestroy(S.copy_stream);
+  for (cudaEvent_t ev : S.chunk_done)
+    if (ev) cudaEventDestroy(ev);
   S = Sector{};
 }
 
@@ -596,8 +599,30 @@ int edg_hv_host(edg_sector* s, const void* v, void* w, int dtype) {
   if (e == cudaSuccess) e = ensure(S.host_out, bytes);
   if (e != cudaSuccess) return cuda_fail(e, "hv_host buffers");
   e = cudaMemcpyAsync(S.host_in.ptr, v, bytes, cudaMemcpyHostToDevice, S.stream);
-  if (e == cudaSuccess) e = launch_hv(S, S.host_in.ptr, S.host_out.ptr, dtype == EDG_C128, S.stream);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(w, S.host_out.ptr, bytes, cudaMemcpyDeviceToHost, S.stream);
+  const bool fp64 = dtype == EDG_C128;
+  const int64_t n = S.P.n_p;
+  constexpr int kChunks = 8;
+  if (S.col && n >= (1 << 20)) {
+    // rows in row order: the w rows of chunk c go back to the host while the
+    // rows of chunk c + 1 are computed
+    if (!S.copy_stream && e == cudaSuccess) e = cudaStreamCreateWithFlags(&S.copy_stream, cudaStreamNonBlocking);
+    for (int c = 0; c < kChunks && e == cudaSuccess; ++c)
+      if (!S.chunk_done[c]) e = cudaEventCreateWithFlags(&S.chunk_done[c], cudaEventDisableTiming);
+    const size_t elem = fp64 ? 16 : 8;
+    for (int c = 0; c < kChunks && e == cudaSuccess; ++c) {
+      const int64_t r0 = n * c / kChunks, r1 = n * (c + 1) / kChunks;
+      e = launch_hv_rows(S, S.host_in.ptr, S.host_out.ptr, fp64, r0, r1, c == 0, S.stream);
+      if (e == cudaSuccess) e = cudaEventRecord(S.chunk_done[c], S.stream);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(S.copy_stream, S.chunk_done[c], 0);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(static_cast<char*>(w) + r0 * elem, static_cast<char*>(S.host_out.ptr) + r0 * elem,
+                            (size_t)(r1 - r0) * elem, cudaMemcpyDeviceToHost, S.copy_stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(S.copy_stream);
+  } else {
+    if (e == cudaSuccess) e = launch_hv(S, S.host_in.ptr, S.host_out.ptr, fp64, S.stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(w, S.host_out.ptr, bytes, cudaMemcpyDeviceToHost, S.stream);
+  }
   if (e == cudaSuccess) e = cudaStreamSynchronize(S.stream);
   if (e != cudaSuccess) return cuda_fail(e, "hv_host");
   return EDG_OK;

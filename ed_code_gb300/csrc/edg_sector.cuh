@@ -79,6 +79,10 @@ struct Sector {
   // scratch kept for host-buffer H*v calls
   DeviceBuffer host_in, host_out;
   cudaStream_t stream = nullptr;
+  // edg_hv_host: a second stream and per-chunk events to copy finished rows
+  // of w back while the next rows are computed
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t chunk_done[8] = {};
   // Lanczos work area (allocated on first use)
   DeviceBuffer lz_work;
   // torus plan (null when the sector does not qualify)
@@ -148,6 +152,9 @@ int build_targets(Sector& S, int64_t max_bytes, std::string& err);
 void free_targets(Sector& S);
 cudaError_t launch_hv_stored(const Sector& S, const void* v, void* w, bool fp64, cudaStream_t st);
 int pack_panels(Sector& S, int n_panels, std::string& err);
+// stored rows in row order: rows [r0, r1) of H*v, with the u = v/norm pass first when with_u
+cudaError_t launch_hv_rows(const Sector& S, const void* v, void* w, bool fp64, int64_t r0, int64_t r1, bool with_u,
+                           cudaStream_t st);
 int tune_rows(Sector& S, int lpr, int* chosen, double* ms_out);
 int hv_grid_blocks(bool fp64, bool torus, bool chch);
 

@@ -343,10 +343,11 @@ __global__ void __launch_bounds__(kTgtThreads) k_hv_csr(const uint64_t* __restri
                                                         const typename CT2<Real>::T* __restrict__ vtab, int n_vals,
                                                         const double* __restrict__ ezz,
                                                         const uint8_t* __restrict__ lid,
-                                                        const double* __restrict__ nrm_tab, int64_t n_p,
-                                                        const typename CT2<Real>::T* __restrict__ v,
+                                                        const double* __restrict__ nrm_tab, int64_t row0,
+                                                        int64_t n_p, const typename CT2<Real>::T* __restrict__ v,
                                                         const typename CT2<Real>::T* __restrict__ u,
                                                         typename CT2<Real>::T* __restrict__ w) {
+  // rows [row0, n_p)
   using CT = typename CT2<Real>::T;
   constexpr int kRows = 32 / LPR;  // rows per warp
   extern __shared__ __align__(16) uint8_t sm[];
@@ -360,13 +361,13 @@ __global__ void __launch_bounds__(kTgtThreads) k_hv_csr(const uint64_t* __restri
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const unsigned long long* rp = reinterpret_cast<const unsigned long long*>(row_ptr);
-  int64_t i = warp * kRows + sub;
+  int64_t i = row0 + warp * kRows + sub;
   uint64_t beg = 0, end = 0;
   if (i < n_p) {
     beg = __ldg(rp + i);
     end = __ldg(rp + i + 1);
   }
-  for (int64_t base = warp * kRows; base < n_p; base += n_warps * kRows) {
+  for (int64_t base = row0 + warp * kRows; base < n_p; base += n_warps * kRows) {
     const int64_t inext = i + n_warps * kRows;
     uint64_t nbeg = 0, nend = 0;
     if (inext < n_p) {
@@ -408,43 +409,51 @@ const double* params_field(const Sector& S, size_t offset) {
   return reinterpret_cast<const double*>(reinterpret_cast<const char*>(S.dP) + offset);
 }
 
+// rows [r0, r1); u = v / norm first when with_u
 template <typename Real, int LPR, int kPol>
-cudaError_t launch_csr_lpr(const Sector& S, const void* v, void* w, cudaStream_t st) {
+cudaError_t launch_csr_lpr(const Sector& S, const void* v, void* w, cudaStream_t st, int64_t r0, int64_t r1,
+                           bool with_u) {
   using CT = typename CT2<Real>::T;
   const int64_t n = S.P.n_p;
-  k_u_scale<Real><<<(int)std::min<int64_t>((n + 255) / 256, 152 * 32), 256, 0, st>>>(
-      reinterpret_cast<const CT*>(v), S.lid, params_field(S, offsetof(SectorParams, nrm_inv)), n,
-      reinterpret_cast<CT*>(S.ubuf.ptr));
+  if (with_u)
+    k_u_scale<Real><<<(int)std::min<int64_t>((n + 255) / 256, 152 * 32), 256, 0, st>>>(
+        reinterpret_cast<const CT*>(v), S.lid, params_field(S, offsetof(SectorParams, nrm_inv)), n,
+        reinterpret_cast<CT*>(S.ubuf.ptr));
   const CT* tab = reinterpret_cast<const CT*>(sizeof(Real) == 8 ? (const void*)S.vtab64 : (const void*)S.vtab32);
   const size_t tab_bytes = sizeof(CT) * S.n_vals;
   const double* nrm = params_field(S, offsetof(SectorParams, nrm));
-  const int64_t threads_needed = (n * LPR + 31) / 32 * 32;
+  if (r1 <= r0) return cudaGetLastError();
+  const int64_t threads_needed = ((r1 - r0) * LPR + 31) / 32 * 32;
   if (tab_bytes <= 96 * 1024) {
     auto kern = k_hv_csr<Real, LPR, true, kPol>;
     kern<<<grid_for(kern, tab_bytes, threads_needed, kTgtThreads), kTgtThreads, tab_bytes, st>>>(
-        S.row_ptr, S.col, S.vid, tab, S.n_vals, S.ezz, S.lid, nrm, n, reinterpret_cast<const CT*>(v),
+        S.row_ptr, S.col, S.vid, tab, S.n_vals, S.ezz, S.lid, nrm, r0, r1, reinterpret_cast<const CT*>(v),
         reinterpret_cast<const CT*>(S.ubuf.ptr), reinterpret_cast<CT*>(w));
   } else {
     auto kern = k_hv_csr<Real, LPR, false, kPol>;
     kern<<<grid_for(kern, 0, threads_needed, kTgtThreads), kTgtThreads, 0, st>>>(
-        S.row_ptr, S.col, S.vid, tab, S.n_vals, S.ezz, S.lid, nrm, n, reinterpret_cast<const CT*>(v),
+        S.row_ptr, S.col, S.vid, tab, S.n_vals, S.ezz, S.lid, nrm, r0, r1, reinterpret_cast<const CT*>(v),
         reinterpret_cast<const CT*>(S.ubuf.ptr), reinterpret_cast<CT*>(w));
   }
   return cudaGetLastError();
 }
 
 template <typename Real, int kPol>
-cudaError_t launch_csr_p(const Sector& S, const void* v, void* w, cudaStream_t st) {
+cudaError_t launch_csr_p(const Sector& S, const void* v, void* w, cudaStream_t st, int64_t r0, int64_t r1,
+                         bool with_u) {
   switch (S.csr_lpr) {
-    case 8: return launch_csr_lpr<Real, 8, kPol>(S, v, w, st);
-    case 16: return launch_csr_lpr<Real, 16, kPol>(S, v, w, st);
-    default: return launch_csr_lpr<Real, 32, kPol>(S, v, w, st);
+    case 8: return launch_csr_lpr<Real, 8, kPol>(S, v, w, st, r0, r1, with_u);
+    case 16: return launch_csr_lpr<Real, 16, kPol>(S, v, w, st, r0, r1, with_u);
+    default: return launch_csr_lpr<Real, 32, kPol>(S, v, w, st, r0, r1, with_u);
   }
 }
 
 template <typename Real>
-cudaError_t launch_csr_t(const Sector& S, const void* v, void* w, cudaStream_t st) {
-  return S.csr_pol == 2 ? launch_csr_p<Real, 2>(S, v, w, st) : launch_csr_p<Real, 1>(S, v, w, st);
+cudaError_t launch_csr_t(const Sector& S, const void* v, void* w, cudaStream_t st, int64_t r0 = 0,
+                         int64_t r1 = -1, bool with_u = true) {
+  if (r1 < 0) r1 = S.P.n_p;
+  return S.csr_pol == 2 ? launch_csr_p<Real, 2>(S, v, w, st, r0, r1, with_u)
+                        : launch_csr_p<Real, 1>(S, v, w, st, r0, r1, with_u);
 }
 
 // ---- column panels -------------------------------------------------------
@@ -1013,6 +1022,11 @@ int tune_rows(Sector& S, int lpr, int* chosen, double* ms_out) {
   S.csr_lpr = best;
   if (chosen) *chosen = best;
   return cudaGetLastError() == cudaSuccess ? EDG_OK : EDG_ERR_CUDA;
+}
+
+cudaError_t launch_hv_rows(const Sector& S, const void* v, void* w, bool fp64, int64_t r0, int64_t r1, bool with_u,
+                           cudaStream_t st) {
+  return fp64 ? launch_csr_t<double>(S, v, w, st, r0, r1, with_u) : launch_csr_t<float>(S, v, w, st, r0, r1, with_u);
 }
 
 cudaError_t launch_hv_stored(const Sector& S, const void* v, void* w, bool fp64, cudaStream_t st) {

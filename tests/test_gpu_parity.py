@@ -201,6 +201,24 @@ def test_tune_keeps_a_valid_choice(gpu):
     assert lanes == 16 and ms[1] > 0 and ms[0] == -1 and ms[2] == -1
 
 
+@pytest.mark.parametrize("dtype", [np.complex128, np.complex64])
+def test_host_call_in_row_chunks_equals_device_call(gpu, dtype):
+    """edg_hv_host copies finished rows back while later rows run (sectors of
+    2^20 rows and more): the same bits as one device call."""
+    import torch
+    from ed_code_gb300 import lattice as L
+
+    sec = gpu.GpuSector(L.make_model(L.TorusSpec("triangular", 6, 5, Jz=0.8, Ch=0.2), 0, 1, 4, bowties=False))
+    assert sec.n_p >= 1 << 20 and sec.build_targets()
+    v = O.splitmix_vector(sec.n_p, 12).astype(dtype)
+    w_host = sec.sHv(v, dtype=dtype)
+    vd = torch.from_numpy(v).cuda()
+    wd = torch.empty_like(vd)
+    sec.hv(vd, wd)
+    torch.cuda.synchronize()
+    assert np.array_equal(wd.cpu().numpy(), w_host)
+
+
 def test_hv_device_equals_host(gpu):
     import torch
 
