@@ -83,14 +83,19 @@ class Model:
     lattice: Optional[str] = None
     Lx: int = 0
     Ly: int = 0
+    # 3-D tori (ED_3D_Lattice_Geometry, read_input_file.cpp:443-780): the third
+    # translation and its momentum; T3 empty for 2-D models.
+    T3: List[int] = dataclasses.field(default_factory=list)
+    kz: int = 0
+    Lz: int = 1
 
     @property
     def n_ones(self) -> int:
         """Number of up spins for ``Sz`` (Lanczos_sector.cpp:45-46)."""
         return int(self.Sz + self.n_sites // 2 + 1.0e-6)
 
-    def with_sector(self, Sz: float, kx: int, ky: int) -> "Model":
-        return dataclasses.replace(self, Sz=float(Sz), kx=int(kx), ky=int(ky))
+    def with_sector(self, Sz: float, kx: int, ky: int, kz: int = 0) -> "Model":
+        return dataclasses.replace(self, Sz=float(Sz), kx=int(kx), ky=int(ky), kz=int(kz))
 
 
 # ----------------------------------------------------------------------------
@@ -149,6 +154,44 @@ def triangles_ccw(Lx: int, Ly: int) -> List[Tuple[int, int, int]]:
     return out
 
 
+def _site3(x: int, y: int, z: int, Lx: int, Ly: int, Lz: int) -> int:
+    return (x % Lx) + Lx * ((y % Ly) + Ly * (z % Lz))
+
+
+def translations3(Lx: int, Ly: int, Lz: int) -> Tuple[List[int], List[int], List[int]]:
+    """T1 = +x, T2 = +y, T3 = +z for labels s = x + Lx (y + Ly z)."""
+    n = Lx * Ly * Lz
+    xyz = [(s % Lx, (s // Lx) % Ly, s // (Lx * Ly)) for s in range(n)]
+    T1 = [_site3(x + 1, y, z, Lx, Ly, Lz) for x, y, z in xyz]
+    T2 = [_site3(x, y + 1, z, Lx, Ly, Lz) for x, y, z in xyz]
+    T3 = [_site3(x, y, z + 1, Lx, Ly, Lz) for x, y, z in xyz]
+    return T1, T2, T3
+
+
+def cubic_pairs(Lx: int, Ly: int, Lz: int) -> List[Tuple[int, int]]:
+    """Nearest-neighbour bonds of the simple-cubic torus, each listed once
+    (along a direction of length 2 the +1 and -1 neighbours coincide)."""
+    seen, out = set(), []
+    for z in range(Lz):
+        for y in range(Ly):
+            for x in range(Lx):
+                a = _site3(x, y, z, Lx, Ly, Lz)
+                for dx, dy, dz in ((1, 0, 0), (0, 1, 0), (0, 0, 1)):
+                    b = _site3(x + dx, y + dy, z + dz, Lx, Ly, Lz)
+                    key = (min(a, b), max(a, b))
+                    if a != b and key not in seen:
+                        seen.add(key)
+                        out.append((a, b))
+    return out
+
+
+def cubic_triangles(Lx: int, Ly: int, Lz: int) -> List[Tuple[int, int, int]]:
+    """Triangles (x,y,z), (x+1,y,z), (x,y+1,z) in every xy plane, for the
+    chirality term of the cubic torus."""
+    return [(_site3(x, y, z, Lx, Ly, Lz), _site3(x + 1, y, z, Lx, Ly, Lz), _site3(x, y + 1, z, Lx, Ly, Lz))
+            for z in range(Lz) for y in range(Ly) for x in range(Lx)]
+
+
 @dataclasses.dataclass
 class TorusSpec:
     """A torus plus couplings, before it is turned into reference term lists."""
@@ -162,30 +205,39 @@ class TorusSpec:
     ChCh: float = 0.0
     bond_phases: Optional[Sequence[float]] = None   # one phase per Pairs1 entry
     relabel: Optional[Sequence[int]] = None         # optional site permutation
+    Lz: int = 1                  # "cubic" only: the third dimension
 
     @property
     def n_sites(self) -> int:
-        return self.Lx * self.Ly
+        return self.Lx * self.Ly * self.Lz
 
     def pairs1(self):
+        if self.lattice == "cubic":
+            return cubic_pairs(self.Lx, self.Ly, self.Lz)
         vec = SQUARE_NN if self.lattice == "square" else TRIANGULAR_NN
         return _bond_set(self.Lx, self.Ly, vec)
 
     def pairs2(self):
         if self.J2 == 0.0:
             return []
+        if self.lattice == "cubic":
+            raise ValueError("J2 is not defined for the cubic torus")
         vec = SQUARE_NNN if self.lattice == "square" else TRIANGULAR_NNN
         return _bond_set(self.Lx, self.Ly, vec)
 
     def triangles(self):
-        if self.lattice != "triangular" or (self.Ch == 0.0 and self.ChCh == 0.0):
+        if self.Ch == 0.0 and self.ChCh == 0.0:
+            return []
+        if self.lattice == "cubic":
+            return cubic_triangles(self.Lx, self.Ly, self.Lz)
+        if self.lattice != "triangular":
             return []
         return triangles_ccw(self.Lx, self.Ly)
 
 
 def input_file_text(spec: TorusSpec, Sz: float = 0.0, kx: int = 0, ky: int = 0, *,
                     num_eigenvalues: int = 4, tol: float = 1e-12, iterations: int = 200,
-                    ncycles: int = 2, find_vectors: bool = False) -> str:
+                    ncycles: int = 2, find_vectors: bool = False, kz: int = 0) -> str:
     """Render ``spec`` in the reference's input format (read_input_file.cpp).
 
     Each key sits on its own line: ``J1=`` does not clear the parser's token
@@ -197,7 +249,11 @@ def input_file_text(spec: TorusSpec, Sz: float = 0.0, kx: int = 0, ky: int = 0, 
     perm = list(spec.relabel) if spec.relabel is not None else list(range(spec.n_sites))
     if sorted(perm) != list(range(spec.n_sites)):
         raise ValueError("relabel must be a permutation of the sites")
-    T1, T2 = translations(spec.Lx, spec.Ly)
+    cubic = spec.lattice == "cubic"
+    if cubic:
+        T1, T2, T3 = translations3(spec.Lx, spec.Ly, spec.Lz)
+    else:
+        T1, T2 = translations(spec.Lx, spec.Ly)
     # new label of old site s is perm[s]; T'[perm[s]] = perm[T[s]]
     T1p = [0] * spec.n_sites
     T2p = [0] * spec.n_sites
@@ -208,7 +264,8 @@ def input_file_text(spec: TorusSpec, Sz: float = 0.0, kx: int = 0, ky: int = 0, 
     phases = [float(p) for p in spec.bond_phases] if spec.bond_phases is not None else [0.0] * len(p1)
     if len(phases) != len(p1):
         raise ValueError("one bond phase per Pairs1 entry")
-    lines = [f"[{spec.lattice} torus {spec.Lx}x{spec.Ly}, row-major labels]"]
+    dims = f"{spec.Lx}x{spec.Ly}" + (f"x{spec.Lz}" if cubic else "")
+    lines = [f"[{spec.lattice} torus {dims}, row-major labels]"]
     lines.append(f"tol={tol!r}")
     lines.append(f"Lanczos_iterations={iterations}")
     lines.append(f"Lanczos_ncycles={ncycles}")
@@ -223,10 +280,17 @@ def input_file_text(spec: TorusSpec, Sz: float = 0.0, kx: int = 0, ky: int = 0, 
     lines.append(f"ChCh={spec.ChCh!r}")
     lines.append("T1=[" + ",".join(str(t) for t in T1p) + "]")
     lines.append("T2=[" + ",".join(str(t) for t in T2p) + "]")
+    if cubic:
+        T3p = [0] * spec.n_sites
+        for s in range(spec.n_sites):
+            T3p[perm[s]] = perm[T3[s]]
+        lines.append("T3=[" + ",".join(str(t) for t in T3p) + "]")
     lines.append("Specific_pSector=1")
     lines.append(f"Sz={Sz!r}")
     lines.append(f"kx={kx}")
     lines.append(f"ky={ky}")
+    if cubic:
+        lines.append(f"kz={kz}")
     lines.append(f"Num_Eigenvalues={num_eigenvalues}")
     lines.append(f"Find_Vectors={int(find_vectors)}")
     tris = spec.triangles()
@@ -293,6 +357,7 @@ def parse_input_text(text: str, bowties: bool = True) -> Model:
     tri_first: List[Triangle] = []
     T1: List[int] = []
     T2: List[int] = []
+    T3: List[int] = []
     kw = {}
     for raw in text.splitlines():
         line = "".join(raw.split())
@@ -315,12 +380,12 @@ def parse_input_text(text: str, bowties: bool = True) -> Model:
                 t3 = Triangle(z, x, y, _expphase_of(z, x, adj))
                 tri_first.append(t1)
                 ch.extend([t1, t2, t3])
-        elif key in ("T1", "T2"):
+        elif key in ("T1", "T2", "T3"):
             nums = [int(n) for n in re.findall(r"-?\d+", rest)]
-            (T1 if key == "T1" else T2).extend(nums)
+            {"T1": T1, "T2": T2, "T3": T3}[key].extend(nums)
         elif key in ("Sz",):
             kw["Sz"] = float(re.match(_NUM, rest).group(0))
-        elif key in ("kx", "ky", "Num_Eigenvalues", "Lanczos_iterations", "Lanczos_ncycles"):
+        elif key in ("kx", "ky", "kz", "Num_Eigenvalues", "Lanczos_iterations", "Lanczos_ncycles"):
             kw[key] = int(re.match(r"-?\d+", rest).group(0))
         elif key in ("Find_Vectors", "Unwrap_pVector"):
             kw[key] = bool(int(re.match(r"-?\d+", rest).group(0)))
@@ -330,6 +395,8 @@ def parse_input_text(text: str, bowties: bool = True) -> Model:
             kw["Vector_File_Path"] = rest
     if len(T1) != len(T2):
         raise ValueError("ERROR: input T1 != T2")   # read_input_file.cpp:423-427
+    if T3 and len(T3) != len(T1):
+        raise ValueError("ERROR: input T1 != T2 != T3")   # read_input_file.cpp:774-778
     chch = bowties_from_triangles(tri_first, adj) if (tri_first and bowties) else []
     return Model(
         n_sites=len(T1), T1=T1, T2=T2, adj_list=adj, ch_list=ch, chch_list=chch,
@@ -338,7 +405,7 @@ def parse_input_text(text: str, bowties: bool = True) -> Model:
         num_eigenvalues=kw.get("Num_Eigenvalues", 2), find_vectors=kw.get("Find_Vectors", False),
         unwrap_pvector=kw.get("Unwrap_pVector", True), vector_file_path=kw.get("Vector_File_Path", ""),
         tol=kw.get("tol", 1e-11), lanczos_iterations=kw.get("Lanczos_iterations", 100),
-        lanczos_ncycles=kw.get("Lanczos_ncycles", 10),
+        lanczos_ncycles=kw.get("Lanczos_ncycles", 10), T3=T3, kz=kw.get("kz", 0),
     )
 
 
@@ -347,5 +414,5 @@ def make_model(spec: TorusSpec, Sz: float = 0.0, kx: int = 0, ky: int = 0, bowti
     ``bowties=False`` leaves the ChCh bowtie list empty (it is O(triangles^2)
     to build and unused when ChCh is 0)."""
     m = parse_input_text(input_file_text(spec, Sz, kx, ky, **kw), bowties=bowties)
-    m.lattice, m.Lx, m.Ly = spec.lattice, spec.Lx, spec.Ly
+    m.lattice, m.Lx, m.Ly, m.Lz = spec.lattice, spec.Lx, spec.Ly, spec.Lz
     return m

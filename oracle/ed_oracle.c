@@ -79,13 +79,17 @@ void or_LxLy(const int *T1, const int *T2, int n_sites, int *L1, int *L2) {
  * between x steps.  The first strict minimum wins and records lx = L1-tx,
  * ly = L2-ty.  lid counts translates equal to v (identity included); p_id
  * tests the accumulated phase sum against 1e-8. */
-int64_t or_representative(int64_t v, const int *T1, const int *T2, int n_sites, int L1, int L2, double px,
-                          double py, int *lx, int *ly, int *lid, int *p_id) {
-  *lx = 0; *ly = 0;
+/* representative_p, 3-D (Momentum_Basis.cpp:545-643): for x < L1 { if x>0
+ * T1; for y < L2 { if y>0 T2; for z < L3 { if z>0 T3 } } }.  With T3 == NULL
+ * (L3 = 1) the z loop applies nothing and this is the 2-D walk
+ * (Momentum_Basis.cpp:472-543) step for step. */
+int64_t or_representative3(int64_t v, const int *T1, const int *T2, const int *T3, int n_sites, int L1, int L2,
+                           int L3, double px, double py, double pz, int *lx, int *ly, int *lz, int *lid, int *p_id) {
+  *lx = 0; *ly = 0; *lz = 0;
   int64_t rep = v, tmp = v;
-  int tx = 0, ty = 0;
+  int tx = 0, ty = 0, tz = 0;
   double complex ph = 1.0, id_coeff = 1.0;
-  const double complex ex = cexp(CMPLX(0.0, -px)), ey = cexp(CMPLX(0.0, -py));
+  const double complex ex = cexp(CMPLX(0.0, -px)), ey = cexp(CMPLX(0.0, -py)), ez = cexp(CMPLX(0.0, -pz));
   *lid = 1;
   for (int x = 0; x < L1; ++x) {
     if (x > 0) {
@@ -93,7 +97,7 @@ int64_t or_representative(int64_t v, const int *T1, const int *T2, int n_sites, 
       ++tx;
       ph = ph * ex;
       if (v == tmp) { id_coeff = id_coeff + ph; ++*lid; }
-      if (rep > tmp) { rep = tmp; *lx = L1 - tx; *ly = L2 - ty; }
+      if (rep > tmp) { rep = tmp; *lx = L1 - tx; *ly = L2 - ty; *lz = L3 - tz; }
     }
     for (int y = 0; y < L2; ++y) {
       if (y > 0) {
@@ -101,12 +105,34 @@ int64_t or_representative(int64_t v, const int *T1, const int *T2, int n_sites, 
         ++ty;
         ph = ph * ey;
         if (v == tmp) { id_coeff = id_coeff + ph; ++*lid; }
-        if (rep > tmp) { rep = tmp; *lx = L1 - tx; *ly = L2 - ty; }
+        if (rep > tmp) { rep = tmp; *lx = L1 - tx; *ly = L2 - ty; *lz = L3 - tz; }
+      }
+      for (int z = 1; z < L3; ++z) {
+        tmp = (int64_t)or_translate((uint64_t)tmp, T3, n_sites);
+        ++tz;
+        ph = ph * ez;
+        if (v == tmp) { id_coeff = id_coeff + ph; ++*lid; }
+        if (rep > tmp) { rep = tmp; *lx = L1 - tx; *ly = L2 - ty; *lz = L3 - tz; }
       }
     }
   }
   *p_id = (fabs(creal(id_coeff)) > 1e-8 || fabs(cimag(id_coeff)) > 1e-8) ? 1 : 0;
   return rep;
+}
+
+int64_t or_representative(int64_t v, const int *T1, const int *T2, int n_sites, int L1, int L2, double px,
+                          double py, int *lx, int *ly, int *lid, int *p_id) {
+  int lz;
+  return or_representative3(v, T1, T2, NULL, n_sites, L1, L2, 1, px, py, 0.0, lx, ly, &lz, lid, p_id);
+}
+
+/* L3 of LxLyLz (Momentum_Basis.cpp:38-63); 1 without T3. */
+int or_L3(const int *T3, int n_sites) {
+  if (!T3) return 1;
+  int L3 = 0;
+  uint64_t t = 1;
+  do { t = or_translate(t, T3, n_sites); ++L3; } while (t != 1);
+  return L3;
 }
 
 /* findstate (binary search over the ascending representatives, as
@@ -122,17 +148,21 @@ static int64_t find_state(int64_t key, const int64_t *reps, int64_t n) {
   return -1;
 }
 
-/* pConstruct_States, 2-D (Momentum_Basis.cpp:645-778). */
-or_basis *or_build_basis(int n_sites, int n_ones, const int *T1, const int *T2, int kx, int ky) {
+/* pConstruct_States, 2-D (Momentum_Basis.cpp:645-778) and 3-D (:781-895):
+ * T3 == NULL is the 2-D case. */
+or_basis *or_build_basis3(int n_sites, int n_ones, const int *T1, const int *T2, const int *T3, int kx, int ky,
+                          int kz) {
   if (n_sites < 1 || n_sites > 62 || n_ones < 0 || n_ones > n_sites) return NULL;
   or_basis *b = (or_basis *)calloc(1, sizeof(or_basis));
-  b->n_sites = n_sites; b->n_ones = n_ones; b->kx = kx; b->ky = ky;
+  b->n_sites = n_sites; b->n_ones = n_ones; b->kx = kx; b->ky = ky; b->kz = kz;
   int half = n_sites / 2;
   if (n_sites % 2 == 1) ++half; /* Momentum_Basis.cpp:681-682 */
   b->half_sites = half;
   or_LxLy(T1, T2, n_sites, &b->L1, &b->L2);
-  const int L1 = b->L1, L2 = b->L2;
+  b->L3 = or_L3(T3, n_sites);
+  const int L1 = b->L1, L2 = b->L2, L3 = b->L3;
   const double px = 2 * kx * OR_PI / L1, py = 2 * ky * OR_PI / L2; /* Lanczos_sector.cpp:57 */
+  const double pz = 2 * kz * OR_PI / L3;                              /* Lanczos_sector.cpp:240 */
   const int64_t nc = or_n_choose_k(n_sites, n_ones);
   b->n_configs = nc;
   const int64_t nh = (int64_t)1 << half;
@@ -149,6 +179,7 @@ or_basis *or_build_basis(int n_sites, int n_ones, const int *T1, const int *T2, 
   b->state_ph = (double *)malloc(sizeof(double) * 2 * (nc ? nc : 1));
   b->lx = (int32_t *)malloc(sizeof(int32_t) * (nc ? nc : 1));
   b->ly = (int32_t *)malloc(sizeof(int32_t) * (nc ? nc : 1));
+  b->lz = (int32_t *)malloc(sizeof(int32_t) * (nc ? nc : 1));
 
   /* constrained_dets: all states in increasing order. */
   int64_t t = n_ones ? (((int64_t)1 << n_ones) - 1) : 0;
@@ -165,17 +196,21 @@ or_basis *or_build_basis(int n_sites, int n_ones, const int *T1, const int *T2, 
   }
 #pragma omp parallel for schedule(dynamic, 4096)
   for (int64_t i = 0; i < nc; ++i) {
-    int lx, ly, lid, pid;
-    rep_ids[i] = or_representative(all[i], T1, T2, n_sites, L1, L2, px, py, &lx, &ly, &lid, &pid);
+    int lx, ly, lz, lid, pid;
+    rep_ids[i] = or_representative3(all[i], T1, T2, T3, n_sites, L1, L2, L3, px, py, pz, &lx, &ly, &lz, &lid, &pid);
     pids[i] = (unsigned char)pid;
     lids[i] = lid;
     lx = lx % L1;
     ly = ly % L2;
+    lz = lz % L3;
     if (lx < 0) lx += L1;
     if (ly < 0) ly += L2;
+    if (lz < 0) lz += L3;
     b->lx[i] = lx;
     b->ly[i] = ly;
-    double complex ph = cexp(CMPLX(0.0, -px * lx - py * ly)); /* Momentum_Basis.cpp:753 */
+    b->lz[i] = lz;
+    /* Momentum_Basis.cpp:753 (2-D), :872 (3-D); pz*lz is 0 without T3 */
+    double complex ph = T3 ? cexp(CMPLX(0.0, -px * lx - py * ly - pz * lz)) : cexp(CMPLX(0.0, -px * lx - py * ly));
     b->state_ph[2 * i] = creal(ph);
     b->state_ph[2 * i + 1] = cimag(ph);
   }
@@ -190,7 +225,7 @@ or_basis *or_build_basis(int n_sites, int n_ones, const int *T1, const int *T2, 
   np = 0;
   for (int64_t i = 0; i < nc; ++i) {
     if (rep_ids[i] == all[i] && pids[i]) {
-      int64_t N = (int64_t)(L1 * L2) / lids[i]; /* integer division, Momentum_Basis.cpp:764 */
+      int64_t N = (int64_t)(L1 * L2 * L3) / lids[i]; /* integer division, Momentum_Basis.cpp:764, :883 */
       b->states[np] = all[i];
       b->norm[np] = sqrt((double)N);
       b->norm_inv[np] = 1 / sqrt((double)N);
@@ -204,10 +239,14 @@ or_basis *or_build_basis(int n_sites, int n_ones, const int *T1, const int *T2, 
   return b;
 }
 
+or_basis *or_build_basis(int n_sites, int n_ones, const int *T1, const int *T2, int kx, int ky) {
+  return or_build_basis3(n_sites, n_ones, T1, T2, NULL, kx, ky, 0);
+}
+
 void or_free_basis(or_basis *b) {
   if (!b) return;
   free(b->states); free(b->norm); free(b->norm_inv); free(b->lid); free(b->rep_loc);
-  free(b->state_ph); free(b->lx); free(b->ly); free(b->Ia); free(b->Ib);
+  free(b->state_ph); free(b->lx); free(b->ly); free(b->lz); free(b->Ia); free(b->Ib);
   free(b);
 }
 
@@ -462,17 +501,20 @@ int or_allowed_rep(int64_t state, const int *T1, const int *T2, int n_sites, int
 
 /* Character count of the sector dimension: (1/|G|) sum_{a,b} chi(a,b) Fix(T1^a T2^b),
  * Fix(g) = number of n_ones-subsets that are unions of cycles of g. */
-int64_t or_sector_dim(int n_sites, int n_ones, const int *T1, const int *T2, int kx, int ky) {
+int64_t or_sector_dim3(int n_sites, int n_ones, const int *T1, const int *T2, const int *T3, int kx, int ky, int kz) {
   int L1, L2;
   or_LxLy(T1, T2, n_sites, &L1, &L2);
+  const int L3 = or_L3(T3, n_sites);
   int perm[64], seen[64];
   long double total = 0;
   for (int a = 0; a < L1; ++a) {
     for (int b = 0; b < L2; ++b) {
+     for (int c3 = 0; c3 < L3; ++c3) {
       for (int s = 0; s < n_sites; ++s) {
         int t = s;
         for (int k = 0; k < a; ++k) t = T1[t];
         for (int k = 0; k < b; ++k) t = T2[t];
+        for (int k = 0; k < c3; ++k) t = T3[t];
         perm[s] = t;
       }
       /* coefficient of x^n_ones in prod (1 + x^len) */
@@ -486,11 +528,16 @@ int64_t or_sector_dim(int n_sites, int n_ones, const int *T1, const int *T2, int
         while (!seen[t]) { seen[t] = 1; t = perm[t]; ++len; }
         for (int k = 64; k >= len; --k) poly[k] += poly[k - len];
       }
-      double ang = 2 * OR_PI * ((double)kx * a / L1 + (double)ky * b / L2);
+      double ang = 2 * OR_PI * ((double)kx * a / L1 + (double)ky * b / L2 + (double)kz * c3 / L3);
       total += poly[n_ones] * (long double)cos(ang);
+     }
     }
   }
-  return (int64_t)llroundl(total / (L1 * L2));
+  return (int64_t)llroundl(total / (L1 * L2 * L3));
+}
+
+int64_t or_sector_dim(int n_sites, int n_ones, const int *T1, const int *T2, int kx, int ky) {
+  return or_sector_dim3(n_sites, n_ones, T1, T2, NULL, kx, ky, 0);
 }
 
 /* Unrank Lin index r (increasing-integer order of n_sites-bit words with

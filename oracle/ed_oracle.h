@@ -33,6 +33,8 @@ typedef struct {
   double *state_ph;     /* exp(-i(px lx + py ly)), interleaved re/im      (2*n_configs)*/
   int32_t *lx, *ly;     /* translation indices behind state_ph            (n_configs)  */
   int64_t *Ia, *Ib;     /* Lin tables                                      (2^half)     */
+  int L3, kz;           /* 3-D tori (1, 0 otherwise)                                    */
+  int32_t *lz;          /*                                                 (n_configs)  */
 } or_basis;
 
 int64_t or_n_choose_k(int n, int k);
@@ -44,6 +46,12 @@ int64_t or_representative(int64_t v, const int *T1, const int *T2, int n_sites, 
 
 /* Full tables as pConstruct_States builds them.  Returns NULL on bad input. */
 or_basis *or_build_basis(int n_sites, int n_ones, const int *T1, const int *T2, int kx, int ky);
+or_basis *or_build_basis3(int n_sites, int n_ones, const int *T1, const int *T2, const int *T3, int kx, int ky,
+                          int kz);
+int64_t or_representative3(int64_t v, const int *T1, const int *T2, const int *T3, int n_sites, int L1, int L2,
+                           int L3, double px, double py, double pz, int *lx, int *ly, int *lz, int *lid, int *p_id);
+int or_L3(const int *T3, int n_sites);
+int64_t or_sector_dim3(int n_sites, int n_ones, const int *T1, const int *T2, const int *T3, int kx, int ky, int kz);
 void or_free_basis(or_basis *b);
 
 /* w = H v with the reference's tables (sHv, H_v.cpp:192-357).  v, w interleaved re/im. */

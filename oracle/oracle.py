@@ -37,7 +37,8 @@ class Basis(C.Structure):
         ("n_p", C.c_int64), ("states", C.POINTER(C.c_int64)), ("norm", C.POINTER(C.c_double)),
         ("norm_inv", C.POINTER(C.c_double)), ("lid", C.POINTER(C.c_int32)), ("rep_loc", C.POINTER(C.c_int64)),
         ("state_ph", C.POINTER(C.c_double)), ("lx", C.POINTER(C.c_int32)), ("ly", C.POINTER(C.c_int32)),
-        ("Ia", C.POINTER(C.c_int64)), ("Ib", C.POINTER(C.c_int64)),
+        ("Ia", C.POINTER(C.c_int64)), ("Ib", C.POINTER(C.c_int64)), ("L3", C.c_int), ("kz", C.c_int),
+        ("lz", C.POINTER(C.c_int32)),
     ]
 
 
@@ -59,6 +60,9 @@ def lib() -> C.CDLL:
         L = C.CDLL(LIB_PATH)
         L.or_build_basis.restype = C.POINTER(Basis)
         L.or_build_basis.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int, C.c_int]
+        L.or_build_basis3.restype = C.POINTER(Basis)
+        L.or_build_basis3.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                      C.c_int, C.c_int, C.c_int]
         L.or_free_basis.argtypes = [C.POINTER(Basis)]
         L.or_hv_tables.argtypes = [C.POINTER(Basis), C.c_void_p, C.c_void_p, C.c_double, C.POINTER(Bond), C.c_int,
                                    C.c_double, C.POINTER(Tri), C.c_int, C.c_double, C.POINTER(Bowtie), C.c_int]
@@ -70,6 +74,9 @@ def lib() -> C.CDLL:
         L.or_allowed_rep.restype = C.c_int
         L.or_sector_dim.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int, C.c_int]
         L.or_sector_dim.restype = C.c_int64
+        L.or_sector_dim3.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                     C.c_int, C.c_int, C.c_int]
+        L.or_sector_dim3.restype = C.c_int64
         L.or_build_reps.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int, C.c_int,
                                     C.POINTER(C.POINTER(C.c_int64)), C.POINTER(C.POINTER(C.c_int32)), C.c_int]
         L.or_build_reps.restype = C.c_int64
@@ -108,6 +115,7 @@ class TermLists:
         self.nbw = len(model.chch_list)
         self.T1 = _ints(model.T1)
         self.T2 = _ints(model.T2)
+        self.T3 = _ints(model.T3) if getattr(model, "T3", None) else None
 
 
 class OracleSector:
@@ -116,14 +124,18 @@ class OracleSector:
     def __init__(self, model):
         self.model = model
         self.terms = TermLists(model)
-        p = lib().or_build_basis(model.n_sites, model.n_ones, self.terms.T1, self.terms.T2, model.kx, model.ky)
+        if self.terms.T3 is not None:
+            p = lib().or_build_basis3(model.n_sites, model.n_ones, self.terms.T1, self.terms.T2, self.terms.T3,
+                                      model.kx, model.ky, model.kz)
+        else:
+            p = lib().or_build_basis(model.n_sites, model.n_ones, self.terms.T1, self.terms.T2, model.kx, model.ky)
         if not p:
             raise ValueError("oracle: bad sector")
         self._p = p
         b = p.contents
         self.n_p = int(b.n_p)
         self.n_configs = int(b.n_configs)
-        self.L1, self.L2 = int(b.L1), int(b.L2)
+        self.L1, self.L2, self.L3 = int(b.L1), int(b.L2), int(b.L3)
         self.bits_right = int(b.bits_right)
         arr = np.ctypeslib.as_array
         n, nc, nh = self.n_p, self.n_configs, 1 << b.half_sites
@@ -231,6 +243,8 @@ def allowed_rep(model, state: int) -> int:
 
 def sector_dim(model) -> int:
     t = TermLists(model)
+    if t.T3 is not None:
+        return int(lib().or_sector_dim3(model.n_sites, model.n_ones, t.T1, t.T2, t.T3, model.kx, model.ky, model.kz))
     return int(lib().or_sector_dim(model.n_sites, model.n_ones, t.T1, t.T2, model.kx, model.ky))
 
 

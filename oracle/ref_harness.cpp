@@ -7,7 +7,7 @@
 // (H_v.cpp:192) to caller-supplied vectors.  Everything is written as raw
 // little-endian arrays into an output directory:
 //
-//   meta.txt          n_sites n_ones L1 L2 kx ky n_p n_configs bits_right
+//   meta.txt          n_sites n_ones L1 L2 kx ky n_p n_configs bits_right t_basis [L3 kz]
 //   states.i64        pblock_states            (n_p)
 //   norm.f64          norm                     (n_p)
 //   rep_loc.i64       rep_loc                  (n_configs)      [tables mode]
@@ -15,6 +15,10 @@
 //   Ia.i64, Ib.i64    Lin tables               (2^half)         [tables mode]
 //   w<k>.c128         sHv(v<k>)                                 [if v<k>.c128 given]
 //   terms.txt         adj_list / ch_list / chch_list / T1 / T2 as parsed
+//
+// An input file with a T3= line is read with ED_3D_Lattice_Geometry
+// (read_input_file.cpp:443) and goes through the 3-D pConstruct_States
+// (Momentum_Basis.cpp:781) and sHv (H_v.cpp:360); meta.txt then ends with L3 kz.
 //
 // usage: ref_harness <input-file> <out-dir> [tables|notables] [nvec] [reps]
 // The v<k>.c128 inputs are read from <out-dir>.  With reps > 1 each sHv call
@@ -66,22 +70,40 @@ int main(int argc, char** argv) {
   std::vector<int> T1, T2, cut; double sSz = -1; int kx = -1, ky = -1;
   bool all_s = false, psec = false, find_v = false, unwrap = true; double szs = -1;
   int nev = 2; std::string vpath;
-  ED_2D_Lattice_Geometry(in, n_spins, Jz, J1, J2, adj, Ch, chl, ChCh, chch, T1, T2, cut, sSz, kx, ky, all_s, szs,
-                         psec, nev, find_v, unwrap, vpath, log);
+  bool three_d = false;
+  {
+    std::ifstream f(in.c_str());
+    std::string line;
+    while (std::getline(f, line))
+      if (line.compare(0, 3, "T3=") == 0) three_d = true;
+  }
+  std::vector<int> T3;
+  int kz = 0;
+  if (three_d)
+    ED_3D_Lattice_Geometry(in, n_spins, Jz, J1, J2, adj, Ch, chl, ChCh, chch, T1, T2, T3, cut, sSz, kx, ky, kz, all_s,
+                           szs, psec, nev, find_v, unwrap, vpath, log);
+  else
+    ED_2D_Lattice_Geometry(in, n_spins, Jz, J1, J2, adj, Ch, chl, ChCh, chch, T1, T2, cut, sSz, kx, ky, all_s, szs,
+                           psec, nev, find_v, unwrap, vpath, log);
   // Same n_ones rule as Lanczos_sector.cpp:45-46.
   int n_ones = int(sSz + n_spins / 2 + 1.0e-6);
-  int L1 = 0, L2 = 0;
-  LxLy(L1, L2, T1, T2);
-  double px = 2 * kx * M_PI / L1, py = 2 * ky * M_PI / L2;
+  int L1 = 0, L2 = 0, L3 = 1;
+  if (three_d) LxLyLz(L1, L2, L3, T1, T2, T3);
+  else LxLy(L1, L2, T1, T2);
+  double px = 2 * kx * M_PI / L1, py = 2 * ky * M_PI / L2, pz = 2 * kz * M_PI / L3;
   std::vector<int64_t> states, rep_loc, Ia, Ib; std::vector<double> norm, norm_inv;
   std::vector<std::complex<double>> state_ph; int64_t n_p = 0; int bits_right = 0;
   double t0 = wall_clock();
-  pConstruct_States(states, norm, norm_inv, T1, T2, n_ones, px, py, n_p, rep_loc, state_ph, Ia, Ib, bits_right, log);
+  if (three_d)
+    pConstruct_States(states, norm, norm_inv, T1, T2, T3, n_ones, px, py, pz, n_p, rep_loc, state_ph, Ia, Ib,
+                      bits_right, log);
+  else
+    pConstruct_States(states, norm, norm_inv, T1, T2, n_ones, px, py, n_p, rep_loc, state_ph, Ia, Ib, bits_right, log);
   double t_basis = wall_clock() - t0;
 
   FILE* m = std::fopen((out + "/meta.txt").c_str(), "w");
-  std::fprintf(m, "%d %d %d %d %d %d %lld %lld %d %.6f\n", n_spins, n_ones, L1, L2, kx, ky, (long long)n_p,
-               (long long)rep_loc.size(), bits_right, t_basis);
+  std::fprintf(m, "%d %d %d %d %d %d %lld %lld %d %.6f %d %d\n", n_spins, n_ones, L1, L2, kx, ky, (long long)n_p,
+               (long long)rep_loc.size(), bits_right, t_basis, L3, kz);
   std::fclose(m);
   {
     // Term lists exactly as the reference parser produced them.
@@ -91,6 +113,10 @@ int main(int argc, char** argv) {
     for (int v : T1) std::fprintf(t, " %d", v);
     std::fprintf(t, "\nT2");
     for (int v : T2) std::fprintf(t, " %d", v);
+    if (three_d) {
+      std::fprintf(t, "\nT3");
+      for (int v : T3) std::fprintf(t, " %d", v);
+    }
     std::fprintf(t, "\n");
     for (auto& b : adj) std::fprintf(t, "bond %d %d %.17g %.17g %.17g\n", b.x, b.y, b.J, b.expphase.real(), b.expphase.imag());
     for (auto& c : chl) std::fprintf(t, "ch %d %d %d %.17g %.17g\n", c.i, c.j, c.k, c.expphase.real(), c.expphase.imag());
@@ -111,8 +137,12 @@ int main(int argc, char** argv) {
     if (!read_vec(out + "/v" + std::to_string(k) + ".c128", v, n_p)) break;
     for (int r = 0; r < reps; ++r) {
       double t1 = wall_clock();
-      sHv(v.data(), w.data(), states, norm, norm_inv, rep_loc, state_ph, Jz, adj, Ch, chl, ChCh, chch, n_spins, Ia,
-          Ib, bits_right, T1, T2, px, py, log);
+      if (three_d)
+        sHv(v.data(), w.data(), states, norm, norm_inv, rep_loc, state_ph, Jz, adj, Ch, chl, ChCh, chch, n_spins, Ia,
+            Ib, bits_right, T1, T2, T3, px, py, pz, log);
+      else
+        sHv(v.data(), w.data(), states, norm, norm_inv, rep_loc, state_ph, Jz, adj, Ch, chl, ChCh, chch, n_spins, Ia,
+            Ib, bits_right, T1, T2, px, py, log);
       t_hv += wall_clock() - t1; ++calls;
     }
     dump(out + "/w" + std::to_string(k) + ".c128", w);

@@ -33,7 +33,8 @@ def golden_model(name, sector_index):
     meta = golden_cases()[name]
     s = meta["sectors"][sector_index]
     spec = L.TorusSpec(**meta["spec"])
-    return L.make_model(spec, s["Sz"], s["kx"], s["ky"])
+    extra = dict(kz=s.get("kz", 0)) if spec.lattice == "cubic" else {}
+    return L.make_model(spec, s["Sz"], s["kx"], s["ky"], **extra)
 
 
 def all_golden_sectors(max_configs=None, full_only=False):

@@ -54,7 +54,7 @@ def rng_relabel(n, seed):
 
 
 
-# name -> (spec kwargs, [(Sz, kx, ky)], run ED2?, ED2 kwargs)
+# name -> (spec kwargs, [(Sz, kx, ky) or (Sz, kx, ky, kz)], run ED2?, ED2 kwargs)
 CASES = {
     "sq4x4": (dict(lattice="square", Lx=4, Ly=4), [(0, 0, 0)], True, dict(num_eigenvalues=4)),
     "sq4x4_j2": (dict(lattice="square", Lx=4, Ly=4, Jz=0.7, J2=0.4), [(0, 2, 2), (0, 1, 0)], True,
@@ -77,6 +77,12 @@ CASES = {
                    dict(num_eigenvalues=2, iterations=120, ncycles=3, tol=1e-12)),
     "sq6x4_k00": (dict(lattice="square", Lx=6, Ly=4), [(0, 0, 0)], True,
                   dict(num_eigenvalues=4, iterations=200, ncycles=2, tol=1e-12)),
+    # 3-D tori go through the reference's 3-D pConstruct_States and sHv.  Its
+    # driver fixes dim = 2 (ED.cpp:69), so there is no ED2 run for them.
+    "cub3x2x2": (dict(lattice="cubic", Lx=3, Ly=2, Lz=2, Jz=0.9, Ch=0.2), [(0, 0, 0, 0), (0, 1, 1, 1), (1, 2, 0, 1)],
+                 False, dict(num_eigenvalues=3)),
+    "cub4x2x2": (dict(lattice="cubic", Lx=4, Ly=2, Lz=2, Jz=1.1), [(0, 2, 1, 0), (0, 1, 0, 1)], False,
+                 dict(num_eigenvalues=3)),
 }
 
 
@@ -103,16 +109,19 @@ def run_case(name: str, workdir: str) -> dict:
     spec = L.TorusSpec(**spec_kw)
     store = {}
     meta = {"spec": {k: v for k, v in spec_kw.items()}, "sectors": []}
-    for si, (Sz, kx, ky) in enumerate(sectors):
+    for si, sec in enumerate(sectors):
+        Sz, kx, ky = sec[:3]
+        kz = sec[3] if len(sec) > 3 else 0
+        extra = dict(kz=kz) if spec.lattice == "cubic" else {}
         tag = f"s{si}"
         d = os.path.join(workdir, f"{name}_{tag}")
         os.makedirs(d, exist_ok=True)
-        text = L.input_file_text(spec, Sz, kx, ky, **ed2_kw)
+        text = L.input_file_text(spec, Sz, kx, ky, **extra, **ed2_kw)
         inp = os.path.join(d, "in.txt")
         with open(inp, "w") as f:
             f.write(text)
-        model = L.make_model(spec, Sz, kx, ky)
-        n_p_guess = O.sector_dim(model)
+        model = L.make_model(spec, Sz, kx, ky, **extra)
+        n_p_guess = O.OracleSector(model).n_p if model.T3 else O.sector_dim(model)
         vecs = [O.splitmix_vector(n_p_guess, s) for s in VEC_SEEDS]
         for k, v in enumerate(vecs):
             v.tofile(os.path.join(d, f"v{k}.c128"))
@@ -127,7 +136,7 @@ def run_case(name: str, workdir: str) -> dict:
         Ia = np.fromfile(os.path.join(d, "Ia.i64"), np.int64)
         Ib = np.fromfile(os.path.join(d, "Ib.i64"), np.int64)
         ws = [np.fromfile(os.path.join(d, f"w{k}.c128"), np.complex128) for k in range(len(vecs))]
-        sm = {"Sz": Sz, "kx": kx, "ky": ky, "n_sites": n_sites, "n_ones": n_ones, "L1": L1, "L2": L2, "n_p": n_p,
+        sm = {"Sz": Sz, "kx": kx, "ky": ky, "kz": kz, "L3": int(meta_line[10]), "n_sites": n_sites, "n_ones": n_ones, "L1": L1, "L2": L2, "n_p": n_p,
               "n_configs": n_cfg, "bits_right": bits_right, "vec_seeds": list(VEC_SEEDS),
               "sha_states": sha(states), "sha_norm": sha(norm), "sha_rep_loc": sha(rep_loc), "sha_Ia": sha(Ia),
               "sha_Ib": sha(Ib), "full": n_cfg <= FULL_TABLE_LIMIT}

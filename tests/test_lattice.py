@@ -63,3 +63,18 @@ def test_bowties_only_when_triangles_neighbour():
     m = L.make_model(L.TorusSpec("triangular", 4, 3, Ch=0.2, ChCh=0.1))
     ntri = len(m.ch_list) // 3
     assert len(m.chch_list) % 9 == 0 and 0 < len(m.chch_list) <= 9 * ntri * (ntri - 1)
+
+
+def test_cubic_torus_round_trip():
+    spec = L.TorusSpec("cubic", 4, 2, Lz=3, Jz=0.9, Ch=0.2)
+    m = L.make_model(spec, 1, 2, 1, kz=2)
+    assert m.n_sites == 24 and m.kz == 2 and (m.kx, m.ky, m.Sz) == (2, 1, 1.0)
+    T1, T2, T3 = L.translations3(4, 2, 3)
+    assert (m.T1, m.T2, m.T3) == (T1, T2, T3)
+    # every site has 6 neighbours on a 4x2x3 torus, the y direction (length 2) counting once
+    assert len(m.adj_list) == 24 * 3 - 24 // 2
+    assert len(m.ch_list) == 3 * 24
+    text = L.input_file_text(spec, 1, 2, 1, kz=2)
+    assert "T3=[" in text and "kz=2" in text
+    assert L.parse_input_text(text).T3 == T3
+    assert "T3=" not in L.input_file_text(L.TorusSpec("square", 4, 4))
