@@ -45,7 +45,7 @@ class edg_model(C.Structure):
         ("n_sites", C.c_int), ("T1", C.POINTER(C.c_int)), ("T2", C.POINTER(C.c_int)), ("lambda_", C.c_double),
         ("bonds", C.POINTER(edg_bond)), ("n_bonds", C.c_int), ("Ch", C.c_double),
         ("triangles", C.POINTER(edg_triangle)), ("n_triangles", C.c_int), ("ChCh", C.c_double),
-        ("bowties", C.POINTER(edg_bowtie)), ("n_bowties", C.c_int),
+        ("bowties", C.POINTER(edg_bowtie)), ("n_bowties", C.c_int), ("T3", C.POINTER(C.c_int)),
     ]
 
 
@@ -54,7 +54,7 @@ class edg_sector_info(C.Structure):
         ("n_sites", C.c_int), ("n_ones", C.c_int), ("L1", C.c_int), ("L2", C.c_int), ("kx", C.c_int),
         ("ky", C.c_int), ("torus", C.c_int), ("n_groups", C.c_int), ("n_p", C.c_int64), ("n_configs", C.c_int64),
         ("device_bytes", C.c_int64), ("n_targets", C.c_int64), ("lanes_per_row", C.c_int),
-        ("cache_policy", C.c_int), ("panels", C.c_int),
+        ("cache_policy", C.c_int), ("panels", C.c_int), ("L3", C.c_int), ("kz", C.c_int),
     ]
 
 
@@ -105,6 +105,8 @@ SIGNATURES = {
     "edg_last_error": (C.c_char_p, []),
     "edg_abi_version": (C.c_int, []),
     "edg_sector_create": (C.c_int, [C.POINTER(edg_model), C.c_int, C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
+    "edg_sector_create3": (C.c_int, [C.POINTER(edg_model), C.c_int, C.c_int, C.c_int, C.c_int,
+                                     C.POINTER(C.c_void_p)]),
     "edg_sector_destroy": (C.c_int, [C.c_void_p]),
     "edg_sector_get_info": (C.c_int, [C.c_void_p, C.POINTER(edg_sector_info)]),
     "edg_sector_copy_basis": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

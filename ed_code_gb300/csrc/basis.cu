@@ -28,6 +28,7 @@ struct BuildTables {
   const uint16_t* rots;
   const uint64_t* p1;
   const uint64_t* p2;
+  const uint64_t* p3;  // T3 (3-D tori only)
 };
 
 template <bool kTorus>
@@ -44,11 +45,12 @@ __device__ BuildTables stage_build_tables(const SectorView& V, uint8_t* sm) {
     T.nk = nk;
     T.rots = rots;
   } else {
-    const int n = 2 * V.n_chunks * 256;
+    const int n = V.n_perm * V.n_chunks * 256;
     uint64_t* p = reinterpret_cast<uint64_t*>(sm);
     for (int i = threadIdx.x; i < n; i += blockDim.x) p[i] = V.perms[i];
     T.p1 = p;
     T.p2 = p + V.n_chunks * 256;
+    T.p3 = p + 2 * V.n_chunks * 256;
   }
   return T;
 }
@@ -56,7 +58,7 @@ __device__ BuildTables stage_build_tables(const SectorView& V, uint8_t* sm) {
 template <bool kTorus>
 __device__ __forceinline__ int allowed(uint64_t t, const SectorParams& P, const BuildTables& T, int n_chunks) {
   if (kTorus) return torus_allowed(t, P, T.nk, T.rots);
-  return walk_allowed(t, P, T.p1, T.p2, n_chunks);
+  return walk_allowed(t, P, T.p1, T.p2, T.p3, n_chunks);
 }
 
 template <bool kTorus>
@@ -217,7 +219,7 @@ __global__ void __launch_bounds__(kBuildThreads) k_walk_tables(SectorView V, int
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < P.n_configs;
        i += (int64_t)gridDim.x * blockDim.x) {
     uint64_t t = unrank_config((uint64_t)i, P.n_sites, P.n_ones, V.binom);
-    Orbit o = orbit_walk(t, P, T.p1, T.p2, V.n_chunks);
+    Orbit o = orbit_walk(t, P, T.p1, T.p2, T.p3, V.n_chunks);
     int bit;
     const uint32_t q = vrec_of(o.rep, &bit);
     rep_loc[i] = (int64_t)q < P.n_vrecs ? rank_lookup_bit(bit, V.vrecs[q]) : -1;
@@ -243,7 +245,7 @@ __global__ void k_vrank_count(const RankRec* __restrict__ vrecs, int64_t n, uint
 
 size_t build_smem_bytes(const SectorView& V, bool torus) {
   if (torus) return (size_t)3 << V.row_bits;
-  return (size_t)2 * V.n_chunks * 256 * sizeof(uint64_t);
+  return (size_t)V.n_perm * V.n_chunks * 256 * sizeof(uint64_t);
 }
 
 int grid_for(const void* kernel, size_t smem, int64_t work_items) {
@@ -363,7 +365,7 @@ cudaError_t build_basis(Sector& S, std::string& err) {
 }
 
 cudaError_t export_walk_tables(const Sector& S, int64_t* rep_loc_dev, int32_t* g_dev, cudaStream_t st) {
-  const size_t smem = (size_t)2 * S.V.n_chunks * 256 * sizeof(uint64_t);
+  const size_t smem = (size_t)S.V.n_perm * S.V.n_chunks * 256 * sizeof(uint64_t);
   cudaFuncSetAttribute(k_walk_tables, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   k_walk_tables<<<grid_for((const void*)k_walk_tables, smem, S.P.n_configs), kBuildThreads, smem, st>>>(S.V, rep_loc_dev,
                                                                                                   g_dev);

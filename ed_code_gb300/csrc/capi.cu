@@ -84,22 +84,31 @@ static uint64_t binomial(int n, int k) {
   return r;
 }
 
-static int create_sector(const edg_model* m, int n_ones, int kx, int ky, Sector& S) {
+static int create_sector(const edg_model* m, int n_ones, int kx, int ky, int kz, Sector& S) {
   if (!m || !m->T1 || !m->T2) return fail(EDG_ERR_INVALID, "model or T1/T2 missing");
   const int N = m->n_sites;
   if (N < 2 || N > kMaxSites) return fail(EDG_ERR_UNSUPPORTED, "n_sites must be in [2, 40]");
   if (N % 2) return fail(EDG_ERR_UNSUPPORTED, "odd n_sites: the reference's split_id/bits_right disagree for odd N");
   if (n_ones < 0 || n_ones > N) return fail(EDG_ERR_INVALID, "n_ones out of range");
   if (!is_perm(m->T1, N) || !is_perm(m->T2, N)) return fail(EDG_ERR_INVALID, "T1/T2 must be permutations of the sites");
+  if (m->T3 && !is_perm(m->T3, N)) return fail(EDG_ERR_INVALID, "T3 must be a permutation of the sites");
   S.T1.assign(m->T1, m->T1 + N);
   S.T2.assign(m->T2, m->T2 + N);
+  if (m->T3) S.T3.assign(m->T3, m->T3 + N);
   S.lambda = m->lambda;
   S.Ch = m->Ch;
   S.ChCh = m->ChCh;
-  int L1, L2;
+  int L1, L2, L3 = 1;
   lxly(S.T1, S.T2, L1, L2);
-  if (kx >= L1 || ky >= L2 || kx < 0 || ky < 0) return fail(EDG_ERR_MOMENTUM, "Invalid kx or ky");
-  if (L1 * L2 > 64) return fail(EDG_ERR_UNSUPPORTED, "L1*L2 > 64 translations");
+  if (m->T3) {  // LxLyLz (Momentum_Basis.cpp:38-63): the cycle length of site 0
+    L3 = 0;
+    int s = 0;
+    do { s = S.T3[s]; ++L3; } while (s != 0);
+  }
+  // Lanczos_sector.cpp:50-55 (2-D), :234-238 (3-D)
+  if (kx >= L1 || ky >= L2 || kz >= L3 || kx < 0 || ky < 0 || kz < 0)
+    return fail(EDG_ERR_MOMENTUM, "Invalid kx or ky");
+  if (L1 * L2 * L3 > 64) return fail(EDG_ERR_UNSUPPORTED, "L1*L2*L3 > 64 translations");
 
   SectorParams& P = S.P;
   std::memset(&P, 0, sizeof(P));
@@ -110,16 +119,18 @@ static int create_sector(const edg_model* m, int n_ones, int kx, int ky, Sector&
   P.L2 = L2;
   P.kx = kx;
   P.ky = ky;
+  P.L3 = L3;
+  P.kz = kz;
   P.full_mask = (N == 64) ? ~0ull : ((1ull << N) - 1ull);
   P.right_mask = (1ull << P.half) - 1ull;
   P.n_configs = (int64_t)binomial(N, n_ones);
   P.n_recs = (P.n_configs + kRecBits - 1) / kRecBits;
   P.ChCh = m->ChCh;
 
-  // Row-major torus test: T1 = +x, T2 = +y with Lx = L1, Ly = L2.
+  // Row-major torus test: T1 = +x, T2 = +y with Lx = L1, Ly = L2 (2-D only).
   {
     const int Lx = L1, Ly = L2;
-    bool t = (Lx * Ly == N) && Lx >= 2 && Lx <= kMaxTorusRow && Ly <= 16;
+    bool t = !m->T3 && (Lx * Ly == N) && Lx >= 2 && Lx <= kMaxTorusRow && Ly <= 16;
     for (int s = 0; t && s < N; ++s) {
       const int x = s % Lx, y = s / Lx;
       if (S.T1[s] != (x + 1) % Lx + Lx * y) t = false;
@@ -128,23 +139,27 @@ static int create_sector(const edg_model* m, int n_ones, int kx, int ky, Sector&
     P.torus = t ? 1 : 0;
   }
 
-  // Phases exp(-i(px*lx + py*ly)) for the translation (a, b) from a state to
-  // its representative, lx = (L1-a)%L1, ly = (L2-b)%L2 (Momentum_Basis.cpp:
-  // 747-753; px, py as Lanczos_sector.cpp:57).
-  const double px = 2 * kx * kPi / L1, py = 2 * ky * kPi / L2;
-  for (int b = 0; b < L2; ++b)
-    for (int a = 0; a < L1; ++a) {
-      const int lx = (L1 - a) % L1, ly = (L2 - b) % L2;
-      const std::complex<double> ph = std::exp(std::complex<double>(0.0, -px * lx - py * ly));
-      P.ph_re[a + L1 * b] = ph.real();
-      P.ph_im[a + L1 * b] = ph.imag();
-    }
+  // Phases exp(-i(px*lx + py*ly [+ pz*lz])) for the translation (a, b, c)
+  // from a state to its representative, lx = (L1-a)%L1, ly = (L2-b)%L2,
+  // lz = (L3-c)%L3, with the reference's expressions (Momentum_Basis.cpp:
+  // 747-753 and :861-872; px, py, pz as Lanczos_sector.cpp:57 and :240).
+  const double px = 2 * kx * kPi / L1, py = 2 * ky * kPi / L2, pz = 2 * kz * kPi / L3;
+  for (int c = 0; c < L3; ++c)
+    for (int b = 0; b < L2; ++b)
+      for (int a = 0; a < L1; ++a) {
+        const int lx = (L1 - a) % L1, ly = (L2 - b) % L2, lz = (L3 - c) % L3;
+        const std::complex<double> ph =
+            m->T3 ? std::exp(std::complex<double>(0.0, -px * lx - py * ly - pz * lz))
+                  : std::exp(std::complex<double>(0.0, -px * lx - py * ly));
+        P.ph_re[a + L1 * b + L1 * L2 * c] = ph.real();
+        P.ph_im[a + L1 * b + L1 * L2 * c] = ph.imag();
+      }
+  const int G = L1 * L2 * L3;
   for (int lid = 1; lid <= 64; ++lid) {
-    const int64_t n = (int64_t)(L1 * L2) / lid;  // integer division as Momentum_Basis.cpp:764
+    const int64_t n = (int64_t)G / lid;  // integer division as Momentum_Basis.cpp:764, :883
     P.nrm[lid] = n > 0 ? std::sqrt((double)n) : 0.0;
     P.nrm_inv[lid] = n > 0 ? 1 / std::sqrt((double)n) : 0.0;
   }
-  const int G = L1 * L2;
   for (int k = 0; k < G; ++k) {
     P.chi_re[k] = std::cos(2 * kPi * k / G);
     P.chi_im[k] = -std::sin(2 * kPi * k / G);
@@ -355,9 +370,10 @@ static int create_sector(const edg_model* m, int n_ones, int kx, int ky, Sector&
     }
   }
   const int n_chunks = (N + 7) / 8;
-  std::vector<uint64_t> perms(2 * n_chunks * 256, 0);
-  for (int which = 0; which < 2; ++which) {
-    const std::vector<int>& T = which ? S.T2 : S.T1;
+  const int n_perm = m->T3 ? 3 : 2;
+  std::vector<uint64_t> perms((size_t)n_perm * n_chunks * 256, 0);
+  for (int which = 0; which < n_perm; ++which) {
+    const std::vector<int>& T = which == 0 ? S.T1 : (which == 1 ? S.T2 : S.T3);
     for (int c = 0; c < n_chunks; ++c)
       for (int byte = 0; byte < 256; ++byte) {
         uint64_t out = 0;
@@ -413,6 +429,7 @@ static int create_sector(const edg_model* m, int n_ones, int kx, int ky, Sector&
   V.perms = S.perms;
   V.binom = S.binom;
   V.n_chunks = n_chunks;
+  V.n_perm = n_perm;
   V.row_bits = row_bits;
 
   std::string err;
@@ -450,13 +467,13 @@ extern "C" {
 const char* edg_last_error(void) { return g_last_error.c_str(); }
 int edg_abi_version(void) { return EDGPU_ABI_VERSION; }
 
-int edg_sector_create(const edg_model* model, int n_ones, int kx, int ky, edg_sector** out) {
+int edg_sector_create3(const edg_model* model, int n_ones, int kx, int ky, int kz, edg_sector** out) {
   if (!out) return fail(EDG_ERR_INVALID, "out is NULL");
   *out = nullptr;
   if (!model || !model->T1 || !model->T2) return fail(EDG_ERR_INVALID, "model or T1/T2 missing");
   edg_sector* h = new edg_sector();
   cudaGetDevice(&h->s.device);
-  int rc = create_sector(model, n_ones, kx, ky, h->s);
+  int rc = create_sector(model, n_ones, kx, ky, kz, h->s);
   if (rc != EDG_OK) {
     free_sector(h->s);
     delete h;
@@ -464,6 +481,11 @@ int edg_sector_create(const edg_model* model, int n_ones, int kx, int ky, edg_se
   }
   *out = h;
   return EDG_OK;
+}
+
+int edg_sector_create(const edg_model* model, int n_ones, int kx, int ky, edg_sector** out) {
+  if (model && model->T3) return fail(EDG_ERR_INVALID, "a model with T3 needs edg_sector_create3 (kz)");
+  return edg_sector_create3(model, n_ones, kx, ky, 0, out);
 }
 
 int edg_sector_destroy(edg_sector* s) {
@@ -482,6 +504,8 @@ int edg_sector_get_info(const edg_sector* s, edg_sector_info* info) {
   info->L2 = P.L2;
   info->kx = P.kx;
   info->ky = P.ky;
+  info->L3 = P.L3;
+  info->kz = P.kz;
   info->torus = P.torus;
   info->n_groups = P.n_groups;
   info->n_p = P.n_p;
@@ -558,7 +582,7 @@ int edg_sector_copy_config_tables(const edg_sector* s, int64_t max_configs, int6
   if (e != cudaSuccess) return cuda_fail(e, "config tables");
   const int L1 = S.P.L1, L2 = S.P.L2;
   for (int64_t i = 0; i < nc; ++i) {
-    const int a = g[i] % L1, b = g[i] / L1;
+    const int a = g[i] % L1, b = (g[i] / L1) % L2;
     if (state_ph) {
       state_ph[2 * i] = S.P.ph_re[g[i]];
       state_ph[2 * i + 1] = S.P.ph_im[g[i]];

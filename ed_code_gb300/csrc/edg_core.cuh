@@ -3,7 +3,7 @@
 //
 // Reference path (hiteshjc/ED_Code, src/):
 //   translateT / LxLy ............ Momentum_Basis.cpp:4-36
-//   representative_p ............. Momentum_Basis.cpp:472-543
+//   representative_p ............. Momentum_Basis.cpp:472-543 (2-D), :545-643 (3-D)
 //   Lin_Tables / split_id ........ Lin_Tables.cpp:42-78, Momentum_Basis.cpp:731-737
 //   sHv row formula .............. H_v.cpp:218-355
 //
@@ -94,23 +94,25 @@ struct SectorParams {
   int n_sites, n_ones, half;        // half = N/2 (even N only)
   int L1, L2;
   int kx, ky;
+  int L3, kz;                       // third translation of a 3-D torus (L3 = 1, kz = 0 in 2-D)
   int torus;                        // 1: row-major torus T1=+x, T2=+y (Lx=L1, Ly=L2)
   int n_groups, n_ch, n_bowties;
   int use_ch, use_chch;
-  int pad0;
+  int pad0, pad1;
   int64_t n_p, n_configs, n_recs;   // n_recs: Lin-indexed records used while building
   int64_t n_vrecs;                  // value-indexed rank records (see value_rank)
   uint64_t full_mask, right_mask;
   double total_fac;                 // sum over bonds of 0.25*lambda*J
   double ChCh;
-  // Phase for translation (a, b) = T1^a T2^b from a state to its
-  // representative: exp(-i(px*lx + py*ly)), lx=(L1-a)%L1, ly=(L2-b)%L2,
-  // evaluated on the host with the reference's expression (Momentum_Basis.cpp:753).
+  // Phase for translation g = a + L1 b + L1 L2 c (T1^a T2^b T3^c) from a
+  // state to its representative: exp(-i(px*lx + py*ly + pz*lz)),
+  // lx=(L1-a)%L1, ly=(L2-b)%L2, lz=(L3-c)%L3, evaluated on the host with the
+  // reference's expression (Momentum_Basis.cpp:753, :872).
   double ph_re[64], ph_im[64];
-  // Norm tables by stabiliser count: sqrt(L1*L2/lid) and its inverse, with the
-  // reference's integer division (Momentum_Basis.cpp:764-766).
+  // Norm tables by stabiliser count: sqrt(G/lid) and its inverse, G = L1 L2 L3,
+  // with the reference's integer division (Momentum_Basis.cpp:764-766, :883).
   double nrm[65], nrm_inv[65];
-  // e^{-2 pi i m/(L1 L2)}: character values for the p_id test.
+  // e^{-2 pi i m/G}: character values for the p_id test.
   double chi_re[64], chi_im[64];
   // Torus search tables (row length Lx = L1, Ly = L2 rows).
   uint64_t rot_hi[kMaxTorusRow], rot_lo[kMaxTorusRow];  // per-row masks of bits x >= a / x < a
@@ -199,7 +201,7 @@ EDG_HD int64_t rank_lookup(int64_t lin, const RankRec& rec) {
 // --------------------------------------------------------------------------
 struct Orbit {
   uint64_t rep;  // smallest translate
-  int g;         // translation index a + L1*b with rep = T1^a T2^b t
+  int g;         // translation index a + L1*b + L1*L2*c with rep = T1^a T2^b T3^c t
   int stab;      // number of translations mapping t to itself
 };
 
@@ -210,37 +212,46 @@ EDG_HD uint64_t apply_perm(uint64_t t, const uint64_t* perm, int n_chunks) {
   return out;
 }
 
-// The reference's literal walk (Momentum_Basis.cpp:493-535): for x < L1
-// { if x>0 apply T1; for y < L2 { if y>0 apply T2 } }, first strict minimum
-// wins.  Works for any T1/T2.  tx, ty are the walk's step counts at the
-// minimum, reduced mod L1/L2 into g.  chi_sum (optional) accumulates the
-// p_id phase sum over walk positions equal to t.
+// The reference's literal walk (Momentum_Basis.cpp:493-535, 3-D :566-634):
+// for x < L1 { if x>0 apply T1; for y < L2 { if y>0 apply T2; for z < L3
+// { if z>0 apply T3 } } }, first strict minimum wins.  Works for any
+// T1/T2/T3; with L3 = 1 (2-D) the z loop applies nothing.  tx, ty, tz are
+// the walk's step counts at the minimum, reduced mod L1/L2/L3 into g.
+// chi_sum (optional) accumulates the p_id phase sum over walk positions
+// equal to t.
 EDG_HD Orbit orbit_walk(uint64_t t, const SectorParams& P, const uint64_t* perm1, const uint64_t* perm2,
-                        int n_chunks, double* chi_re_sum = nullptr, double* chi_im_sum = nullptr) {
+                        const uint64_t* perm3, int n_chunks, double* chi_re_sum = nullptr,
+                        double* chi_im_sum = nullptr) {
   Orbit o{t, 0, 1};
   uint64_t tmp = t;
-  int tx = 0, ty = 0;
-  const int G = P.L1 * P.L2;
+  int tx = 0, ty = 0, tz = 0;
+  const int G = P.L1 * P.L2 * P.L3;
   double cr = 1.0, ci = 0.0;
   for (int x = 0; x < P.L1; ++x) {
     for (int y = 0; y < P.L2; ++y) {
-      if (x == 0 && y == 0) continue;
-      if (y == 0) {
-        tmp = apply_perm(tmp, perm1, n_chunks);
-        ++tx;
-      } else {
-        tmp = apply_perm(tmp, perm2, n_chunks);
-        ++ty;
-      }
-      if (tmp == t) {
-        ++o.stab;
-        int m = (int)(((int64_t)P.kx * tx * P.L2 + (int64_t)P.ky * ty * P.L1) % G);
-        cr += P.chi_re[m];
-        ci += P.chi_im[m];
-      }
-      if (tmp < o.rep) {
-        o.rep = tmp;
-        o.g = (tx % P.L1) + P.L1 * (ty % P.L2);
+      for (int z = 0; z < P.L3; ++z) {
+        if (x == 0 && y == 0 && z == 0) continue;
+        if (z > 0) {
+          tmp = apply_perm(tmp, perm3, n_chunks);
+          ++tz;
+        } else if (y > 0) {
+          tmp = apply_perm(tmp, perm2, n_chunks);
+          ++ty;
+        } else {
+          tmp = apply_perm(tmp, perm1, n_chunks);
+          ++tx;
+        }
+        if (tmp == t) {
+          ++o.stab;
+          int m = (int)(((int64_t)P.kx * tx * P.L2 * P.L3 + (int64_t)P.ky * ty * P.L1 * P.L3 +
+                         (int64_t)P.kz * tz * P.L1 * P.L2) % G);
+          cr += P.chi_re[m];
+          ci += P.chi_im[m];
+        }
+        if (tmp < o.rep) {
+          o.rep = tmp;
+          o.g = (tx % P.L1) + P.L1 * (ty % P.L2) + P.L1 * P.L2 * (tz % P.L3);
+        }
       }
     }
   }
@@ -251,13 +262,20 @@ EDG_HD Orbit orbit_walk(uint64_t t, const SectorParams& P, const uint64_t* perm1
 // Early-exit test used by the basis build: is t smaller than every other
 // translate (ties allowed)?  Any order of translates works.
 EDG_HD bool walk_is_min(uint64_t t, const SectorParams& P, const uint64_t* perm1, const uint64_t* perm2,
-                        int n_chunks) {
+                        const uint64_t* perm3, int n_chunks) {
   uint64_t row = t;
   for (int x = 0; x < P.L1; ++x) {
-    uint64_t tmp = row;
-    for (int y = 1; y < P.L2; ++y) {
-      tmp = apply_perm(tmp, perm2, n_chunks);
-      if (tmp < t) return false;
+    uint64_t col = row;
+    for (int y = 0; y < P.L2; ++y) {
+      if (y > 0) {
+        col = apply_perm(col, perm2, n_chunks);
+        if (col < t) return false;
+      }
+      uint64_t tmp = col;
+      for (int z = 1; z < P.L3; ++z) {
+        tmp = apply_perm(tmp, perm3, n_chunks);
+        if (tmp < t) return false;
+      }
     }
     row = apply_perm(row, perm1, n_chunks);
     if (x + 1 < P.L1 && row < t) return false;
@@ -351,10 +369,10 @@ EDG_HD int torus_allowed(uint64_t t, const SectorParams& P, const uint8_t* nk, c
 }
 
 EDG_HD int walk_allowed(uint64_t t, const SectorParams& P, const uint64_t* perm1, const uint64_t* perm2,
-                        int n_chunks) {
-  if (!walk_is_min(t, P, perm1, perm2, n_chunks)) return 0;
+                        const uint64_t* perm3, int n_chunks) {
+  if (!walk_is_min(t, P, perm1, perm2, perm3, n_chunks)) return 0;
   double cr, ci;
-  Orbit o = orbit_walk(t, P, perm1, perm2, n_chunks, &cr, &ci);
+  Orbit o = orbit_walk(t, P, perm1, perm2, perm3, n_chunks, &cr, &ci);
   if (o.rep != t) return 0;
   bool pid = (cr > 1e-8 || cr < -1e-8 || ci > 1e-8 || ci < -1e-8);
   return pid ? o.stab : 0;

@@ -26,9 +26,10 @@ struct SectorView {
   const Bowtie* bows;
   const uint8_t* nk;       // torus: rotation minimum of each row value
   const uint16_t* rots;    // torus: rotations reaching it
-  const uint64_t* perms;   // walk: 2 x n_chunks x 256 permutation chunk tables
+  const uint64_t* perms;   // walk: n_perm x n_chunks x 256 permutation chunk tables (T1, T2[, T3])
   const uint64_t* binom;   // (kMaxSites+1)^2 binomials
   int n_chunks;
+  int n_perm;              // 2, or 3 on a 3-D torus
   int row_bits;            // torus: Lx (table size 2^Lx)
 };
 
@@ -74,7 +75,7 @@ struct Sector {
   uint64_t* binom = nullptr;
   size_t device_bytes = 0;
   // host copies used by the adapters
-  std::vector<int> T1, T2;
+  std::vector<int> T1, T2, T3;  // T3 empty in 2-D
   double lambda = 1, Ch = 0, ChCh = 0;
   // scratch kept for host-buffer H*v calls
   DeviceBuffer host_in, host_out;

@@ -175,7 +175,7 @@ int persistent_grid(K kernel, size_t smem, int64_t rows) {
 template <typename Real, bool kTorus, bool kChCh>
 cudaError_t launch_t(const Sector& S, const void* v, void* w, cudaStream_t st) {
   using CT = typename C2<Real>::T;
-  const size_t smem = hv_smem_bytes<Real>(S.P.n_groups, S.P.n_ch, kTorus, S.V.row_bits, S.V.n_chunks);
+  const size_t smem = hv_smem_bytes<Real>(S.P.n_groups, S.P.n_ch, kTorus, S.V.row_bits, S.V.n_chunks, S.V.n_perm);
   auto kern = k_hv<Real, kTorus, kChCh>;
   const int grid = persistent_grid(kern, smem, S.P.n_p);
   kern<<<grid, kHvThreads, smem, st>>>(S.V, reinterpret_cast<const CT*>(v), reinterpret_cast<CT*>(w));
@@ -202,7 +202,7 @@ cudaError_t launch_hv_generic(const Sector& S, const void* v, void* w, bool fp64
 
 cudaError_t count_offdiag(const Sector& S, unsigned long long* nnz_dev, cudaStream_t st) {
   const bool torus = S.P.torus != 0;
-  const size_t smem = hv_smem_bytes<float>(S.P.n_groups, S.P.n_ch, torus, S.V.row_bits, S.V.n_chunks);
+  const size_t smem = hv_smem_bytes<float>(S.P.n_groups, S.P.n_ch, torus, S.V.row_bits, S.V.n_chunks, S.V.n_perm);
   cudaMemsetAsync(nnz_dev, 0, sizeof(unsigned long long), st);
   if (torus) {
     const int grid = persistent_grid(k_count_offdiag<true>, smem, S.P.n_p);

@@ -29,17 +29,19 @@ struct HvSmem {
   const uint16_t* rots;
   const uint64_t* p1;
   const uint64_t* p2;
+  const uint64_t* p3;  // T3 (3-D tori only)
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
 template <typename Real>
-__host__ __device__ inline size_t hv_smem_bytes(int n_groups, int n_ch, bool torus, int row_bits, int n_chunks) {
+__host__ __device__ inline size_t hv_smem_bytes(int n_groups, int n_ch, bool torus, int row_bits, int n_chunks,
+                                                int n_perm) {
   size_t b = align16(sizeof(SmemGroup<Real>) * n_groups);
   b += align16(sizeof(SmemCh<Real>) * n_ch);
   b += align16(sizeof(Real) * (64 + 64 + 65 + 65));
   if (torus) b += align16((size_t)3 << row_bits);
-  else b += (size_t)2 * n_chunks * 256 * sizeof(uint64_t);
+  else b += (size_t)n_perm * n_chunks * 256 * sizeof(uint64_t);
   return b;
 }
 
@@ -102,11 +104,12 @@ __device__ HvSmem<Real> stage_hv(const SectorView& V, const SectorParams& P, uin
     H.nk = nk;
     H.rots = rots;
   } else {
-    const int n = 2 * V.n_chunks * 256;
+    const int n = V.n_perm * V.n_chunks * 256;
     uint64_t* p = reinterpret_cast<uint64_t*>(sm + off);
     for (int i = threadIdx.x; i < n; i += blockDim.x) p[i] = V.perms[i];
     H.p1 = p;
     H.p2 = p + V.n_chunks * 256;
+    H.p3 = p + 2 * V.n_chunks * 256;
   }
   return H;
 }
@@ -114,7 +117,7 @@ __device__ HvSmem<Real> stage_hv(const SectorView& V, const SectorParams& P, uin
 template <typename Real, bool kTorus>
 __device__ __forceinline__ Orbit search(uint64_t t, const SectorParams& P, const HvSmem<Real>& H, int n_chunks) {
   if (kTorus) return orbit_torus(t, P, H.nk, H.rots);
-  return orbit_walk(t, P, H.p1, H.p2, n_chunks);
+  return orbit_walk(t, P, H.p1, H.p2, H.p3, n_chunks);
 }
 
 // Position j of the representative o.rep; j < 0 when it is not an allowed

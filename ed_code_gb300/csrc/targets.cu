@@ -820,23 +820,27 @@ int build_targets(Sector& S, int64_t max_bytes, std::string& err) {
   std::vector<ChTerm> ch(P.n_ch);
   cudaMemcpy(groups.data(), S.groups, sizeof(TermGroup) * groups.size(), cudaMemcpyDeviceToHost);
   if (!ch.empty()) cudaMemcpy(ch.data(), S.ch, sizeof(ChTerm) * ch.size(), cudaMemcpyDeviceToHost);
-  // phase classes: translation (a, b) has phase index (kx a L2 + ky b L1) mod G
-  const int G = P.L1 * P.L2;
-  const int64_t d = gcd64(gcd64((int64_t)P.kx * P.L2, (int64_t)P.ky * P.L1), G);
+  // phase classes: translation (a, b, c) has phase index
+  // (kx a L2 L3 + ky b L1 L3 + kz c L1 L2) mod G, G = L1 L2 L3 (c = 0 in 2-D)
+  const int G = P.L1 * P.L2 * P.L3;
+  const int64_t d = gcd64(gcd64(gcd64((int64_t)P.kx * P.L2 * P.L3, (int64_t)P.ky * P.L1 * P.L3),
+                                (int64_t)P.kz * P.L1 * P.L2), G);
   const int n_cls = (int)(G / (d ? d : G));
   std::vector<std::complex<double>> cph(n_cls);
   std::vector<char> seen(n_cls, 0);
-  for (int b = 0; b < P.L2; ++b)
-    for (int a = 0; a < P.L1; ++a) {
-      const int g = a + P.L1 * b;
-      const int64_t m = ((int64_t)P.kx * a * P.L2 + (int64_t)P.ky * b * P.L1) % G;
-      const int c = (int)(m / (d ? d : G));
-      P.g2cls[g] = (uint8_t)c;
-      if (!seen[c]) {  // the first translation of a class gives its phase value
-        seen[c] = 1;
-        cph[c] = std::complex<double>(P.ph_re[g], P.ph_im[g]);
+  for (int c3 = 0; c3 < P.L3; ++c3)
+    for (int b = 0; b < P.L2; ++b)
+      for (int a = 0; a < P.L1; ++a) {
+        const int g = a + P.L1 * b + P.L1 * P.L2 * c3;
+        const int64_t m = ((int64_t)P.kx * a * P.L2 * P.L3 + (int64_t)P.ky * b * P.L1 * P.L3 +
+                           (int64_t)P.kz * c3 * P.L1 * P.L2) % G;
+        const int c = (int)(m / (d ? d : G));
+        P.g2cls[g] = (uint8_t)c;
+        if (!seen[c]) {  // the first translation of a class gives its phase value
+          seen[c] = 1;
+          cph[c] = std::complex<double>(P.ph_re[g], P.ph_im[g]);
+        }
       }
-    }
   P.n_cls = n_cls;
   // value table: for each group, every (bit a, chirality z bits) variant
   std::vector<uint16_t> voff(P.n_groups);
@@ -909,7 +913,7 @@ int build_targets(Sector& S, int64_t max_bytes, std::string& err) {
     return EDG_ERR_NOMEM;
   }
   const bool torus = P.torus != 0;
-  const size_t smem = hv_smem_bytes<double>(P.n_groups, P.n_ch, torus, S.V.row_bits, S.V.n_chunks);
+  const size_t smem = hv_smem_bytes<double>(P.n_groups, P.n_ch, torus, S.V.row_bits, S.V.n_chunks, S.V.n_perm);
   const int nw = n_words(P.n_groups);
   auto pass = [&](auto kern, bool fill) {
     kern<<<grid_for(kern, smem, n * 32, kTgtThreads), kTgtThreads, smem, st>>>(

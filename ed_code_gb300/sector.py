@@ -29,9 +29,10 @@ def _model_struct(model: Model):
     # the library ignores the bowties when ChCh is 0, so they are not copied then
     chch = model.chch_list if abs(model.ChCh) > 1e-16 else []
     bows = (N.edg_bowtie * max(1, len(chch)))(*[N.edg_bowtie(b.x, b.y, b.z, b.p, b.q, b.r) for b in chch])
+    T3 = (C.c_int * n)(*model.T3) if getattr(model, "T3", None) else None
     m = N.edg_model(n, T1, T2, model.Jz, bonds, len(model.adj_list), model.Ch, tris, len(model.ch_list),
-                    model.ChCh, bows, len(chch))
-    return m, [T1, T2, bonds, tris, bows]
+                    model.ChCh, bows, len(chch), T3)
+    return m, [T1, T2, T3, bonds, tris, bows]
 
 
 class GpuSector:
@@ -42,7 +43,11 @@ class GpuSector:
         self.n_ones = model.n_ones if n_ones is None else int(n_ones)
         m, self._keep = _model_struct(model)
         h = C.c_void_p()
-        N.check(N.lib().edg_sector_create(C.byref(m), self.n_ones, int(model.kx), int(model.ky), C.byref(h)))
+        if getattr(model, "T3", None):
+            N.check(N.lib().edg_sector_create3(C.byref(m), self.n_ones, int(model.kx), int(model.ky), int(model.kz),
+                                               C.byref(h)))
+        else:
+            N.check(N.lib().edg_sector_create(C.byref(m), self.n_ones, int(model.kx), int(model.ky), C.byref(h)))
         self._h = h
         info = N.edg_sector_info()
         N.check(N.lib().edg_sector_get_info(self._h, C.byref(info)))

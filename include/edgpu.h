@@ -17,7 +17,7 @@
 extern "C" {
 #endif
 
-#define EDGPU_ABI_VERSION 3
+#define EDGPU_ABI_VERSION 4
 
 enum {
   EDG_OK = 0,
@@ -53,6 +53,8 @@ typedef struct {
   double ChCh;
   const edg_bowtie* bowties;
   int n_bowties;
+  const int* T3;         /* third translation of a 3-D torus (ED_3D_Lattice_Geometry,
+                            read_input_file.cpp:443); NULL for 2-D */
 } edg_model;
 
 typedef struct edg_sector edg_sector;
@@ -68,6 +70,7 @@ typedef struct {
   int lanes_per_row;     /* stored-row H*v: lanes of a warp per row (edg_sector_tune) */
   int cache_policy;      /* stored-row H*v: 1 streaming row loads, 2 L2 evict-first row loads */
   int panels;            /* column panels of the stored rows (0: row order) */
+  int L3, kz;            /* third translation's cycle length and momentum (1, 0 in 2-D) */
 } edg_sector_info;
 
 const char* edg_last_error(void);
@@ -79,6 +82,13 @@ int edg_abi_version(void);
  * (Lanczos_sector.cpp:48-97).  Errors: EDG_ERR_MOMENTUM, EDG_ERR_EMPTY as the
  * reference's exit(1) paths (Lanczos_sector.cpp:51-55, 93-97). */
 int edg_sector_create(const edg_model* model, int n_ones, int kx, int ky, edg_sector** out);
+/* Same for a 3-D torus (model->T3 set) with momentum (kx, ky, kz).
+ * Replaces: LxLyLz + the 3-D pConstruct_States (Momentum_Basis.cpp:38-63,
+ * 781-895) as called from the 3-D sector_lanczos (Lanczos_sector.cpp:201-257);
+ * the orbit walk, phases exp(-i(px lx + py ly + pz lz)) and norms
+ * sqrt(L1 L2 L3 / lid) follow representative_p (Momentum_Basis.cpp:545-643).
+ * With model->T3 == NULL and kz == 0 it is edg_sector_create. */
+int edg_sector_create3(const edg_model* model, int n_ones, int kx, int ky, int kz, edg_sector** out);
 int edg_sector_destroy(edg_sector* s);
 int edg_sector_get_info(const edg_sector* s, edg_sector_info* info);
 

@@ -71,3 +71,34 @@ def test_solver_log_lines(gpu):
     sec.solve_plain(n_ev=1, iterations=30, ncycles=3, tol=1e-12, dense_threshold=-1, log=lines.append)
     assert any(l.startswith("Eigs[0]") for l in lines)
     assert any(l.startswith("Eigenvalue number 0") for l in lines)
+
+
+@pytest.mark.parametrize("name,idx", [("cub3x2x2", 1), ("cub4x2x2", 0), ("cub4x2x2", 1)])
+def test_three_d_torus_spectrum(name, idx, cuda_device):
+    """3-D tori: the plain solver (dense path) and the mixed solver against the
+    oracle's dense spectrum, whose H matches the reference's 3-D sHv."""
+    import oracle as O
+    from ed_code_gb300 import sector
+
+    model = golden_model(name, idx)
+    assert model.T3
+    ev = np.linalg.eigvalsh(O.OracleSector(model).dense())
+    sec = sector.GpuSector(model)
+    assert sec.info["L3"] == 2 and sec.info["kz"] == model.kz
+    eigs, _, _ = sec.solve_plain(n_ev=3)
+    np.testing.assert_allclose(eigs[:3], ev[:3], rtol=1e-10)
+    assert sec.build_targets()
+    out = sec.solve_mixed(n_ev=2, iterations=min(150, sec.n_p), reorth_every=1)
+    levels = [ev[0]] + [x for x in ev[1:] if abs(x - ev[0]) > 1e-9 * abs(x)]
+    np.testing.assert_allclose(out["eigs"][0], levels[0], rtol=1e-9)
+
+
+def test_three_d_momentum_out_of_range(cuda_device):
+    from ed_code_gb300 import lattice as L
+    from ed_code_gb300 import sector
+    from ed_code_gb300._native import EdgError
+
+    m = L.make_model(L.TorusSpec("cubic", 3, 2, Lz=2, Jz=0.9), 0, 0, 0, kz=0)
+    m.kz = 2
+    with pytest.raises(EdgError, match="Invalid kx or ky"):
+        sector.GpuSector(m)
