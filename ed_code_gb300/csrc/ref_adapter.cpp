@@ -75,15 +75,17 @@ uint64_t translate(uint64_t s, const std::vector<int>& T) {
   return out;
 }
 
-// Unwrap_pState (Momentum_Basis.cpp:978-1037): expand a momentum eigenvector
-// into the fixed-Sz basis by walking each representative's orbit with the
-// reference's walk order and phases, merging repeated states, dropping
-// coefficients below 1e-8 and sorting by state.
+// Unwrap_pState (Momentum_Basis.cpp:978-1037; 3-D :901-976): expand a
+// momentum eigenvector into the fixed-Sz basis by walking each
+// representative's orbit with the reference's walk order and phases, merging
+// repeated states, dropping coefficients below 1e-8 and sorting by state.
+// T3 == nullptr is the 2-D walk.
 std::vector<std::pair<int64_t, cplx>> unwrap(const std::vector<cplx>& coeff, const std::vector<int64_t>& reps,
-                                             const std::vector<double>& norm, double px, double py, int L1, int L2,
-                                             const std::vector<int>& T1, const std::vector<int>& T2) {
+                                             const std::vector<double>& norm, double px, double py, double pz, int L1,
+                                             int L2, int L3, const std::vector<int>& T1, const std::vector<int>& T2,
+                                             const std::vector<int>* T3) {
   std::vector<std::pair<int64_t, cplx>> out;
-  const cplx ex = std::exp(cplx(0.0, -px)), ey = std::exp(cplx(0.0, -py));
+  const cplx ex = std::exp(cplx(0.0, -px)), ey = std::exp(cplx(0.0, -py)), ez = std::exp(cplx(0.0, -pz));
   for (size_t i = 0; i < reps.size(); ++i) {
     std::vector<std::pair<int64_t, cplx>> loc;
     auto add = [&](int64_t id, cplx c) {
@@ -103,10 +105,17 @@ std::vector<std::pair<int64_t, cplx>> unwrap(const std::vector<cplx>& coeff, con
         ph = ph * ex;
         add((int64_t)v, coeff[i] * ph / norm[i]);
       }
-      for (int y = 1; y < L2; ++y) {
-        v = translate(v, T2);
-        ph = ph * ey;
-        add((int64_t)v, coeff[i] * ph / norm[i]);
+      for (int y = 0; y < L2; ++y) {
+        if (y > 0) {
+          v = translate(v, T2);
+          ph = ph * ey;
+          add((int64_t)v, coeff[i] * ph / norm[i]);
+        }
+        for (int z = 1; z < L3 && T3; ++z) {
+          v = translate(v, *T3);
+          ph = ph * ez;
+          add((int64_t)v, coeff[i] * ph / norm[i]);
+        }
       }
     }
     for (auto& e : loc)
@@ -127,36 +136,48 @@ void solve_sector(int kx, int ky, double cSz, int n_spins, double lambda, double
                   const std::vector<coordinates>& adj_list, double Ch, const std::vector<triangles>& ch_list,
                   double ChCh, const std::vector<bowties>& chch_list, const std::vector<int>& T1,
                   const std::vector<int>& T2, int n_sec_ev, bool find_ev, bool unwrap_peigvec,
-                  const std::string& filepath_EV, double tol, int iterations, int ncycles, std::ofstream& outfile) {
+                  const std::string& filepath_EV, double tol, int iterations, int ncycles, std::ofstream& outfile,
+                  const std::vector<int>* T3 = nullptr, int kz = 0) {
+  // T3 != nullptr: the 3-D overload (Lanczos_sector.cpp:201-369)
   int n_ones = int(cSz + n_spins / 2 + 1.0e-6);  // Lanczos_sector.cpp:45-46
-  if ((int)T1.size() != n_spins || (int)T2.size() != n_spins) die(outfile, "\nERROR: input T1 != T2\n");
+  if ((int)T1.size() != n_spins || (int)T2.size() != n_spins || (T3 && (int)T3->size() != n_spins))
+    die(outfile, "\nERROR: input T1 != T2\n");
   ModelArrays ma;
   fill_model(ma, n_spins, T1, T2, lambda, adj_list, Ch, ch_list, ChCh, chch_list);
+  if (T3) ma.m.T3 = T3->data();
   const double Sz = 0.5 * n_ones - 0.5 * (n_spins - n_ones);
   outfile << "\n--------------------------------------------------------------------\n";
   double t_states = now_seconds();
   outfile.flush();
   edg_sector* sec = nullptr;
-  int rc = edg_sector_create(&ma.m, n_ones, kx, ky, &sec);
+  int rc = T3 ? edg_sector_create3(&ma.m, n_ones, kx, ky, kz, &sec) : edg_sector_create(&ma.m, n_ones, kx, ky, &sec);
   if (rc == EDG_ERR_MOMENTUM) die(outfile, "\nInvalid kx or ky\n");
   edg_sector_info info{};
   if (rc == EDG_OK) edg_sector_get_info(sec, &info);
   t_states = now_seconds() - t_states;
   if (rc != EDG_OK && rc != EDG_ERR_EMPTY) die(outfile, std::string("\nERROR: ") + edg_last_error() + "\n");
   // L1, L2 as the reference's LxLy (Momentum_Basis.cpp:19-36)
-  int L1 = 0, L2 = 0;
+  int L1 = 0, L2 = 0, L3 = 1;
   {
     int s = 0;
     do { s = T1[s]; ++L1; } while (s != 0);
     s = 0;
     do { s = T2[s]; ++L2; } while (s != 0);
+    if (T3) {
+      L3 = 0;
+      s = 0;
+      do { s = (*T3)[s]; ++L3; } while (s != 0);
+    }
   }
-  const double px = 2 * kx * kPi / L1, py = 2 * ky * kPi / L2;
+  const double px = 2 * kx * kPi / L1, py = 2 * ky * kPi / L2, pz = 2 * kz * kPi / L3;
   const int64_t n_p = (rc == EDG_OK) ? info.n_p : 0;
   int64_t n_configs = 1;
   for (int i = 1; i <= n_ones; ++i) n_configs = n_configs * (n_spins - n_ones + i) / i;
   outfile << std::endl << "Total size of all states/rep loc vector " << n_configs << std::endl;
-  outfile << " SECTOR : " << Sz << "\t(" << px << "," << py << ")\t" << n_p << std::endl;
+  if (T3)
+    outfile << " SECTOR : " << Sz << "\t(" << px << "," << py << "," << pz << ")\t" << n_p << std::endl;
+  else
+    outfile << " SECTOR : " << Sz << "\t(" << px << "," << py << ")\t" << n_p << std::endl;
   outfile << "Time to construct pStates\t " << t_states / 60.0 << " minutes" << std::endl;
   if (n_p == 0) die(outfile, "\nNo states in psector\n");
   outfile << "------------------------------------------------------------------" << std::endl;
@@ -168,10 +189,12 @@ void solve_sector(int kx, int ky, double cSz, int n_spins, double lambda, double
   o.ncycles = ncycles;
   o.tol = tol;
   o.seed = 0;
-  o.dense_threshold = 10000;  // Lanczos_sector.cpp:105
+  // the 2-D driver diagonalises sectors up to 10000 states densely
+  // (Lanczos_sector.cpp:105); the 3-D one always runs lanczos_evecs (:285)
+  o.dense_threshold = T3 ? -1 : 10000;
   o.log_fn = log_to_stream;
   o.log_ctx = &outfile;
-  const bool dense = n_p <= o.dense_threshold;
+  const bool dense = o.dense_threshold >= 0 && n_p <= o.dense_threshold;
   const int64_t cap = dense ? n_p : std::min<int64_t>(n_sec_ev, n_p);
   std::vector<double> eigs(std::max<int64_t>(cap, 1));
   const int64_t nvec = find_ev ? std::min<int64_t>(n_sec_ev, dense ? n_p : cap) : 0;
@@ -195,11 +218,22 @@ void solve_sector(int kx, int ky, double cSz, int n_spins, double lambda, double
   outfile << "-----------------------------------------------------------" << std::endl;
   outfile << " Wall clock for Lanczos " << (now_seconds() - lanczos_time) / 60.0 << std::endl;
   outfile << "pblock_eigs.size() = " << n_eigs << std::endl;
-  outfile << "\n\nEnergies\t\tEnergies/site\t\tSz\tkx\tky\tJz\tJ2\n\n";
-  outfile.flush();
-  for (int64_t i = 0; i < n_eigs; ++i)
-    outfile << std::fixed << std::setprecision(15) << eigs[i] << "\t" << eigs[i] / double(n_spins) << "\t"
-            << std::setprecision(3) << Sz << "\t" << px << "\t" << py << "\t" << lambda << "\t" << J2 << "\n";
+  if (T3) {
+    outfile << "\n\nEnergies\t\tEnergies/site\t\tSz\tkx\tky\tkz\tJz\tJ2\n\n";
+    outfile.flush();
+    for (int64_t i = 0; i < n_eigs; ++i)
+      outfile << std::fixed << std::setprecision(15) << eigs[i] << "\t" << eigs[i] / double(n_spins) << "\t"
+              << std::setprecision(3) << Sz << "\t" << px << "\t" << py << "\t" << pz << "\t" << lambda << "\t"
+              << J2 << "\n";
+    outfile.flush();
+    outfile << " find_ev = " << find_ev << std::endl;
+  } else {
+    outfile << "\n\nEnergies\t\tEnergies/site\t\tSz\tkx\tky\tJz\tJ2\n\n";
+    outfile.flush();
+    for (int64_t i = 0; i < n_eigs; ++i)
+      outfile << std::fixed << std::setprecision(15) << eigs[i] << "\t" << eigs[i] / double(n_spins) << "\t"
+              << std::setprecision(3) << Sz << "\t" << px << "\t" << py << "\t" << lambda << "\t" << J2 << "\n";
+  }
   outfile.flush();
 
   if (find_ev) {
@@ -211,19 +245,29 @@ void solve_sector(int kx, int ky, double cSz, int n_spins, double lambda, double
           filepath_EV + (unwrap_peigvec ? "_EV" : "_pEV") + index_string(iib) + ".txt";  // Lanczos_sector.cpp:152-157
       std::ofstream ov(path.c_str());
       ov << "\n Eigenvector for state \n";
-      ov << "Sz\t(kx,ky)\tJz/lambda\n";
-      ov << Sz << "\t(" << kx << "," << ky << ")\t" << lambda << std::endl;
+      if (T3) {
+        ov << "Sz\t(kx,ky,kz)\tJz/lambda\n";
+        ov << Sz << "\t(" << kx << "," << ky << "," << kz << ")\t" << lambda << std::endl;
+      } else {
+        ov << "Sz\t(kx,ky)\tJz/lambda\n";
+        ov << Sz << "\t(" << kx << "," << ky << ")\t" << lambda << std::endl;
+      }
       ov << "\n\n-------------------------------------------";
       ov << "\nState Energy " << cplx(eigs[iib], 0.0) << std::endl;
       std::vector<cplx> c(vecs.begin() + (size_t)iib * n_p, vecs.begin() + (size_t)(iib + 1) * n_p);
       if (unwrap_peigvec) {
-        auto psi = unwrap(c, states, norm, px, py, L1, L2, T1, T2);
+        auto psi = unwrap(c, states, norm, px, py, pz, L1, L2, L3, T1, T2, T3);
         ov << "\nEIGENVECTOR\n";
         for (const auto& e : psi) ov << e.first << "\t" << std::fixed << std::setprecision(15) << e.second << std::endl;
       } else {
         ov << "\nMomentum EIGENVECTOR\n";
-        ov << "\nnp \t\t px \t\tpy\n";
-        ov << n_p << "\t\t" << px << "\t\t" << py << std::endl;
+        if (T3) {
+          ov << "\nnp \t\t px \t\tpy \t\tpz\n";
+          ov << n_p << "\t\t" << px << "\t\t" << py << "\t\t" << pz << std::endl;
+        } else {
+          ov << "\nnp \t\t px \t\tpy\n";
+          ov << n_p << "\t\t" << px << "\t\t" << py << std::endl;
+        }
         ov << "\n\npblock_states \t\t Norm \t\t\t v_coeff\n\n";
         for (int64_t jb = 0; jb < n_p; ++jb)
           ov << states[jb] << "\t\t\t" << norm[jb] << "\t\t\t" << std::fixed << std::setprecision(15) << c[jb]
@@ -263,7 +307,8 @@ void sector_lanczos(int& kx, int& ky, int& kz, double& cSz, int& n_spins, double
                     std::vector<bowties>& chch_list, std::vector<int>& T1, std::vector<int>& T2, std::vector<int>& T3,
                     int& n_sec_ev, bool& find_ev, bool& unwrap_peigvec, std::string& filepath_EV, double& tol,
                     int& iterations, int& ncycles, std::ofstream& outfile) {
-  die(outfile, "\nERROR: 3-D tori (T3) are not implemented by the GPU sector solver\n");
+  solve_sector(kx, ky, cSz, n_spins, lambda, J2, adj_list, Ch, ch_list, ChCh, chch_list, T1, T2, n_sec_ev, find_ev,
+               unwrap_peigvec, filepath_EV, tol, iterations, ncycles, outfile, &T3, kz);
 }
 
 void sector_eigs_eigvecs(int& kx, int& ky, double& cSz, int& n_spins, double& lambda, double& J2,

@@ -9,7 +9,8 @@
 // Terms file (one item per line): "n_sites N", "lambda x", "J2 x", "Ch x",
 // "ChCh x", "T1 a b ...", "T2 a b ...", "bond x y J re im", "ch i j k re im",
 // "chch x y z p q r", "sector Sz kx ky nev iterations ncycles tol find_ev
-// unwrap vector_path".
+// unwrap vector_path"; a 3-D torus adds "T3 a b ..." and "kz k", and the
+// 3-D sector_lanczos overload is called.
 #include <complex>
 #include <cstdio>
 #include <fstream>
@@ -23,12 +24,12 @@
 struct Terms {
   int n_sites = 0;
   double lambda = 1, J2 = 0, Ch = 0, ChCh = 0;
-  std::vector<int> T1, T2;
+  std::vector<int> T1, T2, T3;
   std::vector<coordinates> adj;
   std::vector<triangles> chl;
   std::vector<bowties> chch;
   double Sz = 0, tol = 1e-11;
-  int kx = 0, ky = 0, nev = 2, iterations = 100, ncycles = 10, find_ev = 0, unwrap = 0;
+  int kx = 0, ky = 0, kz = 0, nev = 2, iterations = 100, ncycles = 10, find_ev = 0, unwrap = 0;
   std::string vpath;
 };
 
@@ -45,9 +46,10 @@ static Terms read_terms(const char* path) {
     else if (k == "J2") ss >> t.J2;
     else if (k == "Ch") ss >> t.Ch;
     else if (k == "ChCh") ss >> t.ChCh;
-    else if (k == "T1" || k == "T2") {
+    else if (k == "kz") ss >> t.kz;
+    else if (k == "T1" || k == "T2" || k == "T3") {
       int x;
-      while (ss >> x) (k == "T1" ? t.T1 : t.T2).push_back(x);
+      while (ss >> x) (k == "T1" ? t.T1 : (k == "T2" ? t.T2 : t.T3)).push_back(x);
     } else if (k == "bond") {
       coordinates c;
       double re, im;
@@ -95,8 +97,12 @@ int main(int argc, char** argv) {
   if (mode == "sector") {
     std::ofstream out(argv[3]);
     bool find_ev = t.find_ev, unwrap = t.unwrap;
-    sector_lanczos(t.kx, t.ky, t.Sz, t.n_sites, t.lambda, t.J2, t.adj, t.Ch, t.chl, t.ChCh, t.chch, t.T1, t.T2, t.nev,
-                   find_ev, unwrap, t.vpath, t.tol, t.iterations, t.ncycles, out);
+    if (!t.T3.empty())
+      sector_lanczos(t.kx, t.ky, t.kz, t.Sz, t.n_sites, t.lambda, t.J2, t.adj, t.Ch, t.chl, t.ChCh, t.chch, t.T1, t.T2,
+                     t.T3, t.nev, find_ev, unwrap, t.vpath, t.tol, t.iterations, t.ncycles, out);
+    else
+      sector_lanczos(t.kx, t.ky, t.Sz, t.n_sites, t.lambda, t.J2, t.adj, t.Ch, t.chl, t.ChCh, t.chch, t.T1, t.T2,
+                     t.nev, find_ev, unwrap, t.vpath, t.tol, t.iterations, t.ncycles, out);
     return 0;
   }
   if (mode == "shv" && argc >= 7) {

@@ -57,6 +57,9 @@ def write_terms(path, model, nev=4, iterations=100, ncycles=10, tol=1e-11, find_
         f.write(f"n_sites {model.n_sites}\nlambda {model.Jz!r}\nJ2 {model.J2!r}\nCh {model.Ch!r}\nChCh {model.ChCh!r}\n")
         f.write("T1 " + " ".join(map(str, model.T1)) + "\n")
         f.write("T2 " + " ".join(map(str, model.T2)) + "\n")
+        if getattr(model, "T3", None):
+            f.write("T3 " + " ".join(map(str, model.T3)) + "\n")
+            f.write(f"kz {model.kz}\n")
         for b in model.adj_list:
             f.write(f"bond {b.x} {b.y} {b.J!r} {b.expphase.real!r} {b.expphase.imag!r}\n")
         for t in model.ch_list:
@@ -185,3 +188,49 @@ def test_shv_signature_matches_reference(cuda_device, tmp_path, name):
     w = np.fromfile(tmp_path / "w.c128", np.complex128)
     ref = g["s0_w0"]
     assert np.abs(w - ref).max() / max(1.0, np.abs(ref).max()) <= 1e-13
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,idx", [("cub3x2x2", 1), ("cub4x2x2", 1)])
+def test_three_d_sector_lanczos(cuda_device, tmp_path, name, idx):
+    """The 3-D overload: Lanczos always (no dense path, Lanczos_sector.cpp:285),
+    (px,py,pz) in the SECTOR line, kz in the tables and files, and unwrapped
+    eigenvectors as the reference's Unwrap_pState writes them: it sums every
+    orbit over all L1 L2 L3 translations, so a state whose stabiliser has lid
+    elements comes out lid times too large; divided by lid the vector is an
+    eigenvector of the full-space H."""
+    import oracle as O
+
+    model = golden_model(name, idx)
+    terms = tmp_path / "terms.txt"
+    vpath = str(tmp_path / "vec")
+    write_terms(terms, model, nev=2, iterations=150, ncycles=10, tol=1e-12, find_ev=1, unwrap=1, vpath=vpath)
+    subprocess.run([driver(), "sector", str(terms), str(tmp_path / "out.txt")], check=True)
+    text = (tmp_path / "out.txt").read_text()
+    assert "Lanczos SUMMARY" in text and "EXACT SUMMARY" not in text
+    assert "Energies\t\tEnergies/site\t\tSz\tkx\tky\tkz\tJz\tJ2" in text and " find_ev = 1" in text
+    sector_line = next(l for l in text.splitlines() if l.startswith(" SECTOR :"))
+    assert sector_line.split("(")[1].split(")")[0].count(",") == 2
+    e = energies(text)
+    ev = np.linalg.eigvalsh(O.OracleSector(model).dense())
+    np.testing.assert_allclose(e[:2], ev[:2], rtol=1e-10)
+    states, H = full_space_hamiltonian(model)
+    index = {s: i for i, s in enumerate(states)}
+    osec = O.OracleSector(model)
+    half = model.n_sites // 2
+
+    def lid_of(s):  # stabiliser size of the orbit of s, from the reference's tables
+        lin = osec.Ia[s & ((1 << half) - 1)] + osec.Ib[s >> half] - 1
+        return osec.lid[osec.rep_loc[lin]]
+
+    for k in range(2):
+        body = open(f"{vpath}_EV{k}.txt").read()
+        assert f"({model.kx},{model.ky},{model.kz})" in body
+        psi = np.zeros(len(states), dtype=np.complex128)
+        for line in body.split("EIGENVECTOR")[1].strip().splitlines():
+            sid, c = line.split("\t")
+            re_, im_ = map(float, c.strip("()").split(","))
+            psi[index[int(sid)]] = (re_ + 1j * im_) / lid_of(int(sid))
+        assert abs(np.linalg.norm(psi) - 1) < 1e-9
+        r = H @ psi - e[k] * psi
+        assert np.linalg.norm(r) < 1e-9
