@@ -45,6 +45,7 @@
 
 #include "../../include/edgpu.h"
 #include "blas1.cuh"
+#include "csr_row.cuh"
 #include "edg_sector.cuh"
 #include "ff.cuh"
 #include "lanczos_common.cuh"
@@ -134,7 +135,9 @@ __global__ void __launch_bounds__(kThreads) k_b_u(const SegDev* __restrict__ seg
   }
 }
 
-// w = H V_j on the tile's rows: 32/LPR rows per warp, LPR lanes per row
+// w = H V_j on the tile's rows: 32/LPR rows per warp, LPR lanes per row, each
+// row summed by the single-sector kernel's routine (unrolled column and
+// value-id loads, streaming hint on the row data, L2 evict_last on u)
 template <int LPR>
 __global__ void __launch_bounds__(kThreads) k_b_hv(const SegDev* __restrict__ segs, const SegState* __restrict__ ss,
                                                    const TileDev* __restrict__ tiles) {
@@ -150,18 +153,8 @@ __global__ void __launch_bounds__(kThreads) k_b_hv(const SegDev* __restrict__ se
     const bool ok = r < t.rows;
     const int64_t i = t.row0 + (ok ? r : 0);
     const uint64_t beg = ok ? S.row_ptr[i] : 0, end = ok ? S.row_ptr[i + 1] : 0;
-    float ar = 0.f, ai = 0.f;
-    for (uint64_t e = beg + sl; e < end; e += LPR) {
-      const float2 c = __ldg(S.vtab + __ldg(S.vid + e));
-      const float2 x = S.u[__ldg(S.col + e)];
-      ar += c.x * x.x - c.y * x.y;
-      ai += c.x * x.y + c.y * x.x;
-    }
-#pragma unroll
-    for (int o = LPR / 2; o > 0; o >>= 1) {
-      ar += __shfl_down_sync(0xffffffffu, ar, o, LPR);
-      ai += __shfl_down_sync(0xffffffffu, ai, o, LPR);
-    }
+    float ar, ai;
+    csr_row<float, LPR, false, 1>(beg, end, sl, S.col, S.vid, S.vtab, S.u, ar, ai);
     if (ok && sl == 0) {
       const float ni = (float)S.nrm[S.lid[i]];
       const float d = (float)S.ezz[i];

@@ -28,6 +28,7 @@
 #include <string>
 #include <vector>
 
+#include "csr_row.cuh"
 #include "hv_common.cuh"
 
 namespace edg {
@@ -223,13 +224,6 @@ __global__ void __launch_bounds__(kScan) k_scan64_apply(const uint32_t* __restri
   if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = *total;
 }
 
-template <typename Real>
-struct CT2;
-template <>
-struct CT2<float> { using T = float2; };
-template <>
-struct CT2<double> { using T = double2; };
-
 // u_j = v_j / norm_j
 template <typename Real>
 __global__ void k_u_scale(const typename CT2<Real>::T* __restrict__ v, const uint8_t* __restrict__ lid,
@@ -243,94 +237,6 @@ __global__ void k_u_scale(const typename CT2<Real>::T* __restrict__ v, const uin
     x.x *= s;
     x.y *= s;
     u[i] = x;
-  }
-}
-
-// Cache policy of the CSR loads (tuned per sector with the lanes per row).
-// The row data (col, vid) are read once per H*v; the gathered u entries are
-// reused by other rows while they stay in L2.  Policy 1 reads the row data
-// with the streaming hint (ld.global.cs); policy 2 gives them the L2
-// evict_first priority instead.  Both give the u gathers L2 evict_last.  At
-// 36 sites (a 2 GB u against a 129 MB L2) policy 2 measured 68 ms against
-// 84 ms; at 30-32 sites policy 1 is the faster one.
-__device__ __forceinline__ uint64_t l2_evict_first() {
-  uint64_t p;
-  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
-  return p;
-}
-__device__ __forceinline__ uint64_t l2_evict_last() {
-  uint64_t p;
-  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
-  return p;
-}
-template <int kPol>
-__device__ __forceinline__ uint32_t ld_row(const uint32_t* a, uint64_t pol) {
-  if (kPol == 1) return __ldcs(a);
-  uint32_t r;
-  asm volatile("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(r) : "l"(a), "l"(pol));
-  return r;
-}
-template <int kPol>
-__device__ __forceinline__ int ld_row(const uint16_t* a, uint64_t pol) {
-  if (kPol == 1) return __ldcs(a);
-  uint16_t r;
-  asm volatile("ld.global.nc.L2::cache_hint.u16 %0, [%1], %2;" : "=h"(r) : "l"(a), "l"(pol));
-  return r;
-}
-__device__ __forceinline__ float2 ld_keep(const float2* a, uint64_t pol) {
-  float2 r;
-  asm volatile("ld.global.nc.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;" : "=f"(r.x), "=f"(r.y) : "l"(a), "l"(pol));
-  return r;
-}
-__device__ __forceinline__ double2 ld_keep(const double2* a, uint64_t pol) {
-  double2 r;
-  asm volatile("ld.global.nc.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;" : "=d"(r.x), "=d"(r.y) : "l"(a), "l"(pol));
-  return r;
-}
-
-// One CSR row, handled by LPR lanes of a warp (sl = lane within the row).
-// The row's first LPR*kU entries are resolved in one unrolled step -- all
-// column/value-id loads, then all gathers -- longer rows finish in a loop.
-// Returns the row sum in lane sl == 0 after a segmented reduction.
-template <typename Real, int LPR, bool kSmemTab, int kPol>
-__device__ __forceinline__ void csr_row(uint64_t beg, uint64_t end, int sl, const uint32_t* __restrict__ col,
-                                        const uint16_t* __restrict__ vid, const typename CT2<Real>::T* vtab,
-                                        const typename CT2<Real>::T* __restrict__ u, Real& ar, Real& ai) {
-  using CT = typename CT2<Real>::T;
-  constexpr int kU = 64 / LPR < 2 ? 2 : 64 / LPR;
-  ar = 0;
-  ai = 0;
-  const uint64_t pf = kPol == 2 ? l2_evict_first() : 0, pl = l2_evict_last();
-  uint32_t j[kU];
-  int id[kU];
-#pragma unroll
-  for (int q = 0; q < kU; ++q) {
-    const uint64_t t = beg + sl + LPR * q;
-    j[q] = t < end ? ld_row<kPol>(col + t, pf) : 0xFFFFFFFFu;
-    id[q] = t < end ? ld_row<kPol>(vid + t, pf) : 0;
-  }
-  CT x[kU];
-#pragma unroll
-  for (int q = 0; q < kU; ++q)
-    if (j[q] != 0xFFFFFFFFu) x[q] = ld_keep(u + j[q], pl);
-#pragma unroll
-  for (int q = 0; q < kU; ++q) {
-    if (j[q] == 0xFFFFFFFFu) continue;
-    const CT c = kSmemTab ? vtab[id[q]] : __ldg(vtab + id[q]);
-    ar += c.x * x[q].x - c.y * x[q].y;
-    ai += c.x * x[q].y + c.y * x[q].x;
-  }
-  for (uint64_t t = beg + sl + LPR * kU; t < end; t += LPR) {
-    const int idt = ld_row<kPol>(vid + t, pf);
-    const CT c = kSmemTab ? vtab[idt] : __ldg(vtab + idt);
-    const CT y = ld_keep(u + ld_row<kPol>(col + t, pf), pl);
-    ar += c.x * y.x - c.y * y.y;
-    ai += c.x * y.y + c.y * y.x;
-  }
-#pragma unroll
-  for (int o = LPR / 2; o > 0; o >>= 1) {
-    ar += __shfl_down_sync(0xffffffffu, ar, o, LPR);
-    ai += __shfl_down_sync(0xffffffffu, ai, o, LPR);
   }
 }
 
