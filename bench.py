@@ -204,9 +204,9 @@ def run_device(args, world, rank, local_rank):
 
     import numpy as np
     import torch
-    import torch.distributed as dist
 
     from ed_code_gb300 import _native as N
+    from ed_code_gb300 import replicas as R
     from ed_code_gb300.sector import GpuSector, fill_random
 
     torch.cuda.set_device(local_rank)
@@ -277,8 +277,7 @@ def run_device(args, world, rank, local_rank):
     sampler = ClockSampler(local_rank)
     sampler.start()
     time.sleep(0.3)
-    if world > 1:
-        dist.barrier()
+    R.barrier()
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -288,15 +287,10 @@ def run_device(args, world, rank, local_rank):
             sec.hv(v, w, stream)
         e1.record(stream)
     torch.cuda.synchronize()
-    if world > 1:
-        dist.barrier()
+    R.barrier()
     clocks = sampler.stop()
-    ms = e0.elapsed_time(e1)
-    t = torch.tensor([ms], dtype=torch.float64, device=dev)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t.item())
-    value = world * args.steps / (ms_max / 1e3)
+    ms_max = R.max_over_ranks(e0.elapsed_time(e1))
+    value = R.job_rate(world, args.steps, ms_max / 1e3)
     ms_step = ms_max / args.steps
 
     # e2e through the C ABI host-buffer call: pinned v in, w out, every step
@@ -308,16 +302,12 @@ def run_device(args, world, rank, local_rank):
         code = N.EDG_C128 if fp64 else N.EDG_C64
         lib = N.lib()
         N.check(lib.edg_hv_host(sec._h, C.c_void_p(hv_in.data_ptr()), C.c_void_p(hv_out.data_ptr()), code))
-        if world > 1:
-            dist.barrier()
+        R.barrier()
         te = time.perf_counter()
         for _ in range(args.steps):
             N.check(lib.edg_hv_host(sec._h, C.c_void_p(hv_in.data_ptr()), C.c_void_p(hv_out.data_ptr()), code))
-        dt = time.perf_counter() - te
-        tt = torch.tensor([dt], dtype=torch.float64, device=dev)
-        if world > 1:
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e = {"value": world * args.steps / float(tt.item()), "unit": UNIT,
+        dt = R.max_over_ranks(time.perf_counter() - te)
+        e2e = {"value": R.job_rate(world, args.steps, dt), "unit": UNIT,
                "h2d_bytes_per_step": sec.n_p * elem, "d2h_bytes_per_step": sec.n_p * elem}
         del hv_in, hv_out
 

@@ -13,10 +13,11 @@ from __future__ import annotations
 
 import dataclasses
 import math
-from typing import List, Optional, Sequence
+from typing import Dict, List, Optional, Sequence
 
 from . import _native as N
 from . import lattice as L
+from . import replicas as R
 from .batch import BatchSolver
 from .sector import GpuSector
 
@@ -61,8 +62,12 @@ def sector_list(spec: L.TorusSpec, Sz: Optional[float] = None):
 
 
 def sweep(spec: L.TorusSpec, Sz: Optional[float] = None, n_ev: int = 4, max_iterations: int = 300,
-          res_tol: float = 1e-6, hbm_budget: Optional[int] = None, seed: int = 1) -> List[Level]:
-    """Lowest levels of every sector, sorted as the reference sorts them."""
+          res_tol: float = 1e-6, hbm_budget: Optional[int] = None, seed: int = 1,
+          distributed: bool = False) -> List[Level]:
+    """Lowest levels of every sector, sorted as the reference sorts them.
+
+    distributed: with a process group up (one rank per GPU), each rank solves
+    every world-th sector and the levels are collected on every rank."""
     if hbm_budget is None:
         import torch
 
@@ -83,7 +88,13 @@ def sweep(spec: L.TorusSpec, Sz: Optional[float] = None, n_ev: int = 4, max_iter
             used -= need
         assert not live
 
-    for tag, (n_ones, kx, ky) in enumerate(sector_list(spec, Sz)):
+    rank, world = 0, 1
+    if distributed:
+        import torch.distributed as dist
+
+        if dist.is_initialized():
+            rank, world = dist.get_rank(), dist.get_world_size()
+    for tag, (n_ones, kx, ky) in R.share(list(enumerate(sector_list(spec, Sz))), rank, world):
         sz = 0.5 * n_ones - 0.5 * (n - n_ones)
         meta = (2 * kx * math.pi / spec.Lx, 2 * ky * math.pi / spec.Ly, sz, kx, ky)
         try:
@@ -108,7 +119,14 @@ def sweep(spec: L.TorusSpec, Sz: Optional[float] = None, n_ev: int = 4, max_iter
     if live:
         drain()
     batch.close()
-    # ids count the levels in sector-loop order, as the reference's push_back does
+    if world > 1:
+        per_sector = R.merge(per_sector)
+    return assemble(per_sector)
+
+
+def assemble(per_sector: Dict[int, List[Level]]) -> List[Level]:
+    """Levels of all sectors ({loop position: levels}) in the reference's
+    order, ids counting the levels in sector-loop order as its push_back does."""
     levels: List[Level] = []
     for tag in sorted(per_sector):
         for q in per_sector[tag]:
