@@ -256,8 +256,8 @@ def run_device(args, world, rank, local_rank):
             mode = "stored-rows"
             B = sec.algorithmic_bytes(elem, nnz)
             if args.rows:
-                lanes, pol = (int(x) for x in args.rows.split(","))
-                sec.set_rows(lanes, pol)
+                lanes, pol, *cps = (int(x) for x in args.rows.split(","))
+                sec.set_rows(lanes, pol, cps[0] if cps else 0)
                 lpr = lanes
             else:
                 lpr, tune_ms = sec.tune(0)
@@ -331,9 +331,11 @@ def run_device(args, world, rank, local_rank):
         "config": {"workload": args.workload, "n_p": sec.n_p, "nnz_off": nnz, "vector": args.dtype,
                    "hv_mode": mode, "algorithmic_bytes_per_hv": B, "basis_seconds": round(t_basis, 3),
                    "target_build_seconds": None if t_tgt is None else round(t_tgt, 3),
-                   "stored_row_bytes": 6 * sec.info.get("n_targets", 0) + 16 * sec.n_p,
+                   "stored_row_bytes": (sec.info.get("entry_bytes") or 6) * sec.info.get("n_targets", 0) + 16 * sec.n_p,
+                   "entry_bytes": sec.info.get("entry_bytes"), "n_values": sec.info.get("n_values"),
                    "matrix_free_ms_per_step": mf_ms,
                    "lanes_per_row": lpr, "cache_policy": sec.info.get("cache_policy"),
+                   "ctas_per_sm": sec.info.get("ctas_per_sm"),
                    "panels": sec.info.get("panels"), "panel_pack_seconds": None if t_pack is None else round(t_pack, 3),
                    "row_kernel_ms": None if tune_ms is None else round(float(min(x for x in tune_ms if x > 0)), 3),
                    "tune_ms_lpr_8_16_32": None if tune_ms is None else [round(float(x), 3) for x in tune_ms],
@@ -597,7 +599,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--matrix-free", action="store_true", help="do not store the searched targets")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--rows", default=None, help="LANES,POLICY: fix the stored-row kernel instead of timing it")
+    ap.add_argument("--rows", default=None,
+                    help="LANES,POLICY[,CTAS_PER_SM]: fix the stored-row kernel instead of timing it")
     ap.add_argument("--panels", type=int, default=0,
                     help="regroup the stored rows into this many column panels (0: keep the row kernel)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)

@@ -87,7 +87,8 @@ struct SegDev {
   double* ywork;          // want x 6 m_max: Ritz coefficients + inverse-iteration work
   double* aux;            // [0]: |w|^2 before reorthogonalisation
   int64_t n;
-  int m_max, want, check_every, pad;
+  int m_max, want, check_every;
+  int pack_cb;            // column bits of packed entries (vid == nullptr)
   double tol;
 };
 
@@ -154,7 +155,7 @@ __global__ void __launch_bounds__(kThreads) k_b_hv(const SegDev* __restrict__ se
     const int64_t i = t.row0 + (ok ? r : 0);
     const uint64_t beg = ok ? S.row_ptr[i] : 0, end = ok ? S.row_ptr[i + 1] : 0;
     float ar, ai;
-    csr_row<float, LPR, false, 1>(beg, end, sl, S.col, S.vid, S.vtab, S.u, ar, ai);
+    csr_row<float, LPR, false, 1, kByVid>(beg, end, sl, S.col, S.vid, S.pack_cb, S.vtab, S.u, ar, ai);
     if (ok && sl == 0) {
       const float ni = (float)S.nrm[S.lid[i]];
       const float d = (float)S.ezz[i];
@@ -761,6 +762,7 @@ int edg_batch_add(edg_batch* bh, edg_sector* sec, const edg_batch_request* req) 
   d.row_ptr = S.row_ptr;
   d.col = S.col;
   d.vid = S.vid;
+  d.pack_cb = S.pack_cb;
   d.vtab = S.vtab32;
   d.ezz = S.ezz;
   d.lid = S.lid;

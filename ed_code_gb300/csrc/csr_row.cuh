@@ -57,13 +57,35 @@ __device__ __forceinline__ double2 ld_keep(const double2* a, uint64_t pol) {
   return r;
 }
 
+// Entry formats of the stored rows.  kSplit: a u32 column array and a u16
+// value-id array (6 bytes an entry).  kPacked: one u32 an entry, the column
+// in the low cb bits and the value id above them (4 bytes), used when the
+// deduplicated value table and the sector size leave room (cb < 32 and
+// n_p < 2^cb, so no entry is all ones).  kByVid: either, chosen per row by
+// vid == nullptr (the batch, whose segments may differ).
+constexpr int kSplit = 0, kPacked = 1, kByVid = 2;
+
+template <int kFmt, int kPol>
+__device__ __forceinline__ void ld_entry(const uint32_t* col, const uint16_t* vid, uint64_t t, int cb, uint64_t pf,
+                                         uint32_t& j, int& id) {
+  const bool packed = kFmt == kPacked || (kFmt == kByVid && vid == nullptr);
+  const uint32_t e = ld_row<kPol>(col + t, pf);
+  if (packed) {
+    j = e & ((1u << cb) - 1u);
+    id = (int)(e >> cb);
+  } else {
+    j = e;
+    id = ld_row<kPol>(vid + t, pf);
+  }
+}
+
 // One CSR row, handled by LPR lanes of a warp (sl = lane within the row).
 // The row's first LPR*kU entries are resolved in one unrolled step -- all
-// column/value-id loads, then all gathers -- longer rows finish in a loop.
+// entry loads, then all gathers -- longer rows finish in a loop.
 // Returns the row sum in lane sl == 0 after a segmented reduction.
-template <typename Real, int LPR, bool kSmemTab, int kPol>
+template <typename Real, int LPR, bool kSmemTab, int kPol, int kFmt>
 __device__ __forceinline__ void csr_row(uint64_t beg, uint64_t end, int sl, const uint32_t* __restrict__ col,
-                                        const uint16_t* __restrict__ vid, const typename CT2<Real>::T* vtab,
+                                        const uint16_t* __restrict__ vid, int cb, const typename CT2<Real>::T* vtab,
                                         const typename CT2<Real>::T* __restrict__ u, Real& ar, Real& ai) {
   using CT = typename CT2<Real>::T;
   constexpr int kU = 64 / LPR < 2 ? 2 : 64 / LPR;
@@ -75,8 +97,9 @@ __device__ __forceinline__ void csr_row(uint64_t beg, uint64_t end, int sl, cons
 #pragma unroll
   for (int q = 0; q < kU; ++q) {
     const uint64_t t = beg + sl + LPR * q;
-    j[q] = t < end ? ld_row<kPol>(col + t, pf) : 0xFFFFFFFFu;
-    id[q] = t < end ? ld_row<kPol>(vid + t, pf) : 0;
+    j[q] = 0xFFFFFFFFu;
+    id[q] = 0;
+    if (t < end) ld_entry<kFmt, kPol>(col, vid, t, cb, pf, j[q], id[q]);
   }
   CT x[kU];
 #pragma unroll
@@ -90,9 +113,11 @@ __device__ __forceinline__ void csr_row(uint64_t beg, uint64_t end, int sl, cons
     ai += c.x * x[q].y + c.y * x[q].x;
   }
   for (uint64_t t = beg + sl + LPR * kU; t < end; t += LPR) {
-    const int idt = ld_row<kPol>(vid + t, pf);
+    uint32_t jt;
+    int idt;
+    ld_entry<kFmt, kPol>(col, vid, t, cb, pf, jt, idt);
     const CT c = kSmemTab ? vtab[idt] : __ldg(vtab + idt);
-    const CT y = ld_keep(u + ld_row<kPol>(col + t, pf), pl);
+    const CT y = ld_keep(u + jt, pl);
     ar += c.x * y.x - c.y * y.y;
     ai += c.x * y.y + c.y * y.x;
   }

@@ -94,8 +94,9 @@ struct Sector {
   int hv_variant = 0;
   // stored targets (targets.cu): CSR rows of (column, value id)
   uint64_t* row_ptr = nullptr;  // n_p + 1
-  uint32_t* col = nullptr;
-  uint16_t* vid = nullptr;
+  uint32_t* col = nullptr;      // column, or column | value id << pack_cb
+  uint16_t* vid = nullptr;      // value ids; null when the entries are packed
+  int pack_cb = 0;              // column bits of a packed entry (0: split arrays)
   double* ezz = nullptr;        // diagonal of each row
   double2* vtab64 = nullptr;    // value table: pair coefficient x phase class
   float2* vtab32 = nullptr;
@@ -104,6 +105,7 @@ struct Sector {
   size_t targets_bytes = 0;
   int csr_lpr = 16;             // lanes per CSR row (8, 16 or 32): edg_sector_tune
   int csr_pol = 1;              // cache policy of the CSR loads (1 or 2): edg_sector_tune
+  int csr_cps = 0;              // CTAs per SM of the CSR kernel (0: as many as fit): edg_sector_tune
   // column panels (edg_sector_pack_panels): the stored rows regrouped so that
   // one H*v launch per panel gathers from one L2-sized slice of u
   uint32_t* pan_ent = nullptr;  // (column - p*pan_c) | local row << 23

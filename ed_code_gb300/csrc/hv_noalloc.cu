@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(kThreads) k_na_scale(const typename Cplx<Real>
 template <typename Real, int LPR>
 __global__ void __launch_bounds__(kThreads) k_na_rows(const uint64_t* __restrict__ row_ptr,
                                                       const uint32_t* __restrict__ col,
-                                                      const uint16_t* __restrict__ vid,
+                                                      const uint16_t* __restrict__ vid, int cb,
                                                       const typename Cplx<Real>::T* __restrict__ vtab,
                                                       const double* __restrict__ ezz, const uint8_t* __restrict__ lid,
                                                       const double* __restrict__ nrm_tab, int64_t n,
@@ -126,8 +126,11 @@ __global__ void __launch_bounds__(kThreads) k_na_rows(const uint64_t* __restrict
     }
     Real ar = 0, ai = 0;
     for (uint64_t t = beg + sl; t < end; t += LPR) {
-      const CT c = __ldg(vtab + __ldg(vid + t));
-      const CT x = u[__ldg(col + t)];
+      // split entries: column and value id in two arrays; packed: the id
+      // above the low cb column bits of one u32
+      const uint32_t e = __ldg(col + t);
+      const CT c = __ldg(vtab + (vid ? (uint32_t)__ldg(vid + t) : e >> cb));
+      const CT x = u[vid ? e : e & ((1u << cb) - 1u)];
       ar += c.x * x.x - c.y * x.y;
       ai += c.x * x.y + c.y * x.x;
     }
@@ -170,7 +173,7 @@ cudaError_t launch_rows(const edg::Sector& S, const void* v, void* w, void* u, i
   scale<<<grid_size(scale, n, dev), kThreads, 0, st>>>(reinterpret_cast<const CT*>(v), S.lid, nrm_inv, n,
                                                        reinterpret_cast<CT*>(u));
   auto rows = k_na_rows<Real, LPR>;
-  rows<<<grid_size(rows, n * LPR, dev), kThreads, 0, st>>>(S.row_ptr, S.col, S.vid, tab, S.ezz, S.lid, nrm, n,
+  rows<<<grid_size(rows, n * LPR, dev), kThreads, 0, st>>>(S.row_ptr, S.col, S.vid, S.pack_cb, tab, S.ezz, S.lid, nrm, n,
                                                           reinterpret_cast<const CT*>(v),
                                                           reinterpret_cast<const CT*>(u), reinterpret_cast<CT*>(w));
   return cudaGetLastError();

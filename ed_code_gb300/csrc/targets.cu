@@ -2,21 +2,22 @@
 // kept in HBM as compressed sparse rows.
 //
 // For row i, every anti-aligned flip group g whose flipped state has an
-// allowed representative j contributes one stored entry
-//     col = j                         (u32)
-//     vid = (off[g] + variant) * n_cls + cls        (u16)
-// where `variant` packs bit a of the state and the bits z of the group's
-// chirality terms (the inputs of the coefficient, H_v.cpp:232-303) and `cls`
-// is the phase class of the translation to the representative.  The value
-// table vtab[vid] = coefficient(g, variant) * phase(cls) is built on the host
-// from the same term lists.  Rows also keep their diagonal Ezz.
+// allowed representative j contributes one stored entry: the column j and
+// the value id remap[(off[g] + variant) * n_cls + cls], where `variant` packs
+// bit a of the state and the bits z of the group's chirality terms (the
+// inputs of the coefficient, H_v.cpp:232-303) and `cls` is the phase class of
+// the translation to the representative.  The value table
+// vtab[id] = coefficient(g, variant) * phase(cls) is built on the host from
+// the same term lists and deduplicated (remap).  An entry is one u32 with the
+// id above the column when both fit (4 bytes), else a u32 column and a u16
+// id (6 bytes).  Rows also keep their diagonal Ezz.
 //
 // H*v is then a CSR SpMV with a value dictionary (one warp per row, lanes
 // over the row's entries):
 //     w_i = norm_i * sum_t vtab[vid_t] * u[col_t] + Ezz_i * v_i,
 //     u_j = v_j / norm_j (a streaming pass before the row loop).
-// This stores the Hamiltonian's structure (6 bytes per nonzero, 84 GB for the
-// 36-site Sz=0 sector) instead of searching orbits every H*v; the matrix-free
+// This stores the Hamiltonian's structure (4 bytes per nonzero, 56 GB for the
+// 36-site Sz=0, k=0 sector) instead of searching orbits every H*v; the matrix-free
 // kernels (hv.cu) remain for sectors whose entries do not fit.  The reference
 // has the same trade as an option of its own (sHv on an sMatrix, H_v.cpp:3-19).
 #include <cuda_runtime.h>
@@ -25,7 +26,11 @@
 #include <cmath>
 #include <complex>
 #include <cstddef>
+#include <cstdlib>
+#include <cstring>
+#include <map>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "csr_row.cuh"
@@ -84,8 +89,12 @@ __device__ __forceinline__ int total(const uint32_t (&words)[NW]) {
 
 // Pass 1 (count) and pass 2 (fill) share this walk over a row's targets: one
 // warp per row, lane k resolves the row's k-th anti-aligned pair.
+// The fill pass writes each entry's value id as remap[(pair variant) x class],
+// the index into the deduplicated value table, packed above the column when
+// cb > 0 (csr_row.cuh).
 template <bool kTorus, int NW, bool kFill>
 __global__ void __launch_bounds__(kTgtThreads) k_tgt_pass(SectorView V, const uint16_t* __restrict__ voff,
+                                                          const uint16_t* __restrict__ remap, int cb,
                                                           uint32_t* __restrict__ counts, double* __restrict__ ezz,
                                                           const uint64_t* __restrict__ row_ptr,
                                                           uint32_t* __restrict__ col, uint16_t* __restrict__ vid) {
@@ -125,14 +134,18 @@ __global__ void __launch_bounds__(kTgtThreads) k_tgt_pass(SectorView V, const ui
           j = (uint32_t)jj;
           int variant = (int)((s >> gr.a) & 1u);
           for (int m = gr.ch_begin, b = 1; m < gr.ch_end; ++m, ++b) variant |= (int)((s >> H.ch[m].z) & 1u) << b;
-          id = (uint16_t)((off[g] + variant) * P.n_cls + P.g2cls[o.g]);
+          if (kFill) id = __ldg(remap + (off[g] + variant) * P.n_cls + P.g2cls[o.g]);
         }
       }
       const uint32_t bal = __ballot_sync(0xffffffffu, ok);
       if (kFill && ok) {
         const uint64_t t = pos + __popc(bal & lt);
-        col[t] = j;
-        vid[t] = id;
+        if (cb) {
+          col[t] = j | ((uint32_t)id << cb);
+        } else {
+          col[t] = j;
+          vid[t] = id;
+        }
       }
       pos += __popc(bal);
       cnt += __popc(bal);
@@ -241,11 +254,12 @@ __global__ void k_u_scale(const typename CT2<Real>::T* __restrict__ v, const uin
 }
 
 // CSR SpMV with a value dictionary: 32/LPR rows per warp, the next rows'
-// offsets loaded while the current ones run.
-template <typename Real, int LPR, bool kSmemTab, int kPol>
+// offsets loaded while the current ones run.  kFmt: kSplit or kPacked entries
+// (csr_row.cuh), cb the column bits of a packed entry.
+template <typename Real, int LPR, bool kSmemTab, int kPol, int kFmt>
 __global__ void __launch_bounds__(kTgtThreads) k_hv_csr(const uint64_t* __restrict__ row_ptr,
                                                         const uint32_t* __restrict__ col,
-                                                        const uint16_t* __restrict__ vid,
+                                                        const uint16_t* __restrict__ vid, int cb,
                                                         const typename CT2<Real>::T* __restrict__ vtab, int n_vals,
                                                         const double* __restrict__ ezz,
                                                         const uint8_t* __restrict__ lid,
@@ -281,7 +295,8 @@ __global__ void __launch_bounds__(kTgtThreads) k_hv_csr(const uint64_t* __restri
       nend = __ldg(rp + inext + 1);
     }
     Real ar, ai;
-    csr_row<Real, LPR, kSmemTab, kPol>(beg, i < n_p ? end : beg, sl, col, vid, kSmemTab ? tab : vtab, u, ar, ai);
+    csr_row<Real, LPR, kSmemTab, kPol, kFmt>(beg, i < n_p ? end : beg, sl, col, vid, cb, kSmemTab ? tab : vtab, u, ar,
+                                             ai);
     if (sl == 0 && i < n_p) {
       const CT vi = v[i];
       const Real ni = nrm[lid[i]];
@@ -299,13 +314,16 @@ __global__ void __launch_bounds__(kTgtThreads) k_hv_csr(const uint64_t* __restri
 
 int n_words(int n_groups) { return n_groups <= 128 ? 4 : 8; }
 
+// Grid of a grid-stride kernel: the CTAs that fit on every SM at once, at most
+// cap per SM when cap > 0, no more than the work needs.
 template <typename K>
-int grid_for(K kernel, size_t smem, int64_t work, int threads) {
+int grid_for(K kernel, size_t smem, int64_t work, int threads, int cap = 0) {
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
+  if (cap > 0 && per_sm > cap) per_sm = cap;
   if (per_sm < 1) per_sm = 1;
   const int64_t want = (work + threads - 1) / threads;
   return (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sms * per_sm));
@@ -316,7 +334,7 @@ const double* params_field(const Sector& S, size_t offset) {
 }
 
 // rows [r0, r1); u = v / norm first when with_u
-template <typename Real, int LPR, int kPol>
+template <typename Real, int LPR, int kPol, int kFmt>
 cudaError_t launch_csr_lpr(const Sector& S, const void* v, void* w, cudaStream_t st, int64_t r0, int64_t r1,
                            bool with_u) {
   using CT = typename CT2<Real>::T;
@@ -331,27 +349,34 @@ cudaError_t launch_csr_lpr(const Sector& S, const void* v, void* w, cudaStream_t
   if (r1 <= r0) return cudaGetLastError();
   const int64_t threads_needed = ((r1 - r0) * LPR + 31) / 32 * 32;
   if (tab_bytes <= 96 * 1024) {
-    auto kern = k_hv_csr<Real, LPR, true, kPol>;
-    kern<<<grid_for(kern, tab_bytes, threads_needed, kTgtThreads), kTgtThreads, tab_bytes, st>>>(
-        S.row_ptr, S.col, S.vid, tab, S.n_vals, S.ezz, S.lid, nrm, r0, r1, reinterpret_cast<const CT*>(v),
+    auto kern = k_hv_csr<Real, LPR, true, kPol, kFmt>;
+    kern<<<grid_for(kern, tab_bytes, threads_needed, kTgtThreads, S.csr_cps), kTgtThreads, tab_bytes, st>>>(
+        S.row_ptr, S.col, S.vid, S.pack_cb, tab, S.n_vals, S.ezz, S.lid, nrm, r0, r1, reinterpret_cast<const CT*>(v),
         reinterpret_cast<const CT*>(S.ubuf.ptr), reinterpret_cast<CT*>(w));
   } else {
-    auto kern = k_hv_csr<Real, LPR, false, kPol>;
-    kern<<<grid_for(kern, 0, threads_needed, kTgtThreads), kTgtThreads, 0, st>>>(
-        S.row_ptr, S.col, S.vid, tab, S.n_vals, S.ezz, S.lid, nrm, r0, r1, reinterpret_cast<const CT*>(v),
+    auto kern = k_hv_csr<Real, LPR, false, kPol, kFmt>;
+    kern<<<grid_for(kern, 0, threads_needed, kTgtThreads, S.csr_cps), kTgtThreads, 0, st>>>(
+        S.row_ptr, S.col, S.vid, S.pack_cb, tab, S.n_vals, S.ezz, S.lid, nrm, r0, r1, reinterpret_cast<const CT*>(v),
         reinterpret_cast<const CT*>(S.ubuf.ptr), reinterpret_cast<CT*>(w));
   }
   return cudaGetLastError();
 }
 
+template <typename Real, int kPol, int kFmt>
+cudaError_t launch_csr_f(const Sector& S, const void* v, void* w, cudaStream_t st, int64_t r0, int64_t r1,
+                         bool with_u) {
+  switch (S.csr_lpr) {
+    case 8: return launch_csr_lpr<Real, 8, kPol, kFmt>(S, v, w, st, r0, r1, with_u);
+    case 16: return launch_csr_lpr<Real, 16, kPol, kFmt>(S, v, w, st, r0, r1, with_u);
+    default: return launch_csr_lpr<Real, 32, kPol, kFmt>(S, v, w, st, r0, r1, with_u);
+  }
+}
+
 template <typename Real, int kPol>
 cudaError_t launch_csr_p(const Sector& S, const void* v, void* w, cudaStream_t st, int64_t r0, int64_t r1,
                          bool with_u) {
-  switch (S.csr_lpr) {
-    case 8: return launch_csr_lpr<Real, 8, kPol>(S, v, w, st, r0, r1, with_u);
-    case 16: return launch_csr_lpr<Real, 16, kPol>(S, v, w, st, r0, r1, with_u);
-    default: return launch_csr_lpr<Real, 32, kPol>(S, v, w, st, r0, r1, with_u);
-  }
+  return S.pack_cb ? launch_csr_f<Real, kPol, kPacked>(S, v, w, st, r0, r1, with_u)
+                   : launch_csr_f<Real, kPol, kSplit>(S, v, w, st, r0, r1, with_u);
 }
 
 template <typename Real>
@@ -381,8 +406,9 @@ constexpr int kPanBits = 23;
 
 // entries per (block, panel), panel-major: counts[p * nb + b]
 __global__ void __launch_bounds__(kTgtThreads) k_pan_count(const uint64_t* __restrict__ row_ptr,
-                                                           const uint32_t* __restrict__ col, int64_t n, int64_t nb,
-                                                           int P, int64_t C, uint32_t* __restrict__ counts) {
+                                                           const uint32_t* __restrict__ col, int cb, int64_t n,
+                                                           int64_t nb, int P, int64_t C, uint32_t* __restrict__ counts) {
+  const uint32_t cmask = cb ? (1u << cb) - 1u : 0xFFFFFFFFu;
   extern __shared__ uint32_t hist[];  // kWarpsPerBlock x P
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   uint32_t* h = hist + wid * P;
@@ -391,7 +417,7 @@ __global__ void __launch_bounds__(kTgtThreads) k_pan_count(const uint64_t* __res
     for (int k = lane; k < P; k += 32) h[k] = 0;
     __syncwarp();
     const uint64_t beg = row_ptr[b * kPanRows], end = row_ptr[min(n, (b + 1) * kPanRows)];
-    for (uint64_t t = beg + lane; t < end; t += 32) atomicAdd(&h[(int)(col[t] / C)], 1u);
+    for (uint64_t t = beg + lane; t < end; t += 32) atomicAdd(&h[(int)((col[t] & cmask) / C)], 1u);
     __syncwarp();
     for (int k = lane; k < P; k += 32) counts[(int64_t)k * nb + b] = h[k];
     __syncwarp();
@@ -402,9 +428,11 @@ __global__ void __launch_bounds__(kTgtThreads) k_pan_count(const uint64_t* __res
 // lanes of a 32-entry chunk that share a panel are ranked with match_any
 __global__ void __launch_bounds__(kTgtThreads) k_pan_scatter(const uint64_t* __restrict__ row_ptr,
                                                              const uint32_t* __restrict__ col,
-                                                             const uint16_t* __restrict__ vid, int64_t n, int64_t nb,
-                                                             int P, int64_t C, const uint64_t* __restrict__ off,
+                                                             const uint16_t* __restrict__ vid, int cb, int64_t n,
+                                                             int64_t nb, int P, int64_t C,
+                                                             const uint64_t* __restrict__ off,
                                                              uint32_t* __restrict__ ent, uint16_t* __restrict__ evid) {
+  const uint32_t cmask = cb ? (1u << cb) - 1u : 0xFFFFFFFFu;
   extern __shared__ uint32_t run[];  // kWarpsPerBlock x P running counts
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   uint32_t* rc = run + wid * P;
@@ -418,7 +446,8 @@ __global__ void __launch_bounds__(kTgtThreads) k_pan_scatter(const uint64_t* __r
       for (uint64_t t0 = beg; t0 < end; t0 += 32) {
         const uint64_t t = t0 + lane;
         const bool ok = t < end;
-        const uint32_t c = ok ? col[t] : 0u;
+        const uint32_t e = ok ? col[t] : 0u;
+        const uint32_t c = e & cmask;
         const int p = ok ? (int)(c / C) : -1;
         const unsigned valid = __ballot_sync(0xffffffffu, ok);
         const unsigned same = __match_any_sync(0xffffffffu, p) & valid;
@@ -427,7 +456,7 @@ __global__ void __launch_bounds__(kTgtThreads) k_pan_scatter(const uint64_t* __r
         if (ok) {
           const uint64_t pos = off[(int64_t)p * nb + b] + base + __popc(same & ((1u << lane) - 1u));
           ent[pos] = (uint32_t)(c - (int64_t)p * C) | ((uint32_t)(r - b * kPanRows) << kPanBits);
-          evid[pos] = vid[t];
+          evid[pos] = cb ? (uint16_t)(e >> cb) : vid[t];
           if ((same & ((1u << lane) - 1u)) == 0u) rc[p] = base + __popc(same);
         }
         __syncwarp();
@@ -615,6 +644,7 @@ void free_targets(Sector& S) {
   S.row_ptr = nullptr;
   S.col = nullptr;
   S.vid = nullptr;
+  S.pack_cb = 0;
   S.ezz = nullptr;
   S.vtab64 = nullptr;
   S.vtab32 = nullptr;
@@ -675,12 +705,13 @@ int pack_panels(Sector& S, int n_panels, std::string& err) {
   }
   const size_t hist = sizeof(uint32_t) * kWarpsPerBlock * P;
   const int g1 = grid_for(k_pan_count, hist, nb * 32, kTgtThreads);
-  k_pan_count<<<g1, kTgtThreads, hist, st>>>(S.row_ptr, S.col, n, nb, (int)P, C, counts);
+  k_pan_count<<<g1, kTgtThreads, hist, st>>>(S.row_ptr, S.col, S.pack_cb, n, nb, (int)P, C, counts);
   k_scan64_chunks<<<(unsigned)n_chunks, kScan, 0, st>>>(counts, nc, sums);
   k_scan64_sums<<<1, kScan, 0, st>>>(sums, n_chunks, tot);
   k_scan64_apply<<<(unsigned)n_chunks, kScan, 0, st>>>(counts, nc, sums, tot, off);
   const int g2 = grid_for(k_pan_scatter, hist, nb * 32, kTgtThreads);
-  k_pan_scatter<<<g2, kTgtThreads, hist, st>>>(S.row_ptr, S.col, S.vid, n, nb, (int)P, C, off, ent, evid);
+  k_pan_scatter<<<g2, kTgtThreads, hist, st>>>(S.row_ptr, S.col, S.vid, S.pack_cb, n, nb, (int)P, C, off, ent,
+                                                evid);
   unsigned long long total = 0;
   e = cudaMemcpyAsync(&total, tot, sizeof(total), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -695,9 +726,11 @@ int pack_panels(Sector& S, int n_panels, std::string& err) {
   cudaFree(S.row_ptr);
   cudaFree(S.col);
   cudaFree(S.vid);
+  const size_t entry = S.pack_cb ? 4 : 6;
   S.row_ptr = nullptr;
   S.col = nullptr;
   S.vid = nullptr;
+  S.pack_cb = 0;
   S.pan_ent = ent;
   S.pan_vid = evid;
   S.pan_off = off;
@@ -705,7 +738,7 @@ int pack_panels(Sector& S, int n_panels, std::string& err) {
   S.pan_c = C;
   S.pan_nb = nb;
   const size_t before = S.targets_bytes;
-  S.targets_bytes = nnz * 6 + sizeof(uint64_t) * (nc + 1) + (before - (size_t)nnz * 6 - sizeof(uint64_t) * (n + 1));
+  S.targets_bytes = nnz * 6 + sizeof(uint64_t) * (nc + 1) + (before - (size_t)nnz * entry - sizeof(uint64_t) * (n + 1));
   S.device_bytes += S.targets_bytes - before;
   return EDG_OK;
 }
@@ -784,18 +817,51 @@ int build_targets(Sector& S, int64_t max_bytes, std::string& err) {
       }
     }
   }
+  // Deduplicate the table by bit pattern: with uniform couplings many
+  // (pair, variant, class) combinations share one value.  remap[k] is the
+  // index of combination k in the deduplicated table.
+  std::vector<uint16_t> remap(tab64.size());
+  {
+    std::map<std::pair<uint64_t, uint64_t>, uint16_t> index;
+    std::vector<double2> uniq;
+    for (size_t k = 0; k < tab64.size(); ++k) {
+      std::pair<uint64_t, uint64_t> key;
+      std::memcpy(&key.first, &tab64[k].x, 8);
+      std::memcpy(&key.second, &tab64[k].y, 8);
+      auto it = index.find(key);
+      if (it == index.end()) {
+        it = index.emplace(key, (uint16_t)uniq.size()).first;
+        uniq.push_back(tab64[k]);
+      }
+      remap[k] = it->second;
+    }
+    tab64.swap(uniq);
+  }
   std::vector<float2> tab32(tab64.size());
   for (size_t k = 0; k < tab64.size(); ++k) tab32[k] = make_float2((float)tab64[k].x, (float)tab64[k].y);
+  // Packed entries when the value ids and the columns fit one u32 together:
+  // vb bits of value id above cb = 32 - vb column bits, n_p < 2^cb.
+  // EDG_ROW_FORMAT=split keeps the two arrays (for comparisons).
+  int vb = 1;
+  while ((size_t(1) << vb) < tab64.size()) ++vb;
+  const char* fmt_env = std::getenv("EDG_ROW_FORMAT");
+  const bool want_split = fmt_env && std::strcmp(fmt_env, "split") == 0;
+  const int cb = 32 - vb;
+  S.pack_cb = (!want_split && vb < 32 && P.n_p < (int64_t(1) << cb)) ? cb : 0;
+  const double entry_bytes = S.pack_cb ? 4.0 : 6.0;
 
   cudaStream_t st = S.stream;
   const int64_t n = P.n_p;
   uint32_t* counts = nullptr;
-  uint16_t* d_voff = nullptr;
+  uint16_t *d_voff = nullptr, *d_remap = nullptr;
   unsigned long long *sums = nullptr, *tot = nullptr;
   const int64_t n_chunks = (n + kChunk - 1) / kChunk;
   cudaError_t e = cudaMemcpy(S.dP, &P, sizeof(P), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMalloc(&counts, sizeof(uint32_t) * n);
   if (e == cudaSuccess) e = cudaMalloc(&d_voff, sizeof(uint16_t) * voff.size());
+  if (e == cudaSuccess) e = cudaMalloc(&d_remap, sizeof(uint16_t) * remap.size());
+  if (e == cudaSuccess)
+    e = cudaMemcpy(d_remap, remap.data(), sizeof(uint16_t) * remap.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMalloc(&sums, sizeof(unsigned long long) * n_chunks);
   if (e == cudaSuccess) e = cudaMalloc(&tot, sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMalloc(&S.row_ptr, sizeof(uint64_t) * (n + 1));
@@ -809,6 +875,7 @@ int build_targets(Sector& S, int64_t max_bytes, std::string& err) {
   auto cleanup = [&]() {
     cudaFree(counts);
     cudaFree(d_voff);
+    cudaFree(d_remap);
     cudaFree(sums);
     cudaFree(tot);
   };
@@ -823,7 +890,7 @@ int build_targets(Sector& S, int64_t max_bytes, std::string& err) {
   const int nw = n_words(P.n_groups);
   auto pass = [&](auto kern, bool fill) {
     kern<<<grid_for(kern, smem, n * 32, kTgtThreads), kTgtThreads, smem, st>>>(
-        S.V, d_voff, counts, S.ezz, S.row_ptr, fill ? S.col : nullptr, fill ? S.vid : nullptr);
+        S.V, d_voff, d_remap, S.pack_cb, counts, S.ezz, S.row_ptr, fill ? S.col : nullptr, fill ? S.vid : nullptr);
   };
   if (torus) {
     if (nw == 4) pass(k_tgt_pass<true, 4, false>, false);
@@ -840,7 +907,7 @@ int build_targets(Sector& S, int64_t max_bytes, std::string& err) {
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   size_t free_b = 0, total_b = 0;
   cudaMemGetInfo(&free_b, &total_b);
-  const double need = 6.0 * (double)nnz + 16.0 * (double)n;
+  const double need = entry_bytes * (double)nnz + 16.0 * (double)n;
   if (e != cudaSuccess || need > (double)max_bytes || need > 0.9 * (double)free_b) {
     cleanup();
     free_targets(S);
@@ -849,7 +916,7 @@ int build_targets(Sector& S, int64_t max_bytes, std::string& err) {
     return e != cudaSuccess ? EDG_ERR_CUDA : EDG_ERR_NOMEM;
   }
   e = cudaMalloc(&S.col, sizeof(uint32_t) * std::max<unsigned long long>(1, nnz));
-  if (e == cudaSuccess) e = cudaMalloc(&S.vid, sizeof(uint16_t) * std::max<unsigned long long>(1, nnz));
+  if (e == cudaSuccess && !S.pack_cb) e = cudaMalloc(&S.vid, sizeof(uint16_t) * std::max<unsigned long long>(1, nnz));
   if (e == cudaSuccess) e = cudaMalloc(&S.ubuf.ptr, (size_t)(16 * n));
   if (e != cudaSuccess) {
     cleanup();
@@ -873,16 +940,18 @@ int build_targets(Sector& S, int64_t max_bytes, std::string& err) {
     return EDG_ERR_CUDA;
   }
   P.n_targets = (int64_t)nnz;
-  S.targets_bytes = 6 * nnz + 8 * (n + 1) + 8 * n + 16 * n + 24 * tab64.size();
+  S.targets_bytes = (S.pack_cb ? 4 : 6) * nnz + 8 * (n + 1) + 8 * n + 16 * n + 24 * tab64.size();
   S.device_bytes += S.targets_bytes;
   e = cudaMemcpy(S.dP, &P, sizeof(P), cudaMemcpyHostToDevice);
   return e == cudaSuccess ? EDG_OK : EDG_ERR_CUDA;
 }
 
-// Lanes per CSR row and cache policy.  lpr in {8, 16, 32} fixes the lanes and
-// times the two policies; 0 times all six combinations (FP32, three launches
-// after a warm-up each) on this sector and keeps the fastest.  ms_out[k]
-// receives the best time of lane count 8, 16, 32 (-1 when not timed).
+// Lanes per CSR row, cache policy and CTAs per SM.  lpr in {8, 16, 32} fixes
+// the lanes and times the rest; 0 times every lane count.  Each combination
+// runs twice (FP32) after one warm-up launch, and the fastest is kept.  The
+// CTA cap matters because the gathers reuse u through L2: fewer rows in
+// flight keep their targets' window of u smaller.  ms_out[k] receives the
+// best time of lane count 8, 16, 32 (-1 when not timed).
 int tune_rows(Sector& S, int lpr, int* chosen, double* ms_out) {
   if (!S.col) {
     if (chosen) *chosen = 0;
@@ -901,30 +970,38 @@ int tune_rows(Sector& S, int lpr, int* chosen, double* ms_out) {
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   const int cand[3] = {8, 16, 32};
-  int best = 16, best_pol = 1;
+  const int caps[4] = {0, 4, 3, 2};
+  int best = 16, best_pol = 1, best_cps = 0;
   float best_ms = 1e30f;
+  bool warm = false;
   for (int k = 0; k < 3; ++k) {
     if (ms_out) ms_out[k] = -1;
     if (lpr != 0 && cand[k] != lpr) continue;
     for (int pol = 1; pol <= 2; ++pol) {
-      S.csr_lpr = cand[k];
-      S.csr_pol = pol;
-      launch_hv_stored(S, v, w, false, st);
-      cudaEventRecord(e0, st);
-      for (int r = 0; r < 3; ++r) launch_hv_stored(S, v, w, false, st);
-      cudaEventRecord(e1, st);
-      cudaEventSynchronize(e1);
-      float ms = 0;
-      cudaEventElapsedTime(&ms, e0, e1);
-      if (ms_out && (ms_out[k] < 0 || ms / 3 < ms_out[k])) ms_out[k] = ms / 3;
-      if (ms < best_ms) {
-        best_ms = ms;
-        best = cand[k];
-        best_pol = pol;
+      for (int c = 0; c < 4; ++c) {
+        S.csr_lpr = cand[k];
+        S.csr_pol = pol;
+        S.csr_cps = caps[c];
+        if (!warm) launch_hv_stored(S, v, w, false, st);
+        warm = true;
+        cudaEventRecord(e0, st);
+        for (int r = 0; r < 2; ++r) launch_hv_stored(S, v, w, false, st);
+        cudaEventRecord(e1, st);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms_out && (ms_out[k] < 0 || ms / 2 < ms_out[k])) ms_out[k] = ms / 2;
+        if (ms < best_ms) {
+          best_ms = ms;
+          best = cand[k];
+          best_pol = pol;
+          best_cps = caps[c];
+        }
       }
     }
   }
   S.csr_pol = best_pol;
+  S.csr_cps = best_cps;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaFree(v);

@@ -73,16 +73,18 @@ class GpuSector:
         """Choose the lanes per stored row and the cache policy of its loads by
         timing them on this sector (0: all lane counts; 8/16/32: that count).
         Returns (lanes, [best ms for 8, 16, 32], -1 where not timed); the
-        choices are also in ``info["lanes_per_row"]`` and ``info["cache_policy"]``."""
+        choices are also in ``info["lanes_per_row"]``, ``info["cache_policy"]``
+        and ``info["ctas_per_sm"]``."""
         ch = C.c_int()
         ms = np.zeros(3, np.float64)
         N.check(N.lib().edg_sector_tune(self._h, int(lanes_per_row), C.byref(ch), ms.ctypes.data))
         self.refresh_info()
         return ch.value, ms
 
-    def set_rows(self, lanes_per_row: int, cache_policy: int) -> None:
-        """Fix the stored-row kernel's lanes per row (8/16/32) and cache policy (1/2)."""
-        N.check(N.lib().edg_sector_set_rows(self._h, int(lanes_per_row), int(cache_policy)))
+    def set_rows(self, lanes_per_row: int, cache_policy: int, ctas_per_sm: int = 0) -> None:
+        """Fix the stored-row kernel's lanes per row (8/16/32), cache policy (1/2)
+        and CTAs per SM (0: as many as fit)."""
+        N.check(N.lib().edg_sector_set_rows(self._h, int(lanes_per_row), int(cache_policy), int(ctas_per_sm)))
         self.refresh_info()
 
     def pack_panels(self, n_panels: int = 0) -> None:
@@ -200,10 +202,12 @@ class GpuSector:
             nnz_off = self.count_offdiag()
         S = elem_bytes
         if self.info.get("n_targets", 0):
-            # stored rows: v_i, stabiliser byte, w_i; per nonzero u32 column,
-            # u16 value id and one u_j; row offsets and diagonal; the u pass
+            # stored rows: v_i, stabiliser byte, w_i; per nonzero its entry
+            # (4 bytes packed, 6 split) and one u_j; row offsets and diagonal;
+            # the u pass
             nnz = self.info["n_targets"]
-            return (self.n_p * (2 * S + 1) + nnz * (S + 6) + 8 * (self.n_p + 1) + 8 * self.n_p
+            entry = self.info.get("entry_bytes") or 6
+            return (self.n_p * (2 * S + 1) + nnz * (S + entry) + 8 * (self.n_p + 1) + 8 * self.n_p
                     + self.n_p * (2 * S + 1))
         return self.n_p * (8 + 1 + 2 * S) + nnz_off * S
 

@@ -17,7 +17,7 @@
 extern "C" {
 #endif
 
-#define EDGPU_ABI_VERSION 4
+#define EDGPU_ABI_VERSION 5
 
 enum {
   EDG_OK = 0,
@@ -71,6 +71,10 @@ typedef struct {
   int cache_policy;      /* stored-row H*v: 1 streaming row loads, 2 L2 evict-first row loads */
   int panels;            /* column panels of the stored rows (0: row order) */
   int L3, kz;            /* third translation's cycle length and momentum (1, 0 in 2-D) */
+  int entry_bytes;       /* bytes of one stored nonzero: 4 (column and value id packed in one
+                            u32), 6 (u32 column + u16 value id), 0 without stored rows */
+  int n_values;          /* distinct values of the stored rows' value table */
+  int ctas_per_sm;       /* stored-row H*v: CTAs per SM (0: as many as fit) */
 } edg_sector_info;
 
 const char* edg_last_error(void);
@@ -114,9 +118,12 @@ int edg_sector_copy_config_tables(const edg_sector* s, int64_t max_configs, int6
 int edg_hv(edg_sector* s, const void* v, void* w, int dtype, void* stream);
 
 /* Search every row's flipped states once and keep the result in HBM as
- * compressed sparse rows: per nonzero a u32 column and a u16 index into a
- * table of (pair coefficient x phase) values, per row its diagonal (6 bytes
- * per nonzero, 84 GB for the 36-site Sz=0 sector).  Afterwards edg_hv streams
+ * compressed sparse rows: per nonzero its column and an index into a
+ * deduplicated table of (pair coefficient x phase) values, per row its
+ * diagonal.  Column and index share one u32 when both fit (4 bytes per
+ * nonzero, 56 GB for the 36-site Sz=0, k=0 sector), else a u32 column and a
+ * u16 index (6 bytes; the environment variable EDG_ROW_FORMAT=split forces
+ * this form).  Afterwards edg_hv streams
  * these rows instead of searching orbits.  Fails with EDG_ERR_NOMEM (sector
  * unchanged, still matrix-free) when they need more than max_bytes (<= 0: no
  * limit) or than is free; EDG_ERR_UNSUPPORTED for ChCh terms or more than
@@ -126,17 +133,19 @@ int edg_hv(edg_sector* s, const void* v, void* w, int dtype, void* stream);
 int edg_sector_build_targets(edg_sector* s, int64_t max_bytes);
 int edg_sector_free_targets(edg_sector* s);
 
-/* Lanes of a warp per stored row (8, 16 or 32, i.e. 4, 2 or 1 rows per warp)
- * and the cache policy of the row loads, timed on this sector: a nonzero
- * lanes_per_row fixes the lanes and times the two policies, 0 times all six
- * combinations.  The fastest is kept.  *chosen receives the lanes, ms (NULL
- * allowed) the best time of 8, 16 and 32 lanes in that order (-1: not timed);
- * edg_sector_info reports both choices. */
+/* Lanes of a warp per stored row (8, 16 or 32, i.e. 4, 2 or 1 rows per warp),
+ * the cache policy of the row loads and the CTAs per SM (as many as fit, or
+ * at most 4, 3 or 2: fewer rows in flight keep the gathered part of v in L2),
+ * timed on this sector: a nonzero lanes_per_row fixes the lanes and times the
+ * rest, 0 times every lane count.  The fastest is kept.  *chosen receives the
+ * lanes, ms (NULL allowed) the best time of 8, 16 and 32 lanes in that order
+ * (-1: not timed); edg_sector_info reports the three choices. */
 int edg_sector_tune(edg_sector* s, int lanes_per_row, int* chosen, double* ms);
 
-/* Set both choices without timing: lanes_per_row 8, 16 or 32, cache_policy 1
- * or 2.  Results do not depend on either; only the speed does. */
-int edg_sector_set_rows(edg_sector* s, int lanes_per_row, int cache_policy);
+/* Set the three choices without timing: lanes_per_row 8, 16 or 32,
+ * cache_policy 1 or 2, ctas_per_sm 0 (as many as fit) to 32.  Results do not
+ * depend on them; only the speed does. */
+int edg_sector_set_rows(edg_sector* s, int lanes_per_row, int cache_policy, int ctas_per_sm);
 
 /* Regroup the stored rows into column panels: rows in blocks of 64, columns
  * in n_panels slices (<= 0: enough for each slice of u to fit in 64 MB of L2

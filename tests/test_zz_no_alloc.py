@@ -72,6 +72,37 @@ def test_noalloc_matches_edg_hv_on_consecutive_calls(sectors, dtype):
         assert np.abs(a - b).max() / max(1.0, np.abs(b).max()) <= TOL[dtype]
 
 
+@pytest.mark.parametrize("dtype", ["complex128", "complex64"])
+def test_noalloc_reads_both_entry_formats(cuda_device, monkeypatch, dtype):
+    """Stored rows come packed (column and value id in one u32) or split (two
+    arrays, EDG_ROW_FORMAT=split): the call reads either."""
+    import torch
+    from ed_code_gb300 import _native as N
+    from ed_code_gb300 import sector
+
+    lib = N.lib()
+    tdt = getattr(torch, dtype)
+    st = torch.cuda.current_stream().cuda_stream
+    monkeypatch.setenv("EDG_ROW_FORMAT", "split")
+    split = sector.GpuSector(golden_model("tri6x4_k10", 0))
+    assert split.build_targets() and split.info["entry_bytes"] == 6
+    monkeypatch.delenv("EDG_ROW_FORMAT")
+    packed = sector.GpuSector(golden_model("tri6x4_k10", 0))
+    assert packed.build_targets() and packed.info["entry_bytes"] == 4
+    v = _rand(split.n_p, tdt, 21)
+    outs = {}
+    for name, sec in (("split", split), ("packed", packed)):
+        w = torch.empty_like(v)
+        _hv(lib.edg_hv_noalloc, sec, v, w, st)
+        ref = torch.empty_like(v)
+        _hv(lib.edg_hv, sec, v, ref, st)
+        torch.cuda.synchronize()
+        a, b = w.cpu().numpy().astype(np.complex128), ref.cpu().numpy().astype(np.complex128)
+        assert np.abs(a - b).max() / max(1.0, np.abs(b).max()) <= TOL[dtype], name
+        outs[name] = a
+    assert np.array_equal(outs["split"], outs["packed"])
+
+
 def test_noalloc_rejects_what_it_cannot_serve(cuda_device):
     import torch
     from ed_code_gb300 import _native as N
