@@ -256,8 +256,8 @@ def run_device(args, world, rank, local_rank):
             mode = "stored-rows"
             B = sec.algorithmic_bytes(elem, nnz)
             if args.rows:
-                lanes, pol, *cps = (int(x) for x in args.rows.split(","))
-                sec.set_rows(lanes, pol, cps[0] if cps else 0)
+                lanes, pol, *rest = (int(x) for x in args.rows.split(","))
+                sec.set_rows(lanes, pol, *rest)
                 lpr = lanes
             else:
                 lpr, tune_ms = sec.tune(0)
@@ -335,7 +335,7 @@ def run_device(args, world, rank, local_rank):
                    "entry_bytes": sec.info.get("entry_bytes"), "n_values": sec.info.get("n_values"),
                    "matrix_free_ms_per_step": mf_ms,
                    "lanes_per_row": lpr, "cache_policy": sec.info.get("cache_policy"),
-                   "ctas_per_sm": sec.info.get("ctas_per_sm"),
+                   "ctas_per_sm": sec.info.get("ctas_per_sm"), "pipelined": sec.info.get("pipelined"),
                    "panels": sec.info.get("panels"), "panel_pack_seconds": None if t_pack is None else round(t_pack, 3),
                    "row_kernel_ms": None if tune_ms is None else round(float(min(x for x in tune_ms if x > 0)), 3),
                    "tune_ms_lpr_8_16_32": None if tune_ms is None else [round(float(x), 3) for x in tune_ms],
@@ -600,7 +600,7 @@ def main():
     ap.add_argument("--matrix-free", action="store_true", help="do not store the searched targets")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--rows", default=None,
-                    help="LANES,POLICY[,CTAS_PER_SM]: fix the stored-row kernel instead of timing it")
+                    help="LANES,POLICY[,CTAS_PER_SM[,PIPELINED]]: fix the stored-row kernel instead of timing it")
     ap.add_argument("--panels", type=int, default=0,
                     help="regroup the stored rows into this many column panels (0: keep the row kernel)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)

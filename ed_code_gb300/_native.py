@@ -55,7 +55,7 @@ class edg_sector_info(C.Structure):
         ("ky", C.c_int), ("torus", C.c_int), ("n_groups", C.c_int), ("n_p", C.c_int64), ("n_configs", C.c_int64),
         ("device_bytes", C.c_int64), ("n_targets", C.c_int64), ("lanes_per_row", C.c_int),
         ("cache_policy", C.c_int), ("panels", C.c_int), ("L3", C.c_int), ("kz", C.c_int),
-        ("entry_bytes", C.c_int), ("n_values", C.c_int), ("ctas_per_sm", C.c_int),
+        ("entry_bytes", C.c_int), ("n_values", C.c_int), ("ctas_per_sm", C.c_int), ("pipelined", C.c_int),
     ]
 
 
@@ -115,7 +115,7 @@ SIGNATURES = {
     "edg_sector_copy_config_tables": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
     "edg_hv": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "edg_hv_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
-    "edg_sector_set_rows": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
+    "edg_sector_set_rows": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]),
     "edg_sector_pack_panels": (C.c_int, [C.c_void_p, C.c_int]),
     "edg_batch_create": (C.c_int, [C.POINTER(edg_batch_opts), C.POINTER(C.c_void_p)]),
     "edg_batch_destroy": (C.c_int, [C.c_void_p]),

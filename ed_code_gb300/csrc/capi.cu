@@ -515,6 +515,7 @@ int edg_sector_get_info(const edg_sector* s, edg_sector_info* info) {
   info->lanes_per_row = s->s.col ? s->s.csr_lpr : 0;
   info->cache_policy = s->s.col ? s->s.csr_pol : 0;
   info->ctas_per_sm = s->s.col ? s->s.csr_cps : 0;
+  info->pipelined = s->s.col ? s->s.csr_pipe : 0;
   info->panels = s->s.pan_p;
   info->entry_bytes = s->s.col ? (s->s.pack_cb ? 4 : 6) : (s->s.pan_ent ? 6 : 0);
   info->n_values = s->s.n_vals;
@@ -701,7 +702,7 @@ int edg_sector_pack_panels(edg_sector* s, int n_panels) {
   return EDG_OK;
 }
 
-int edg_sector_set_rows(edg_sector* s, int lanes_per_row, int cache_policy, int ctas_per_sm) {
+int edg_sector_set_rows(edg_sector* s, int lanes_per_row, int cache_policy, int ctas_per_sm, int pipelined) {
   if (!s) return fail(EDG_ERR_INVALID, "NULL sector");
   if (lanes_per_row != 8 && lanes_per_row != 16 && lanes_per_row != 32)
     return fail(EDG_ERR_INVALID, "lanes_per_row must be 8, 16 or 32");
@@ -709,7 +710,9 @@ int edg_sector_set_rows(edg_sector* s, int lanes_per_row, int cache_policy, int 
   if (ctas_per_sm < 0 || ctas_per_sm > 32) return fail(EDG_ERR_INVALID, "ctas_per_sm must be 0 to 32");
   s->s.csr_lpr = lanes_per_row;
   s->s.csr_pol = cache_policy;
+  if (pipelined != 0 && pipelined != 1) return fail(EDG_ERR_INVALID, "pipelined must be 0 or 1");
   s->s.csr_cps = ctas_per_sm;
+  s->s.csr_pipe = pipelined;
   return EDG_OK;
 }
 

@@ -79,36 +79,69 @@ __device__ __forceinline__ void ld_entry(const uint32_t* col, const uint16_t* vi
   }
 }
 
-// One CSR row, handled by LPR lanes of a warp (sl = lane within the row).
-// The row's first LPR*kU entries are resolved in one unrolled step -- all
-// entry loads, then all gathers -- longer rows finish in a loop.
-// Returns the row sum in lane sl == 0 after a segmented reduction.
-template <typename Real, int LPR, bool kSmemTab, int kPol, int kFmt>
-__device__ __forceinline__ void csr_row(uint64_t beg, uint64_t end, int sl, const uint32_t* __restrict__ col,
-                                        const uint16_t* __restrict__ vid, int cb, const typename CT2<Real>::T* vtab,
-                                        const typename CT2<Real>::T* __restrict__ u, Real& ar, Real& ai) {
-  using CT = typename CT2<Real>::T;
-  constexpr int kU = 64 / LPR < 2 ? 2 : 64 / LPR;
-  ar = 0;
-  ai = 0;
-  const uint64_t pf = kPol == 2 ? l2_evict_first() : 0, pl = l2_evict_last();
-  uint32_t j[kU];
-  int id[kU];
+// Entries a lane resolves in the unrolled head of a row (LPR lanes a row).
+template <int LPR>
+__host__ __device__ constexpr int head_entries() {
+  return 64 / LPR < 2 ? 2 : 64 / LPR;
+}
+
+// The head of one CSR row: lane sl loads entries beg + sl + LPR*q (q < kU) as
+// stored (e: the u32 word, h: the u16 value id of split rows), all ones past
+// the row's end.  No valid entry is all ones (a column is below n_p < 2^32 - 1,
+// and below 2^cb when packed).
+template <int LPR, int kFmt, int kPol>
+__device__ __forceinline__ void csr_head(uint64_t beg, uint64_t end, int sl, const uint32_t* __restrict__ col,
+                                         const uint16_t* __restrict__ vid, uint64_t pf,
+                                         uint32_t (&e)[head_entries<LPR>()], uint16_t (&h)[head_entries<LPR>()]) {
+  constexpr int kU = head_entries<LPR>();
+  const bool packed = kFmt == kPacked || (kFmt == kByVid && vid == nullptr);
 #pragma unroll
   for (int q = 0; q < kU; ++q) {
     const uint64_t t = beg + sl + LPR * q;
-    j[q] = 0xFFFFFFFFu;
-    id[q] = 0;
-    if (t < end) ld_entry<kFmt, kPol>(col, vid, t, cb, pf, j[q], id[q]);
+    e[q] = 0xFFFFFFFFu;
+    h[q] = 0;
+    if (t < end) {
+      e[q] = ld_row<kPol>(col + t, pf);
+      if (!packed) h[q] = (uint16_t)ld_row<kPol>(vid + t, pf);
+    }
   }
-  CT x[kU];
+}
+
+// The head's gathers: x[q] = u[column of e[q]] for the valid entries.
+template <typename Real, int LPR, int kFmt>
+__device__ __forceinline__ void csr_gather(const uint16_t* vid, int cb, const typename CT2<Real>::T* __restrict__ u,
+                                           uint64_t pl, const uint32_t (&e)[head_entries<LPR>()],
+                                           typename CT2<Real>::T (&x)[head_entries<LPR>()]) {
+  constexpr int kU = head_entries<LPR>();
+  const bool packed = kFmt == kPacked || (kFmt == kByVid && vid == nullptr);
+  const uint32_t cmask = packed ? (1u << cb) - 1u : 0xFFFFFFFFu;
 #pragma unroll
   for (int q = 0; q < kU; ++q)
-    if (j[q] != 0xFFFFFFFFu) x[q] = ld_keep(u + j[q], pl);
+    if (e[q] != 0xFFFFFFFFu) x[q] = ld_keep(u + (e[q] & cmask), pl);
+}
+
+// The row sum once the head's gathers are issued: the head's products, then
+// the entries past the head in a loop, then a segmented reduction that
+// leaves the row sum in lane sl == 0.
+template <typename Real, int LPR, bool kSmemTab, int kPol, int kFmt>
+__device__ __forceinline__ void csr_consume(uint64_t beg, uint64_t end, int sl, const uint32_t* __restrict__ col,
+                                            const uint16_t* __restrict__ vid, int cb,
+                                            const typename CT2<Real>::T* vtab,
+                                            const typename CT2<Real>::T* __restrict__ u, uint64_t pf, uint64_t pl,
+                                            const uint32_t (&e)[head_entries<LPR>()],
+                                            const uint16_t (&h)[head_entries<LPR>()],
+                                            const typename CT2<Real>::T (&x)[head_entries<LPR>()], Real& ar,
+                                            Real& ai) {
+  using CT = typename CT2<Real>::T;
+  constexpr int kU = head_entries<LPR>();
+  const bool packed = kFmt == kPacked || (kFmt == kByVid && vid == nullptr);
+  ar = 0;
+  ai = 0;
 #pragma unroll
   for (int q = 0; q < kU; ++q) {
-    if (j[q] == 0xFFFFFFFFu) continue;
-    const CT c = kSmemTab ? vtab[id[q]] : __ldg(vtab + id[q]);
+    if (e[q] == 0xFFFFFFFFu) continue;
+    const int id = packed ? (int)(e[q] >> cb) : (int)h[q];
+    const CT c = kSmemTab ? vtab[id] : __ldg(vtab + id);
     ar += c.x * x[q].x - c.y * x[q].y;
     ai += c.x * x[q].y + c.y * x[q].x;
   }
@@ -126,6 +159,35 @@ __device__ __forceinline__ void csr_row(uint64_t beg, uint64_t end, int sl, cons
     ar += __shfl_down_sync(0xffffffffu, ar, o, LPR);
     ai += __shfl_down_sync(0xffffffffu, ai, o, LPR);
   }
+}
+
+// Gathers and row sum of a row whose head is loaded.
+template <typename Real, int LPR, bool kSmemTab, int kPol, int kFmt>
+__device__ __forceinline__ void csr_finish(uint64_t beg, uint64_t end, int sl, const uint32_t* __restrict__ col,
+                                           const uint16_t* __restrict__ vid, int cb,
+                                           const typename CT2<Real>::T* vtab,
+                                           const typename CT2<Real>::T* __restrict__ u, uint64_t pf, uint64_t pl,
+                                           const uint32_t (&e)[head_entries<LPR>()],
+                                           const uint16_t (&h)[head_entries<LPR>()], Real& ar, Real& ai) {
+  typename CT2<Real>::T x[head_entries<LPR>()];
+  csr_gather<Real, LPR, kFmt>(vid, cb, u, pl, e, x);
+  csr_consume<Real, LPR, kSmemTab, kPol, kFmt>(beg, end, sl, col, vid, cb, vtab, u, pf, pl, e, h, x, ar, ai);
+}
+
+// One CSR row, handled by LPR lanes of a warp (sl = lane within the row).
+// The row's first LPR*kU entries are resolved in one unrolled step -- all
+// entry loads, then all gathers -- longer rows finish in a loop.
+// Returns the row sum in lane sl == 0 after a segmented reduction.
+template <typename Real, int LPR, bool kSmemTab, int kPol, int kFmt>
+__device__ __forceinline__ void csr_row(uint64_t beg, uint64_t end, int sl, const uint32_t* __restrict__ col,
+                                        const uint16_t* __restrict__ vid, int cb, const typename CT2<Real>::T* vtab,
+                                        const typename CT2<Real>::T* __restrict__ u, Real& ar, Real& ai) {
+  constexpr int kU = head_entries<LPR>();
+  const uint64_t pf = kPol == 2 ? l2_evict_first() : 0, pl = l2_evict_last();
+  uint32_t e[kU];
+  uint16_t h[kU];
+  csr_head<LPR, kFmt, kPol>(beg, end, sl, col, vid, pf, e, h);
+  csr_finish<Real, LPR, kSmemTab, kPol, kFmt>(beg, end, sl, col, vid, cb, vtab, u, pf, pl, e, h, ar, ai);
 }
 
 }  // namespace

@@ -106,6 +106,7 @@ struct Sector {
   int csr_lpr = 16;             // lanes per CSR row (8, 16 or 32): edg_sector_tune
   int csr_pol = 1;              // cache policy of the CSR loads (1 or 2): edg_sector_tune
   int csr_cps = 0;              // CTAs per SM of the CSR kernel (0: as many as fit): edg_sector_tune
+  int csr_pipe = 0;             // 1: the CSR kernel loads the next rows' entries ahead: edg_sector_tune
   // column panels (edg_sector_pack_panels): the stored rows regrouped so that
   // one H*v launch per panel gathers from one L2-sized slice of u
   uint32_t* pan_ent = nullptr;  // (column - p*pan_c) | local row << 23

@@ -253,10 +253,17 @@ __global__ void k_u_scale(const typename CT2<Real>::T* __restrict__ v, const uin
   }
 }
 
-// CSR SpMV with a value dictionary: 32/LPR rows per warp, the next rows'
-// offsets loaded while the current ones run.  kFmt: kSplit or kPacked entries
-// (csr_row.cuh), cb the column bits of a packed entry.
-template <typename Real, int LPR, bool kSmemTab, int kPol, int kFmt>
+// CSR SpMV with a value dictionary: 32/LPR rows per warp, a warp's row
+// groups a grid stride apart.  kFmt: kSplit or kPacked entries (csr_row.cuh),
+// cb the column bits of a packed entry.  kPipe sets how far a warp loads
+// ahead of the group it sums:
+//   0: the next group's offsets;
+//   1: also the next group's head entries, so their DRAM latency overlaps
+//      the current group's gathers instead of preceding them.
+// The sums are the same bits either way.  (Loading the next group's gathers
+// as well, two groups' gathers in flight per warp, measured slower at 36
+// sites: 74.7 ms against 60.6 ms at 2 CTAs per SM.)
+template <typename Real, int LPR, bool kSmemTab, int kPol, int kFmt, int kPipe>
 __global__ void __launch_bounds__(kTgtThreads) k_hv_csr(const uint64_t* __restrict__ row_ptr,
                                                         const uint32_t* __restrict__ col,
                                                         const uint16_t* __restrict__ vid, int cb,
@@ -270,6 +277,7 @@ __global__ void __launch_bounds__(kTgtThreads) k_hv_csr(const uint64_t* __restri
   // rows [row0, n_p)
   using CT = typename CT2<Real>::T;
   constexpr int kRows = 32 / LPR;  // rows per warp
+  constexpr int kU = head_entries<LPR>();
   extern __shared__ __align__(16) uint8_t sm[];
   __shared__ Real nrm[65];
   CT* tab = reinterpret_cast<CT*>(sm);
@@ -277,38 +285,70 @@ __global__ void __launch_bounds__(kTgtThreads) k_hv_csr(const uint64_t* __restri
   if (kSmemTab)
     for (int k = threadIdx.x; k < n_vals; k += blockDim.x) tab[k] = vtab[k];
   __syncthreads();
+  const CT* vt = kSmemTab ? tab : vtab;
   const int lane = threadIdx.x & 31, sl = lane % LPR, sub = lane / LPR;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int64_t stride = n_warps * kRows;
   const unsigned long long* rp = reinterpret_cast<const unsigned long long*>(row_ptr);
-  int64_t i = row0 + warp * kRows + sub;
-  uint64_t beg = 0, end = 0;
-  if (i < n_p) {
-    beg = __ldg(rp + i);
-    end = __ldg(rp + i + 1);
-  }
-  for (int64_t base = row0 + warp * kRows; base < n_p; base += n_warps * kRows) {
-    const int64_t inext = i + n_warps * kRows;
-    uint64_t nbeg = 0, nend = 0;
-    if (inext < n_p) {
-      nbeg = __ldg(rp + inext);
-      nend = __ldg(rp + inext + 1);
+  const uint64_t pf = kPol == 2 ? l2_evict_first() : 0, pl = l2_evict_last();
+  auto offsets = [&](int64_t r, uint64_t& b, uint64_t& e) {
+    b = e = 0;
+    if (r < n_p) {
+      b = __ldg(rp + r);
+      e = __ldg(rp + r + 1);
     }
-    Real ar, ai;
-    csr_row<Real, LPR, kSmemTab, kPol, kFmt>(beg, i < n_p ? end : beg, sl, col, vid, cb, kSmemTab ? tab : vtab, u, ar,
-                                             ai);
-    if (sl == 0 && i < n_p) {
-      const CT vi = v[i];
-      const Real ni = nrm[lid[i]];
-      const Real d = (Real)ezz[i];
+  };
+  auto store = [&](int64_t r, Real ar, Real ai) {
+    if (sl == 0 && r < n_p) {
+      const CT vi = v[r];
+      const Real ni = nrm[lid[r]];
+      const Real d = (Real)ezz[r];
       CT out;
       out.x = ar * ni + d * vi.x;
       out.y = ai * ni + d * vi.y;
-      w[i] = out;
+      w[r] = out;
     }
-    i = inext;
-    beg = nbeg;
-    end = nend;
+  };
+  int64_t i = row0 + warp * kRows + sub;
+  uint64_t beg, end, beg1, end1;
+  offsets(i, beg, end);
+  offsets(i + stride, beg1, end1);
+  if (kPipe == 0) {
+    for (int64_t base = row0 + warp * kRows; base < n_p; base += stride) {
+      Real ar, ai;
+      csr_row<Real, LPR, kSmemTab, kPol, kFmt>(beg, end, sl, col, vid, cb, vt, u, ar, ai);
+      store(i, ar, ai);
+      i += stride;
+      beg = beg1;
+      end = end1;
+      offsets(i + stride, beg1, end1);
+    }
+  } else {
+    uint32_t e[kU];
+    uint16_t h[kU];
+    csr_head<LPR, kFmt, kPol>(beg, end, sl, col, vid, pf, e, h);
+    for (int64_t base = row0 + warp * kRows; base < n_p; base += stride) {
+      // group k+2's offsets, group k+1's head, then group k's gathers
+      uint64_t beg2, end2;
+      offsets(i + 2 * stride, beg2, end2);
+      uint32_t en[kU];
+      uint16_t hn[kU];
+      csr_head<LPR, kFmt, kPol>(beg1, end1, sl, col, vid, pf, en, hn);
+      Real ar, ai;
+      csr_finish<Real, LPR, kSmemTab, kPol, kFmt>(beg, end, sl, col, vid, cb, vt, u, pf, pl, e, h, ar, ai);
+      store(i, ar, ai);
+      i += stride;
+      beg = beg1;
+      end = end1;
+      beg1 = beg2;
+      end1 = end2;
+#pragma unroll
+      for (int q = 0; q < kU; ++q) {
+        e[q] = en[q];
+        h[q] = hn[q];
+      }
+    }
   }
 }
 
@@ -334,7 +374,7 @@ const double* params_field(const Sector& S, size_t offset) {
 }
 
 // rows [r0, r1); u = v / norm first when with_u
-template <typename Real, int LPR, int kPol, int kFmt>
+template <typename Real, int LPR, int kPol, int kFmt, int kPipe>
 cudaError_t launch_csr_lpr(const Sector& S, const void* v, void* w, cudaStream_t st, int64_t r0, int64_t r1,
                            bool with_u) {
   using CT = typename CT2<Real>::T;
@@ -349,12 +389,12 @@ cudaError_t launch_csr_lpr(const Sector& S, const void* v, void* w, cudaStream_t
   if (r1 <= r0) return cudaGetLastError();
   const int64_t threads_needed = ((r1 - r0) * LPR + 31) / 32 * 32;
   if (tab_bytes <= 96 * 1024) {
-    auto kern = k_hv_csr<Real, LPR, true, kPol, kFmt>;
+    auto kern = k_hv_csr<Real, LPR, true, kPol, kFmt, kPipe>;
     kern<<<grid_for(kern, tab_bytes, threads_needed, kTgtThreads, S.csr_cps), kTgtThreads, tab_bytes, st>>>(
         S.row_ptr, S.col, S.vid, S.pack_cb, tab, S.n_vals, S.ezz, S.lid, nrm, r0, r1, reinterpret_cast<const CT*>(v),
         reinterpret_cast<const CT*>(S.ubuf.ptr), reinterpret_cast<CT*>(w));
   } else {
-    auto kern = k_hv_csr<Real, LPR, false, kPol, kFmt>;
+    auto kern = k_hv_csr<Real, LPR, false, kPol, kFmt, kPipe>;
     kern<<<grid_for(kern, 0, threads_needed, kTgtThreads, S.csr_cps), kTgtThreads, 0, st>>>(
         S.row_ptr, S.col, S.vid, S.pack_cb, tab, S.n_vals, S.ezz, S.lid, nrm, r0, r1, reinterpret_cast<const CT*>(v),
         reinterpret_cast<const CT*>(S.ubuf.ptr), reinterpret_cast<CT*>(w));
@@ -365,10 +405,13 @@ cudaError_t launch_csr_lpr(const Sector& S, const void* v, void* w, cudaStream_t
 template <typename Real, int kPol, int kFmt>
 cudaError_t launch_csr_f(const Sector& S, const void* v, void* w, cudaStream_t st, int64_t r0, int64_t r1,
                          bool with_u) {
-  switch (S.csr_lpr) {
-    case 8: return launch_csr_lpr<Real, 8, kPol, kFmt>(S, v, w, st, r0, r1, with_u);
-    case 16: return launch_csr_lpr<Real, 16, kPol, kFmt>(S, v, w, st, r0, r1, with_u);
-    default: return launch_csr_lpr<Real, 32, kPol, kFmt>(S, v, w, st, r0, r1, with_u);
+  switch (S.csr_pipe * 3 + (S.csr_lpr == 8 ? 0 : S.csr_lpr == 16 ? 1 : 2)) {
+    case 0: return launch_csr_lpr<Real, 8, kPol, kFmt, 0>(S, v, w, st, r0, r1, with_u);
+    case 1: return launch_csr_lpr<Real, 16, kPol, kFmt, 0>(S, v, w, st, r0, r1, with_u);
+    case 2: return launch_csr_lpr<Real, 32, kPol, kFmt, 0>(S, v, w, st, r0, r1, with_u);
+    case 3: return launch_csr_lpr<Real, 8, kPol, kFmt, 1>(S, v, w, st, r0, r1, with_u);
+    case 4: return launch_csr_lpr<Real, 16, kPol, kFmt, 1>(S, v, w, st, r0, r1, with_u);
+    default: return launch_csr_lpr<Real, 32, kPol, kFmt, 1>(S, v, w, st, r0, r1, with_u);
   }
 }
 
@@ -946,12 +989,14 @@ int build_targets(Sector& S, int64_t max_bytes, std::string& err) {
   return e == cudaSuccess ? EDG_OK : EDG_ERR_CUDA;
 }
 
-// Lanes per CSR row, cache policy and CTAs per SM.  lpr in {8, 16, 32} fixes
-// the lanes and times the rest; 0 times every lane count.  Each combination
-// runs twice (FP32) after one warm-up launch, and the fastest is kept.  The
-// CTA cap matters because the gathers reuse u through L2: fewer rows in
-// flight keep their targets' window of u smaller.  ms_out[k] receives the
-// best time of lane count 8, 16, 32 (-1 when not timed).
+// Lanes per CSR row, cache policy, CTAs per SM and pipelining.  lpr in
+// {8, 16, 32} fixes the lanes; 0 times every lane count.  First every (lanes,
+// pipelining 0/1, CTA cap in {as many as fit, 4, 3, 2, 1}) with cache policy 2,
+// then the best of those with policy 1.  Each combination runs twice (FP32)
+// after one warm-up launch, and the fastest is kept.  The CTA cap matters
+// because the gathers reuse u through L2: fewer rows in flight keep their
+// targets' window of u smaller.  ms_out[k] receives the best time of lane
+// count 8, 16, 32 (-1 when not timed).
 int tune_rows(Sector& S, int lpr, int* chosen, double* ms_out) {
   if (!S.col) {
     if (chosen) *chosen = 0;
@@ -969,44 +1014,54 @@ int tune_rows(Sector& S, int lpr, int* chosen, double* ms_out) {
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  const int cand[3] = {8, 16, 32};
-  const int caps[4] = {0, 4, 3, 2};
-  int best = 16, best_pol = 1, best_cps = 0;
-  float best_ms = 1e30f;
   bool warm = false;
+  auto time_it = [&]() {
+    if (!warm) launch_hv_stored(S, v, w, false, st);
+    warm = true;
+    cudaEventRecord(e0, st);
+    for (int r = 0; r < 2; ++r) launch_hv_stored(S, v, w, false, st);
+    cudaEventRecord(e1, st);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    return ms / 2;
+  };
+  const int cand[3] = {8, 16, 32};
+  const int caps[5] = {0, 4, 3, 2, 1};
+  int best = 16, best_cps = 0, best_pipe = 0;
+  float best_ms = 1e30f;
   for (int k = 0; k < 3; ++k) {
     if (ms_out) ms_out[k] = -1;
     if (lpr != 0 && cand[k] != lpr) continue;
-    for (int pol = 1; pol <= 2; ++pol) {
-      for (int c = 0; c < 4; ++c) {
+    for (int pipe = 0; pipe < 2; ++pipe) {
+      for (int c = 0; c < 5; ++c) {
         S.csr_lpr = cand[k];
-        S.csr_pol = pol;
+        S.csr_pol = 2;
         S.csr_cps = caps[c];
-        if (!warm) launch_hv_stored(S, v, w, false, st);
-        warm = true;
-        cudaEventRecord(e0, st);
-        for (int r = 0; r < 2; ++r) launch_hv_stored(S, v, w, false, st);
-        cudaEventRecord(e1, st);
-        cudaEventSynchronize(e1);
-        float ms = 0;
-        cudaEventElapsedTime(&ms, e0, e1);
-        if (ms_out && (ms_out[k] < 0 || ms / 2 < ms_out[k])) ms_out[k] = ms / 2;
+        S.csr_pipe = pipe;
+        const float ms = time_it();
+        if (ms_out && (ms_out[k] < 0 || ms < ms_out[k])) ms_out[k] = ms;
         if (ms < best_ms) {
           best_ms = ms;
           best = cand[k];
-          best_pol = pol;
           best_cps = caps[c];
+          best_pipe = pipe;
         }
       }
     }
   }
-  S.csr_pol = best_pol;
+  S.csr_lpr = best;
   S.csr_cps = best_cps;
+  S.csr_pipe = best_pipe;
+  S.csr_pol = 1;
+  const float ms1 = time_it();
+  const int k = best == 8 ? 0 : best == 16 ? 1 : 2;
+  if (ms_out && ms1 < ms_out[k]) ms_out[k] = ms1;
+  if (ms1 >= best_ms) S.csr_pol = 2;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaFree(v);
   cudaFree(w);
-  S.csr_lpr = best;
   if (chosen) *chosen = best;
   return cudaGetLastError() == cudaSuccess ? EDG_OK : EDG_ERR_CUDA;
 }

@@ -73,18 +73,19 @@ class GpuSector:
         """Choose the lanes per stored row and the cache policy of its loads by
         timing them on this sector (0: all lane counts; 8/16/32: that count).
         Returns (lanes, [best ms for 8, 16, 32], -1 where not timed); the
-        choices are also in ``info["lanes_per_row"]``, ``info["cache_policy"]``
-        and ``info["ctas_per_sm"]``."""
+        choices are also in ``info["lanes_per_row"]``, ``info["cache_policy"]``,
+        ``info["ctas_per_sm"]`` and ``info["pipelined"]``."""
         ch = C.c_int()
         ms = np.zeros(3, np.float64)
         N.check(N.lib().edg_sector_tune(self._h, int(lanes_per_row), C.byref(ch), ms.ctypes.data))
         self.refresh_info()
         return ch.value, ms
 
-    def set_rows(self, lanes_per_row: int, cache_policy: int, ctas_per_sm: int = 0) -> None:
-        """Fix the stored-row kernel's lanes per row (8/16/32), cache policy (1/2)
-        and CTAs per SM (0: as many as fit)."""
-        N.check(N.lib().edg_sector_set_rows(self._h, int(lanes_per_row), int(cache_policy), int(ctas_per_sm)))
+    def set_rows(self, lanes_per_row: int, cache_policy: int, ctas_per_sm: int = 0, pipelined: int = 0) -> None:
+        """Fix the stored-row kernel's lanes per row (8/16/32), cache policy (1/2),
+        CTAs per SM (0: as many as fit) and pipelining (0/1)."""
+        N.check(N.lib().edg_sector_set_rows(self._h, int(lanes_per_row), int(cache_policy), int(ctas_per_sm),
+                                            int(pipelined)))
         self.refresh_info()
 
     def pack_panels(self, n_panels: int = 0) -> None:

@@ -75,6 +75,7 @@ typedef struct {
                             u32), 6 (u32 column + u16 value id), 0 without stored rows */
   int n_values;          /* distinct values of the stored rows' value table */
   int ctas_per_sm;       /* stored-row H*v: CTAs per SM (0: as many as fit) */
+  int pipelined;         /* stored-row H*v: 1 when the next rows' entries load during the gathers */
 } edg_sector_info;
 
 const char* edg_last_error(void);
@@ -134,18 +135,19 @@ int edg_sector_build_targets(edg_sector* s, int64_t max_bytes);
 int edg_sector_free_targets(edg_sector* s);
 
 /* Lanes of a warp per stored row (8, 16 or 32, i.e. 4, 2 or 1 rows per warp),
- * the cache policy of the row loads and the CTAs per SM (as many as fit, or
- * at most 4, 3 or 2: fewer rows in flight keep the gathered part of v in L2),
- * timed on this sector: a nonzero lanes_per_row fixes the lanes and times the
- * rest, 0 times every lane count.  The fastest is kept.  *chosen receives the
- * lanes, ms (NULL allowed) the best time of 8, 16 and 32 lanes in that order
- * (-1: not timed); edg_sector_info reports the three choices. */
+ * the cache policy of the row loads, the CTAs per SM (as many as fit, or at
+ * most 4, 3, 2 or 1: fewer rows in flight keep the gathered part of v in L2)
+ * and pipelining (1: the next rows' entries loaded while the current rows
+ * gather), timed on this sector: a nonzero lanes_per_row fixes the lanes and times the rest, 0 times
+ * every lane count.  The fastest is kept.  *chosen receives the lanes, ms
+ * (NULL allowed) the best time of 8, 16 and 32 lanes in that order (-1: not
+ * timed); edg_sector_info reports the four choices. */
 int edg_sector_tune(edg_sector* s, int lanes_per_row, int* chosen, double* ms);
 
-/* Set the three choices without timing: lanes_per_row 8, 16 or 32,
- * cache_policy 1 or 2, ctas_per_sm 0 (as many as fit) to 32.  Results do not
- * depend on them; only the speed does. */
-int edg_sector_set_rows(edg_sector* s, int lanes_per_row, int cache_policy, int ctas_per_sm);
+/* Set the four choices without timing: lanes_per_row 8, 16 or 32,
+ * cache_policy 1 or 2, ctas_per_sm 0 (as many as fit) to 32, pipelined 0 or
+ * 1.  Results do not depend on them, bit for bit; only the speed does. */
+int edg_sector_set_rows(edg_sector* s, int lanes_per_row, int cache_policy, int ctas_per_sm, int pipelined);
 
 /* Regroup the stored rows into column panels: rows in blocks of 64, columns
  * in n_panels slices (<= 0: enough for each slice of u to fit in 64 MB of L2

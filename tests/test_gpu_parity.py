@@ -145,10 +145,10 @@ def test_stored_rows_every_kernel_choice(gpu, lanes, policy):
     assert np.abs(w32 - w0_32).max() <= FP32_TOL * scale
 
 
-def test_stored_rows_cta_cap_changes_speed_only(gpu):
-    """Each row is summed by the same lanes in the same order whatever the grid,
-    so capping the CTAs per SM gives the same bits; the tuner's choice is one of
-    the timed caps."""
+def test_stored_rows_cta_cap_and_pipelining_change_speed_only(gpu):
+    """Each row is summed by the same lanes in the same order whatever the grid
+    and whether its entries were loaded ahead, so capping the CTAs per SM and
+    pipelining give the same bits; the tuner's choices are among those timed."""
     from ed_code_gb300 import lattice as L
 
     model = L.make_model(L.TorusSpec("triangular", 5, 4, Jz=1.1, J2=0.3, Ch=0.2), 0, 2, 1)
@@ -156,17 +156,21 @@ def test_stored_rows_cta_cap_changes_speed_only(gpu):
     assert sec.build_targets()
     v = O.splitmix_vector(sec.n_p, 6)
     for dt in (np.complex128, np.complex64):
-        sec.set_rows(8, 2, 0)
-        ref = sec.sHv(v.astype(dt), dtype=dt)
-        for cps in (1, 2, 3, 4):
-            sec.set_rows(8, 2, cps)
-            assert sec.info["ctas_per_sm"] == cps
-            assert np.array_equal(sec.sHv(v.astype(dt), dtype=dt), ref), (dt, cps)
+        for lanes in (8, 16, 32):
+            sec.set_rows(lanes, 2, 0, 0)
+            ref = sec.sHv(v.astype(dt), dtype=dt)
+            for cps in (0, 1, 2, 3, 4):
+                for pipe in (0, 1):
+                    sec.set_rows(lanes, 2, cps, pipe)
+                    assert sec.info["ctas_per_sm"] == cps and sec.info["pipelined"] == pipe
+                    assert np.array_equal(sec.sHv(v.astype(dt), dtype=dt), ref), (dt, lanes, cps, pipe)
     lanes, ms = sec.tune(0)
-    assert lanes in (8, 16, 32) and sec.info["ctas_per_sm"] in (0, 2, 3, 4)
+    assert lanes in (8, 16, 32) and sec.info["ctas_per_sm"] in (0, 1, 2, 3, 4) and sec.info["pipelined"] in (0, 1)
     assert all(x > 0 for x in ms)
     with pytest.raises(Exception):
         sec.set_rows(8, 2, -1)
+    with pytest.raises(Exception):
+        sec.set_rows(8, 2, 0, 2)
 
 
 @pytest.mark.parametrize("panels", [1, 3, 7])

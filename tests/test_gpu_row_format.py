@@ -56,12 +56,13 @@ def test_packed_and_split_rows_agree_bitwise(mods, monkeypatch, which):
     v = O.splitmix_vector(packed.n_p, 31 + which)
     for lanes in (8, 16, 32):
         for pol in (1, 2):
-            packed.set_rows(lanes, pol)
-            split.set_rows(lanes, pol)
-            for dt in (np.complex128, np.complex64):
-                a = packed.sHv(v.astype(dt), dtype=dt)
-                b = split.sHv(v.astype(dt), dtype=dt)
-                assert np.array_equal(a, b), (lanes, pol, dt)
+            for pipe in (0, 1):
+                packed.set_rows(lanes, pol, 0, pipe)
+                split.set_rows(lanes, pol, 0, pipe)
+                for dt in (np.complex128, np.complex64):
+                    a = packed.sHv(v.astype(dt), dtype=dt)
+                    b = split.sHv(v.astype(dt), dtype=dt)
+                    assert np.array_equal(a, b), (lanes, pol, pipe, dt)
 
 
 def test_value_table_is_deduplicated_at_gamma(mods):
