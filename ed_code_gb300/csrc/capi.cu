@@ -630,7 +630,18 @@ int edg_hv_host(edg_sector* s, const void* v, void* w, int dtype) {
   const bool fp64 = dtype == EDG_C128;
   const int64_t n = S.P.n_p;
   constexpr int kChunks = 8;
-  if (S.col && n >= (1 << 20)) {
+  // w in page-locked host memory that the device can address (cudaHostAlloc,
+  // cudaHostRegister): the kernel stores each w_i there itself, over the
+  // host link while it runs, with no copy after it.
+  cudaPointerAttributes wa{};
+  void* w_dev = nullptr;
+  if (cudaPointerGetAttributes(&wa, w) != cudaSuccess)
+    cudaGetLastError();  // clear the failed query; w is then copied back
+  else if (wa.type == cudaMemoryTypeHost)
+    w_dev = wa.devicePointer;
+  if (e == cudaSuccess && w_dev) {
+    e = launch_hv(S, S.host_in.ptr, w_dev, fp64, S.stream);
+  } else if (S.col && n >= (1 << 20)) {
     // rows in row order: the w rows of chunk c go back to the host while the
     // rows of chunk c + 1 are computed
     if (!S.copy_stream && e == cudaSuccess) e = cudaStreamCreateWithFlags(&S.copy_stream, cudaStreamNonBlocking);

@@ -160,8 +160,12 @@ int edg_sector_set_rows(edg_sector* s, int lanes_per_row, int cache_policy, int 
  * option.  Batch segments and edg_hv_noalloc need the row form. */
 int edg_sector_pack_panels(edg_sector* s, int n_panels);
 
-/* Same with host buffers: copies v in, applies H, copies w out, synchronises.
- * This is the call the reference's sHv(v, w, ...) adapter makes. */
+/* Same with host buffers: copies v in, applies H, returns w, synchronises.
+ * When w is page-locked memory the device can address (cudaHostAlloc,
+ * cudaHostRegister) the kernel stores w there directly while it runs;
+ * otherwise w comes back by copies, overlapped with the rows still being
+ * computed on stored-row sectors.  Either way w holds the same bits.  This is
+ * the call the reference's sHv(v, w, ...) adapter makes. */
 int edg_hv_host(edg_sector* s, const void* v, void* w, int dtype);
 
 /* w = H v like edg_hv, for callers that must not have the library allocate

@@ -247,6 +247,36 @@ def test_host_call_in_row_chunks_equals_device_call(gpu, dtype):
     assert np.array_equal(wd.cpu().numpy(), w_host)
 
 
+@pytest.mark.parametrize("dtype", [np.complex128, np.complex64])
+@pytest.mark.parametrize("stored", [True, False])
+def test_host_call_into_pinned_w_equals_device_call(gpu, dtype, stored):
+    """With w in page-locked host memory edg_hv_host has the kernel store w
+    there directly: the same bits as one device call, on stored rows and on
+    the matrix-free kernel; pageable w (the copy path) agrees too."""
+    import ctypes as C
+
+    import torch
+    from ed_code_gb300 import _native as N
+    from ed_code_gb300 import lattice as L
+
+    sec = gpu.GpuSector(L.make_model(L.TorusSpec("triangular", 6, 5, Jz=0.8, Ch=0.2), 0, 1, 4, bowties=False))
+    if stored:
+        assert sec.build_targets()
+    tdt = torch.complex128 if dtype == np.complex128 else torch.complex64
+    v = torch.from_numpy(O.splitmix_vector(sec.n_p, 13).astype(dtype))
+    vd = v.cuda()
+    wd = torch.empty_like(vd)
+    sec.hv(vd, wd)
+    torch.cuda.synchronize()
+    code = N.EDG_C128 if dtype == np.complex128 else N.EDG_C64
+    for pinned in (True, False):
+        vh = v.pin_memory() if pinned else v.clone()
+        wh = torch.full((sec.n_p,), float("nan"), dtype=tdt, pin_memory=pinned)
+        for _ in range(2):
+            N.check(N.lib().edg_hv_host(sec._h, C.c_void_p(vh.data_ptr()), C.c_void_p(wh.data_ptr()), code))
+            assert torch.equal(wh, wd.cpu()), pinned
+
+
 def test_hv_device_equals_host(gpu):
     import torch
 
