@@ -593,6 +593,55 @@ def run_solve36(args):
     return 0
 
 
+def run_gather_peak(args):
+    """Random single-entry loads from a vector of the 36-site sector's size
+    (edg_probe_gather): the ceiling of the stored-row H*v's far gathers."""
+    import ctypes as C
+
+    import torch
+
+    from ed_code_gb300 import _native as N
+    from ed_code_gb300.sector import fill_random
+
+    torch.cuda.init()
+    n = 252091362  # 6x6 triangular torus, Sz=0, k=Gamma
+    fp64 = args.dtype == "c128"
+    u = torch.empty(n, dtype=torch.complex128 if fp64 else torch.complex64, device="cuda")
+    out = torch.zeros(1, dtype=torch.float32, device="cuda")
+    st = torch.cuda.Stream()
+    fill_random(u, 5, st)
+    count = 4_000_000_000
+    code = N.EDG_C128 if fp64 else N.EDG_C64
+
+    def launch(seed):
+        N.check(N.lib().edg_probe_gather(C.c_void_p(u.data_ptr()), n, code, args.hint, count, seed,
+                                         C.c_void_p(out.data_ptr()), C.c_void_p(st.cuda_stream)))
+
+    for k in range(args.warmup):
+        launch(100 + k)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for k in range(args.steps):
+        launch(k)
+    e1.record(st)
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3 / args.steps
+    elem = 16 if fp64 else 8
+    peak, peak_kind = measured_peak_hbm()
+    sector_gbs = count * 32 / t / 1e9
+    out = {"metric": "random single-entry loads", "mode": "gather-peak", "value": count / t / 1e9,
+           "unit": "G loads/s", "higher_is_better": True, "n_gpus": 1, "data": "synthetic",
+           "ms_per_launch": t * 1e3, "loads_per_launch": count, "entry_bytes": elem,
+           "sector_GBps": sector_gbs, "sector_frac_of_copy_peak": sector_gbs / peak, "useful_GBps": count * elem / t / 1e9,
+           "copy_peak_GBps": peak, "peak_kind": peak_kind,
+           "config": {"vector_entries": n, "vector_bytes": n * elem, "positions": "splitmix64-hashed, uniform",
+                      "l2_hint": ["none", "evict_last"][args.hint],
+                      "l2": "vector 2 GB (c64) or 4 GB (c128) against a 129 MB L2"}}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -610,7 +659,7 @@ def main():
                     help="regroup the stored rows into this many column panels (0: keep the row kernel)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-step-seconds", type=float, default=4.0)
-    ap.add_argument("--mode", choices=["hv", "serve", "batch", "precision", "solve36"], default="hv",
+    ap.add_argument("--mode", choices=["hv", "serve", "batch", "precision", "solve36", "gather-peak"], default="hv",
                     help="hv: the headline H*v line; the others time the solver configurations")
     ap.add_argument("--requests", type=int, default=64)
     ap.add_argument("--rate", type=float, default=200.0)
@@ -620,10 +669,12 @@ def main():
     ap.add_argument("--plain-sample", type=int, default=4)
     ap.add_argument("--momenta", type=int, default=30)
     ap.add_argument("--reorth", type=int, default=0)
+    ap.add_argument("--hint", type=int, choices=[0, 1], default=1,
+                    help="gather-peak: 0 plain loads, 1 the H*v's L2 evict_last policy")
     args = ap.parse_args()
     if args.mode != "hv" and args.impl == "gb300":
         return {"serve": run_serve, "batch": run_batch, "precision": run_precision,
-                "solve36": run_solve36}[args.mode](args)
+                "solve36": run_solve36, "gather-peak": run_gather_peak}[args.mode](args)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

@@ -305,6 +305,15 @@ int edg_batch_timers(const edg_batch* b, double* seconds);
  * written to device memory; the same generator as the test suite's. */
 int edg_fill_random(void* dst, int64_t n, int dtype, uint64_t seed, void* stream);
 
+/* Measurement helper, no counterpart in the reference: `count` loads of single
+ * entries (EDG_C64: 8 bytes, EDG_C128: 16 bytes) from the device vector u of n
+ * entries at hashed random positions, enqueued on `stream`; time it with
+ * events.  hint 0: plain loads; 1: with the L2 evict_last policy of the H*v's
+ * gathers.  This bounds the stored-row H*v's far gathers.  *out (device
+ * memory) is written only if the loaded sum is NaN. */
+int edg_probe_gather(const void* u, int64_t n, int dtype, int hint, int64_t count, uint64_t seed, float* out,
+                     void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -381,3 +381,27 @@ def test_large_sector_6x5_generic_walk(gpu):
     perm = [int(x) for x in np.random.default_rng(4).permutation(20)]
     sec = large_sector_check(gpu, L.TorusSpec("triangular", 5, 4, Jz=0.9, Ch=0.3, relabel=perm), 0, 1, 2)
     assert sec.info["torus"] == 0
+
+
+def test_probe_gather_runs_and_checks_arguments(gpu):
+    """The random-gather measurement helper: in-range loads only, nothing
+    written for finite data, bad arguments rejected."""
+    import ctypes as C
+
+    import torch
+    from ed_code_gb300 import _native as N
+
+    lib = N.lib()
+    for tdt, code in ((torch.complex64, N.EDG_C64), (torch.complex128, N.EDG_C128)):
+        u = torch.ones(1000, dtype=tdt, device="cuda")
+        out = torch.zeros(1, dtype=torch.float32, device="cuda")
+        st = torch.cuda.current_stream().cuda_stream
+        for hint in (0, 1):
+            N.check(lib.edg_probe_gather(C.c_void_p(u.data_ptr()), 1000, code, hint, 100_003, 7,
+                                         C.c_void_p(out.data_ptr()), C.c_void_p(st)))
+        torch.cuda.synchronize()
+        assert out.item() == 0.0
+    p = C.c_void_p(out.data_ptr())
+    assert lib.edg_probe_gather(C.c_void_p(u.data_ptr()), 1000, 9, 0, 10, 7, p, None) != 0
+    assert lib.edg_probe_gather(C.c_void_p(u.data_ptr()), 0, code, 0, 10, 7, p, None) != 0
+    assert lib.edg_probe_gather(C.c_void_p(u.data_ptr()), 1000, code, 2, 10, 7, p, None) != 0
