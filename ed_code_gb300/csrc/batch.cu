@@ -137,8 +137,10 @@ __global__ void __launch_bounds__(kThreads) k_b_u(const SegDev* __restrict__ seg
 }
 
 // w = H V_j on the tile's rows: 32/LPR rows per warp, LPR lanes per row, each
-// row summed by the single-sector kernel's routine (unrolled column and
-// value-id loads, streaming hint on the row data, L2 evict_last on u)
+// row summed by the single-sector kernel's routines (unrolled entry loads,
+// streaming hint on the row data, L2 evict_last on u).  Pipelined like the
+// single-sector kernel: a warp loads the head entries of its next rows (and
+// the offsets of the rows after) before it gathers for the current ones.
 template <int LPR>
 __global__ void __launch_bounds__(kThreads) k_b_hv(const SegDev* __restrict__ segs, const SegState* __restrict__ ss,
                                                    const TileDev* __restrict__ tiles) {
@@ -146,21 +148,50 @@ __global__ void __launch_bounds__(kThreads) k_b_hv(const SegDev* __restrict__ se
   if (ss[t.seg].status != kRunning) return;
   const SegDev& S = segs[t.seg];
   constexpr int kRowsPerWarp = 32 / LPR;
+  constexpr int kU = head_entries<LPR>();
   const int lane = threadIdx.x & 31, sl = lane % LPR, sub = lane / LPR, wid = threadIdx.x >> 5;
   const float2* v = S.V + (int64_t)ss[t.seg].j * S.n;
   const int rows_per_pass = (kThreads / 32) * kRowsPerWarp;
+  const uint64_t pl = l2_evict_last();
+  auto offsets = [&](int r, uint64_t& b, uint64_t& e) {
+    b = e = 0;
+    if (r < t.rows) {
+      b = S.row_ptr[t.row0 + r];
+      e = S.row_ptr[t.row0 + r + 1];
+    }
+  };
+  int r = wid * kRowsPerWarp + sub;
+  uint64_t beg, end, beg1, end1;
+  offsets(r, beg, end);
+  offsets(r + rows_per_pass, beg1, end1);
+  uint32_t e[kU];
+  uint16_t h[kU];
+  csr_head<LPR, kByVid, 1>(beg, end, sl, S.col, S.vid, 0, e, h);
   for (int r0 = 0; r0 < t.rows; r0 += rows_per_pass) {
-    const int r = r0 + wid * kRowsPerWarp + sub;
-    const bool ok = r < t.rows;
-    const int64_t i = t.row0 + (ok ? r : 0);
-    const uint64_t beg = ok ? S.row_ptr[i] : 0, end = ok ? S.row_ptr[i + 1] : 0;
+    uint64_t beg2, end2;
+    offsets(r + 2 * rows_per_pass, beg2, end2);
+    uint32_t en[kU];
+    uint16_t hn[kU];
+    csr_head<LPR, kByVid, 1>(beg1, end1, sl, S.col, S.vid, 0, en, hn);
     float ar, ai;
-    csr_row<float, LPR, false, 1, kByVid>(beg, end, sl, S.col, S.vid, S.pack_cb, S.vtab, S.u, ar, ai);
-    if (ok && sl == 0) {
+    csr_finish<float, LPR, false, 1, kByVid>(beg, end, sl, S.col, S.vid, S.pack_cb, S.vtab, S.u, 0, pl, e, h, ar,
+                                             ai);
+    if (r < t.rows && sl == 0) {
+      const int64_t i = t.row0 + r;
       const float ni = (float)S.nrm[S.lid[i]];
       const float d = (float)S.ezz[i];
       const float2 vi = v[i];
       S.w[i] = make_float2(ar * ni + d * vi.x, ai * ni + d * vi.y);
+    }
+    r += rows_per_pass;
+    beg = beg1;
+    end = end1;
+    beg1 = beg2;
+    end1 = end2;
+#pragma unroll
+    for (int q = 0; q < kU; ++q) {
+      e[q] = en[q];
+      h[q] = hn[q];
     }
   }
 }
