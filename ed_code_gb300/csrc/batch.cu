@@ -291,46 +291,60 @@ __device__ __forceinline__ void block_sum_n(double* v) {
   __syncthreads();
 }
 
-// tile partials of <V_k|w> for k <= j: CTA (tile, y) takes the groups of
-// kCgsQ consecutive k starting at kCgsQ*y, kCgsQ*(y + kCgsY), ..., reading
-// kCgsQ vectors per pass over its rows
-constexpr int kCgsQ = 4;
+// tile partials of <V_k|w> for k <= j: in CTA (tile, y) warp wid takes
+// k = 8*y + wid, 8*(y + kCgsY) + wid, ..., and sums its vector over all the
+// tile's rows (lanes over rows, w re-read from L1 by the CTA's warps), so a
+// warp shuffle, not a block reduction, closes each partial.  Products are
+// summed with Kahan's compensation (ff.cuh): the q_k only correct w's small
+// components along the V_k.
 __global__ void __launch_bounds__(kThreads) k_b_cgs_dot(const SegDev* __restrict__ segs,
                                                         const SegState* __restrict__ ss,
                                                         const TileDev* __restrict__ tiles, int n_tiles,
                                                         double* __restrict__ part, int pass) {
+  constexpr int kWarps = kThreads / 32;
   const TileDev t = tiles[blockIdx.x];
   const SegDev& S = segs[t.seg];
   const bool run = ss[t.seg].status == kRunning && (pass == 0 || ss[t.seg].redo);
   const int K = run ? ss[t.seg].j + 1 : 0;
-  for (int k0 = blockIdx.y * kCgsQ; k0 < K; k0 += kCgsY * kCgsQ) {  // K is the same for the whole CTA
-    FFAcc sr[kCgsQ], si[kCgsQ];
-    for (int r = threadIdx.x; r < t.rows; r += blockDim.x) {
-      const int64_t i = t.row0 + r;
-      const float2 y = S.w[i];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const float2* __restrict__ w = S.w + t.row0;
+  for (int k = blockIdx.y * kWarps + wid; k < K; k += kCgsY * kWarps) {
+    const float2* __restrict__ x = S.V + (int64_t)k * S.n + t.row0;
+    KahanAcc sr, si;
+    int r = lane;
+    for (; r + 96 < t.rows; r += 128) {
+      float2 a[4], b[4];
 #pragma unroll
-      for (int q = 0; q < kCgsQ; ++q)
-        if (k0 + q < K) {
-          const float2 x = S.V[(int64_t)(k0 + q) * S.n + i];
-          sr[q].add_prod(x.x, y.x);
-          sr[q].add_prod(x.y, y.y);
-          si[q].add_prod(x.x, y.y);
-          si[q].sub_prod(x.y, y.x);
-        }
-    }
-    double v[2 * kCgsQ];
-#pragma unroll
-    for (int q = 0; q < kCgsQ; ++q) {
-      v[2 * q] = sr[q].value();
-      v[2 * q + 1] = si[q].value();
-    }
-    block_sum_n<kCgsQ>(v);
-    if (threadIdx.x == 0)
-      for (int q = 0; q < kCgsQ && k0 + q < K; ++q) {
-        const int64_t o = ((int64_t)(k0 + q) * n_tiles + blockIdx.x) * 2;
-        part[o] = v[2 * q];
-        part[o + 1] = v[2 * q + 1];
+      for (int q = 0; q < 4; ++q) {
+        a[q] = __ldcs(x + r + 32 * q);
+        b[q] = w[r + 32 * q];
       }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        sr.add_prod(a[q].x, b[q].x);
+        sr.add_prod(a[q].y, b[q].y);
+        si.add_prod(a[q].x, b[q].y);
+        si.sub_prod(a[q].y, b[q].x);
+      }
+    }
+    for (; r < t.rows; r += 32) {
+      const float2 a = __ldcs(x + r), b = w[r];
+      sr.add_prod(a.x, b.x);
+      sr.add_prod(a.y, b.y);
+      si.add_prod(a.x, b.y);
+      si.sub_prod(a.y, b.x);
+    }
+    double re = sr.value(), im = si.value();
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      re += __shfl_down_sync(0xffffffffu, re, o);
+      im += __shfl_down_sync(0xffffffffu, im, o);
+    }
+    if (lane == 0) {
+      const int64_t o = ((int64_t)k * n_tiles + blockIdx.x) * 2;
+      part[o] = re;
+      part[o + 1] = im;
+    }
   }
 }
 

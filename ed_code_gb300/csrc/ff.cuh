@@ -51,6 +51,24 @@ struct FFAcc {
   __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
 };
 
+// Running sum with Kahan's compensation, for dot products whose products
+// may be rounded: each product enters as fma(a, b, -c), rounded once, so a
+// term costs four FP32 instructions instead of add_prod's ten.  The products'
+// own rounding errors total at most 2^-24 sum |a_i b_i| (at most 2^-24 |a||b|
+// by Cauchy-Schwarz, below the FP32 rounding of the vectors themselves); the
+// summation error is about 2^-23 of the sum plus n 2^-48 of the magnitudes.
+struct KahanAcc {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add_y(float y) {
+    const float t = __fadd_rn(s, y);
+    c = __fsub_rn(__fsub_rn(t, s), y);
+    s = t;
+  }
+  __device__ __forceinline__ void add_prod(float a, float b) { add_y(fmaf(a, b, -c)); }
+  __device__ __forceinline__ void sub_prod(float a, float b) { add_y(fmaf(-a, b, -c)); }
+  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
 // x - a*u - b*w for an FP64 scalar pair (a, b) split into FP32 heads and
 // tails, rounded once to FP32 at the end: the result agrees with the FP64
 // expression rounded to FP32 except in near-ties.
