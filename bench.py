@@ -308,12 +308,16 @@ def run_device(args, world, rank, local_rank):
         lib = N.lib()
         N.check(lib.edg_hv_host(sec._h, C.c_void_p(hv_in.data_ptr()), C.c_void_p(hv_out.data_ptr()), code))
         R.barrier()
+        calls = []
         te = time.perf_counter()
         for _ in range(args.steps):
+            tc = time.perf_counter()
             N.check(lib.edg_hv_host(sec._h, C.c_void_p(hv_in.data_ptr()), C.c_void_p(hv_out.data_ptr()), code))
+            calls.append(time.perf_counter() - tc)
         dt = R.max_over_ranks(time.perf_counter() - te)
         e2e = {"value": R.job_rate(world, args.steps, dt), "unit": UNIT,
-               "h2d_bytes_per_step": sec.n_p * elem, "d2h_bytes_per_step": sec.n_p * elem}
+               "h2d_bytes_per_step": sec.n_p * elem, "d2h_bytes_per_step": sec.n_p * elem,
+               "ms_per_call_min_median_max": [round(1e3 * f(calls), 2) for f in (min, np.median, max)]}
         del hv_in, hv_out
 
     cpu = None

@@ -61,8 +61,8 @@ __device__ __forceinline__ double2 ld_keep(const double2* a, uint64_t pol) {
 // value-id array (6 bytes an entry).  kPacked: one u32 an entry, the column
 // in the low cb bits and the value id above them (4 bytes), used when the
 // deduplicated value table and the sector size leave room (cb < 32 and
-// n_p < 2^cb, so no entry is all ones).  kByVid: either, chosen per row by
-// vid == nullptr (the batch, whose segments may differ).
+// n_p < 2^cb, so no entry is all ones).  kByVid: either, chosen per segment
+// by vid == nullptr (the batch, whose segments may differ).
 constexpr int kSplit = 0, kPacked = 1, kByVid = 2;
 
 template <int kFmt, int kPol>
