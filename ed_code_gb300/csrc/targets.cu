@@ -992,11 +992,12 @@ int build_targets(Sector& S, int64_t max_bytes, std::string& err) {
 // Lanes per CSR row, cache policy, CTAs per SM and pipelining.  lpr in
 // {8, 16, 32} fixes the lanes; 0 times every lane count.  First every (lanes,
 // pipelining 0/1, CTA cap in {as many as fit, 4, 3, 2, 1}) with cache policy 2,
-// then the best of those with policy 1.  Each combination runs twice (FP32)
-// after one warm-up launch, and the fastest is kept.  The CTA cap matters
-// because the gathers reuse u through L2: fewer rows in flight keep their
-// targets' window of u smaller.  ms_out[k] receives the best time of lane
-// count 8, 16, 32 (-1 when not timed).
+// then the best of those with policy 1.  Each combination runs twice (FP32;
+// once on sectors whose launch takes over 5 ms) after one warm-up launch, and
+// the fastest is kept.  The CTA cap matters because the gathers reuse u
+// through L2: fewer rows in flight keep their targets' window of u smaller.
+// ms_out[k] receives the best time of lane count 8, 16, 32 (-1 when not
+// timed).
 int tune_rows(Sector& S, int lpr, int* chosen, double* ms_out) {
   if (!S.col) {
     if (chosen) *chosen = 0;
@@ -1015,16 +1016,19 @@ int tune_rows(Sector& S, int lpr, int* chosen, double* ms_out) {
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   bool warm = false;
+  int reps = 2;  // one launch per trial once a launch takes over 5 ms
   auto time_it = [&]() {
     if (!warm) launch_hv_stored(S, v, w, false, st);
     warm = true;
     cudaEventRecord(e0, st);
-    for (int r = 0; r < 2; ++r) launch_hv_stored(S, v, w, false, st);
+    for (int r = 0; r < reps; ++r) launch_hv_stored(S, v, w, false, st);
     cudaEventRecord(e1, st);
     cudaEventSynchronize(e1);
     float ms = 0;
     cudaEventElapsedTime(&ms, e0, e1);
-    return ms / 2;
+    ms /= reps;
+    if (ms > 5.f) reps = 1;
+    return ms;
   };
   const int cand[3] = {8, 16, 32};
   const int caps[5] = {0, 4, 3, 2, 1};
