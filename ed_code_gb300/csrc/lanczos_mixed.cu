@@ -10,15 +10,16 @@
 //    them, twice (classical Gram-Schmidt with FP64 coefficients).  With FP32
 //    vectors orthogonality decays within a few steps once a level converges:
 //    every step (1) or every few steps keeps T exact; every 20 steps does not;
-//    reorth_every = 0 keeps three vectors resident (the 36-site case: 2 GB
-//    each), reorthogonalises w locally against the two latest vectors each
-//    step, and removes the copies of converged levels afterwards;
+//    reorth_every = 0 reorthogonalises w locally against the two latest
+//    vectors each step and removes the copies of converged levels
+//    afterwards; it keeps every vector when they fit with room to spare,
+//    else three resident (the 36-site case: 2 GB each) plus a small ring;
 //  * T's lowest eigenvalues by bisection and their eigenvectors by inverse
 //    iteration, in FP64 in one CTA on the GPU; Ritz values that T shares with
 //    T-without-its-first-row are copies produced by lost orthogonality and are
 //    dropped (Cullum and Willoughby's test);
 //  * Ritz vectors in FP64 -- from the stored vectors, or by re-running the
-//    recurrence with the same alpha/beta when only three vectors are kept;
+//    recurrence with the same alpha/beta when only a few vectors are kept;
 //  * one FP64 H*v per Ritz vector x: the reported eigenvalue is the Rayleigh
 //    quotient <x|Hx>/<x|x>, and |Hx - theta x|/|x| is its residual.
 #include <cuda_runtime.h>
@@ -26,6 +27,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -406,7 +408,8 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
   const int m = (int)std::min<int64_t>(o.iterations, n);
   const int want = std::min(std::min(o.n_ev, kMaxEv), m);
   if (want <= 0 || m < 2) return fail(EDG_ERR_INVALID, "need n_ev >= 1 and at least 2 iterations");
-  const bool store = o.reorth_every > 0;
+  const bool reorth = o.reorth_every > 0;
+  bool store = reorth;  // every Krylov vector kept in HBM
   cudaStream_t st = S.stream;
   using clk = std::chrono::steady_clock;
   const auto t_start = clk::now();
@@ -415,10 +418,28 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
   int ring = 3;  // resident vectors without storage: the recurrence needs 3
   double *alpha, *beta, *part, *scal, *lq;
   cudaError_t e = cudaSuccess;
-  if (store) {
+  if (!reorth) {
+    // Without full reorthogonalisation the vectors are still kept when they
+    // fit beside the FP64 Ritz vectors with room to spare: the Ritz vectors
+    // then come from storage, and the second pass that regenerates the
+    // vectors is not needed.  The recurrence is the same either way.
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    const int n_try = std::min(kMaxEv, std::min(want + 4, m));
+    const double need = 8.0 * n * (m + 1) + 16.0 * n * n_try + 8.0 * n * 4 + double(1 << 30);
+    // EDG_MIXED_RESIDENT=1 keeps the resident form regardless (for comparisons)
+    const char* resident = std::getenv("EDG_MIXED_RESIDENT");
+    if (need < 0.9 * (double)free_b && !(resident && std::strcmp(resident, "1") == 0)) {
+      if (D.alloc(&V, (size_t)n * (m + 1)) == cudaSuccess)
+        store = true;
+      else
+        cudaGetLastError();
+    }
+  }
+  if (reorth) {
     if ((e = D.alloc(&V, (size_t)n * (m + 1))) != cudaSuccess)
       return fail(EDG_ERR_NOMEM, "mixed Lanczos: the stored FP32 Krylov vectors do not fit (use reorth_every=0)");
-  } else {
+  } else if (!store) {
     for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = D.alloc(&buf[k], (size_t)n);
     if (e != cudaSuccess) return fail(EDG_ERR_NOMEM, "mixed Lanczos: vectors do not fit");
     // up to kRing - 3 more when they fit with room to spare: the second pass
@@ -473,7 +494,7 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
         k_finish<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, alpha + j, 1);
       }
       k_step<<<kRedBlocks, kRedThreads, 0, st>>>(w, vec(j), j > 0 ? vec(j - 1) : nullptr, alpha + j, beta + j, n, part);
-      if (!second && store && ((j + 1) % o.reorth_every == 0)) {
+      if (!second && reorth && ((j + 1) % o.reorth_every == 0)) {
         // Periodic reorthogonalisation in its two-vector form: between two
         // reorthogonalisations v_j has drifted too, so it is cleaned against
         // v_0..v_{j-1} first, then w against v_0..v_j; each classical
@@ -495,7 +516,7 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
         }
         cgs2(w, j + 1);
         norm_into(w, beta + j + 1);
-      } else if (!store) {
+      } else if (!reorth) {
         // Local reorthogonalisation of w against v_j and v_{j-1}, the vectors
         // still resident: it slows the growth of the copies that FP32 vectors
         // make without full reorthogonalisation.  The second pass repeats it

@@ -222,7 +222,9 @@ typedef struct {
   int reorth_every;         /* > 0: keep every FP32 Krylov vector and reorthogonalise the
                                last two against all of them every reorth_every steps
                                (1 or a few: FP32 vectors lose orthogonality fast);
-                               0: three resident vectors, Ritz vectors by a second pass */
+                               0: w reorthogonalised against the two latest vectors only;
+                               every vector kept when they fit with room to spare, else
+                               three resident and the Ritz vectors by a second pass */
   uint64_t seed;            /* start vector: splitmix64 stream */
   int want_vectors;         /* copy the FP64 eigenvectors out */
 } edg_mixed_opts;
