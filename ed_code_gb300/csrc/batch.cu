@@ -608,7 +608,7 @@ void finish_stopped(Batch& B) {
     Segment& g = B.segs[idx[i]];
     const int m = g.st.j, na = (int)sel[i].acc.size();
     cudaMemcpyAsync(B.fin.y, sel[i].y.data(), sizeof(double) * na * m, cudaMemcpyHostToDevice, B.st);
-    status[i] = B.fin.ritz_stored(B.st, g.d.V, g.d.n, m, na);
+    status[i] = B.fin.ritz_stored(B.st, g.d.V, g.d.n, m, na, m);
     if (status[i] == EDG_OK && (e = B.fin.rayleigh_async(g.sec->s, B.st, g.d.n, na, B.fin.res + 4 * off[i])) != cudaSuccess)
       status[i] = cuda_fail(e, "batch: FP64 H*v");
   }

@@ -141,8 +141,9 @@ struct MixedFinish {
   ~MixedFinish();
   cudaError_t reserve(int64_t n, int m, int n_res);
   cudaError_t reserve_x(int64_t n, int na);
-  // X_q = sum_j y_q[j] V_j from m stored FP32 vectors (leading dimension n)
-  int ritz_stored(cudaStream_t st, const float2* V, int64_t n, int m, int na);
+  // X_q = sum_{j < cnt} y_q[j] V_j from the first cnt stored FP32 vectors
+  // (y_q holds m coefficients; the vectors' leading dimension is n)
+  int ritz_stored(cudaStream_t st, const float2* V, int64_t n, int m, int na, int cnt);
   // res[4q..4q+3] = |x_q|^2, <x_q|H x_q>, Rayleigh quotient, residual, queued
   // on st (no wait)
   cudaError_t rayleigh_async(Sector& S, cudaStream_t st, int64_t n, int na, double* res_dev);

@@ -248,28 +248,28 @@ __global__ void __launch_bounds__(kRedThreads) k_rq_partial(const double2* __res
   }
 }
 
-// X_q = sum_j y[q*m + j] V_j for q in [q0, q0 + qn), qn <= kRitzChunk: each
-// V_j is read once per chunk of Ritz vectors.  The coefficients are split into
-// FP32 heads and tails and the sums kept in float-float (ff.cuh), written out
-// in FP64.
+// X_q = sum_{j < cnt} y[q*m + j] V_j for q in [q0, q0 + qn), qn <= kRitzChunk:
+// each V_j is read once per chunk of Ritz vectors.  The coefficients are split
+// into FP32 heads and tails and the sums kept in float-float (ff.cuh), written
+// out in FP64.
 constexpr int kRitzChunk = 8;
 __global__ void __launch_bounds__(256) k_ritz_vectors(double2* __restrict__ X, int64_t n,
                                                       const float2* __restrict__ V, int64_t ldv,
-                                                      const double* __restrict__ y, int m, int q0, int qn) {
-  extern __shared__ float2 sy2[];  // qn * m (head, tail)
-  for (int k = threadIdx.x; k < qn * m; k += blockDim.x) {
-    const FFScalar c(y[(int64_t)q0 * m + k]);
+                                                      const double* __restrict__ y, int m, int cnt, int q0, int qn) {
+  extern __shared__ float2 sy2[];  // qn * cnt (head, tail)
+  for (int k = threadIdx.x; k < qn * cnt; k += blockDim.x) {
+    const FFScalar c(y[(int64_t)(q0 + k / cnt) * m + k % cnt]);
     sy2[k] = make_float2(c.h, c.l);
   }
   __syncthreads();
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     FFAcc ar[kRitzChunk], ai[kRitzChunk];
-    for (int j = 0; j < m; ++j) {
+    for (int j = 0; j < cnt; ++j) {
       const float2 v = V[(int64_t)j * ldv + i];
 #pragma unroll
       for (int q = 0; q < kRitzChunk; ++q)
         if (q < qn) {
-          const float2 c = sy2[q * m + j];
+          const float2 c = sy2[q * cnt + j];
           ar[q].add_prod(c.x, v.x);
           ar[q].lo = fmaf(c.y, v.x, ar[q].lo);
           ai[q].add_prod(c.x, v.y);
@@ -361,10 +361,10 @@ cudaError_t MixedFinish::reserve_x(int64_t n, int na) {
   return grow((void**)&X, sizeof(double2) * n * na, x_bytes);
 }
 
-int MixedFinish::ritz_stored(cudaStream_t st, const float2* V, int64_t n, int m, int na) {
+int MixedFinish::ritz_stored(cudaStream_t st, const float2* V, int64_t n, int m, int na, int cnt) {
   for (int q0 = 0; q0 < na; q0 += kRitzChunk) {
     const int qn = std::min(kRitzChunk, na - q0);
-    k_ritz_vectors<<<grid_n(n), 256, sizeof(float2) * qn * m, st>>>(X, n, V, n, y, m, q0, qn);
+    k_ritz_vectors<<<grid_n(n), 256, sizeof(float2) * qn * cnt, st>>>(X, n, V, n, y, m, cnt, q0, qn);
   }
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? EDG_OK : cuda_fail(e, "mixed Lanczos: Ritz vectors");
@@ -415,31 +415,41 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
   const auto t_start = clk::now();
   Dev D;
   float2 *V = nullptr, *w = nullptr, *buf[kRing] = {};
-  int ring = 3;  // resident vectors without storage: the recurrence needs 3
+  int ring = 3;  // resident vectors past the stored ones: the recurrence needs 3
+  int kept = 0;   // v_0 .. v_{kept-1} stored in V; the later ones live in the ring
   double *alpha, *beta, *part, *scal, *lq;
   cudaError_t e = cudaSuccess;
-  if (!reorth) {
-    // Without full reorthogonalisation the vectors are still kept when they
-    // fit beside the FP64 Ritz vectors with room to spare: the Ritz vectors
-    // then come from storage, and the second pass that regenerates the
-    // vectors is not needed.  The recurrence is the same either way.
-    size_t free_b = 0, total_b = 0;
-    cudaMemGetInfo(&free_b, &total_b);
-    const int n_try = std::min(kMaxEv, std::min(want + 4, m));
-    const double need = 8.0 * n * (m + 1) + 16.0 * n * n_try + 8.0 * n * 4 + double(1 << 30);
-    // EDG_MIXED_RESIDENT=1 keeps the resident form regardless (for comparisons)
-    const char* resident = std::getenv("EDG_MIXED_RESIDENT");
-    if (need < 0.9 * (double)free_b && !(resident && std::strcmp(resident, "1") == 0)) {
-      if (D.alloc(&V, (size_t)n * (m + 1)) == cudaSuccess)
-        store = true;
-      else
-        cudaGetLastError();
-    }
-  }
   if (reorth) {
     if ((e = D.alloc(&V, (size_t)n * (m + 1))) != cudaSuccess)
       return fail(EDG_ERR_NOMEM, "mixed Lanczos: the stored FP32 Krylov vectors do not fit (use reorth_every=0)");
-  } else if (!store) {
+    kept = m + 1;
+  } else {
+    // Without full reorthogonalisation the vectors are still stored, as many
+    // as fit beside the FP64 Ritz vectors, the ring and w with room to spare.
+    // All of them: the Ritz vectors come from storage and no second pass is
+    // needed.  Some of them: the second pass starts where storage ends.  The
+    // recurrence is the same in every form.
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    const int n_try = std::min(kMaxEv, std::min(want + 4, m));
+    const double vb = 8.0 * (double)n;
+    const double rest = 16.0 * n * n_try + vb * (kRing + 2) + double(1 << 30);
+    const double fit = std::floor((0.9 * (double)free_b - rest) / vb);
+    int k = fit >= (double)(m + 1) ? m + 1 : (int)std::max(0.0, fit);
+    // EDG_MIXED_KEEP=k stores at most k vectors (0: the resident form), for
+    // comparisons of the three forms
+    if (const char* cap = std::getenv("EDG_MIXED_KEEP")) k = std::min(k, std::max(0, std::atoi(cap)));
+    if (k < m + 1 && k > m - 8) k = m - 8;  // a second pass of a handful of steps is not worth keeping
+    if (k < 8) k = 0;
+    if (k > 0) {
+      if (D.alloc(&V, (size_t)n * k) == cudaSuccess)
+        kept = k;
+      else
+        cudaGetLastError();
+    }
+    store = kept == m + 1;
+  }
+  if (!store) {
     for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = D.alloc(&buf[k], (size_t)n);
     if (e != cudaSuccess) return fail(EDG_ERR_NOMEM, "mixed Lanczos: vectors do not fit");
     // up to kRing - 3 more when they fit with room to spare: the second pass
@@ -460,7 +470,7 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
     return fail(EDG_ERR_NOMEM, "mixed Lanczos: scratch");
   cudaMemsetAsync(beta, 0, sizeof(double) * (m + 2), st);
 
-  auto vec = [&](int j) -> float2* { return store ? V + (int64_t)j * n : buf[j % ring]; };
+  auto vec = [&](int j) -> float2* { return j < kept ? V + (int64_t)j * n : buf[(j - kept) % ring]; };
   auto norm_into = [&](const float2* x, double* dst) {  // dst = |x| in FP64
     k_dot32<<<dim3(kRedBlocks, 1), kRedThreads, 0, st>>>(x, 0, x, n, part);
     k_finish<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, dst, 2);
@@ -468,15 +478,21 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
   double t_hv = 0;
   int64_t hv_calls = 0;
   // one Lanczos pass; in the second pass (same recurrence, same alpha/beta)
-  // the Ritz vectors X are accumulated from the device coefficients yd
+  // the Ritz vectors X are accumulated from the device coefficients yd.  The
+  // second pass starts at the last stored vector, whose predecessors are
+  // stored too; the stored vectors' share of X is already in place.
   auto run = [&](bool second, double2* X, int E, const double* yd) -> cudaError_t {
-    cudaError_t ce = edg_fill_random(w, n, EDG_C64, o.seed, st) == EDG_OK ? cudaSuccess : cudaErrorUnknown;
-    if (ce != cudaSuccess) return ce;
-    norm_into(w, scal);                                     // |v0 unnormalised|
-    k_scale_inv<<<grid_n(n), 256, 0, st>>>(vec(0), w, scal, n);
+    cudaError_t ce = cudaSuccess;
+    const int j0 = second && kept > 0 ? kept - 1 : 0;
+    if (j0 == 0) {
+      ce = edg_fill_random(w, n, EDG_C64, o.seed, st) == EDG_OK ? cudaSuccess : cudaErrorUnknown;
+      if (ce != cudaSuccess) return ce;
+      norm_into(w, scal);                                     // |v0 unnormalised|
+      k_scale_inv<<<grid_n(n), 256, 0, st>>>(vec(0), w, scal, n);
+    }
     const int win = std::max(1, ring - 2);  // vectors V_j0..V_j still resident at step j
-    int acc_from = 0;
-    for (int j = 0; j < m; ++j) {
+    int acc_from = second ? kept : 0;
+    for (int j = j0; j < m; ++j) {
       if (second) {
         if (j - acc_from + 1 == win || j + 1 == m) {
           RingPtrs rp{};
@@ -558,10 +574,14 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
   int passes = 1;
   int rc = EDG_OK;
   if (store) {
-    if ((rc = F.ritz_stored(st, V, n, m, na)) != EDG_OK) return rc;
+    if ((rc = F.ritz_stored(st, V, n, m, na, m)) != EDG_OK) return rc;
   } else {
     passes = 2;
-    cudaMemsetAsync(F.X, 0, sizeof(double2) * na * n, st);
+    if (kept > 0) {
+      if ((rc = F.ritz_stored(st, V, n, m, na, kept)) != EDG_OK) return rc;
+    } else {
+      cudaMemsetAsync(F.X, 0, sizeof(double2) * na * n, st);
+    }
     if ((e = run(true, F.X, na, F.y)) != cudaSuccess) return cuda_fail(e, "mixed Lanczos: second pass");
   }
   // FP64 Rayleigh quotient and residual of each Ritz vector
@@ -589,6 +609,7 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
     stats->hv_calls = hv_calls + na;
     stats->hv_seconds = t_hv;
     stats->passes = passes;
+    stats->stored_vectors = kept;
     stats->total_seconds = std::chrono::duration<double>(clk::now() - t_start).count();
   }
   return EDG_OK;

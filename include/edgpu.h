@@ -224,7 +224,8 @@ typedef struct {
                                (1 or a few: FP32 vectors lose orthogonality fast);
                                0: w reorthogonalised against the two latest vectors only;
                                every vector kept when they fit with room to spare, else
-                               three resident and the Ritz vectors by a second pass */
+                               as many as fit and the Ritz vectors finished by a second
+                               pass from the last stored vector */
   uint64_t seed;            /* start vector: splitmix64 stream */
   int want_vectors;         /* copy the FP64 eigenvectors out */
 } edg_mixed_opts;
@@ -233,6 +234,7 @@ typedef struct {
   int64_t hv_calls;         /* FP32 H*v (both passes) plus one FP64 H*v per Ritz vector */
   double hv_seconds, total_seconds;
   int passes;
+  int stored_vectors;       /* Krylov vectors kept in HBM (the rest lived in a ring) */
 } edg_mixed_stats;
 
 /* Lowest eigenvalues with FP32 Krylov vectors and FP32 H*v; FP64 for alpha/beta

@@ -18,21 +18,22 @@ def gpu(cuda_device):
     return sector
 
 
-# (reorth_every, EDG_MIXED_RESIDENT): 0 stores every vector when they fit and
-# takes the Ritz vectors from storage in one pass; with the resident form
-# forced it keeps three vectors and a ring and runs a second pass
-FORMS = [(1, None), (4, None), (0, None), (0, "1")]
+# (reorth_every, EDG_MIXED_KEEP): 0 stores every vector when they fit and
+# takes the Ritz vectors from storage in one pass; with storage capped it
+# stores the first k vectors (none for k = 0), keeps the later ones in a ring
+# and finishes the Ritz vectors with a second pass from v_{k-1}
+FORMS = [(1, None), (4, None), (0, None), (0, "100"), (0, "0")]
 
 
-def _passes(reorth, resident):
-    return 2 if (reorth == 0 and resident == "1") else 1
+def _passes(reorth, keep):
+    return 2 if (reorth == 0 and keep is not None) else 1
 
 
-@pytest.mark.parametrize("reorth,resident", FORMS)
+@pytest.mark.parametrize("reorth,keep", FORMS)
 @pytest.mark.parametrize("name,n_ev", [("tri6x4_k10", 2), ("sq6x4_k00", 4)])
-def test_mixed_matches_reference(gpu, monkeypatch, name, n_ev, reorth, resident):
-    if resident:
-        monkeypatch.setenv("EDG_MIXED_RESIDENT", resident)
+def test_mixed_matches_reference(gpu, monkeypatch, name, n_ev, reorth, keep):
+    if keep is not None:
+        monkeypatch.setenv("EDG_MIXED_KEEP", keep)
     ref = np.array(golden_cases()[name]["sectors"][0]["ed2_eigs"][:n_ev])
     sec = gpu.GpuSector(golden_model(name, 0))
     out = sec.solve_mixed(n_ev=n_ev, iterations=300, reorth_every=reorth, seed=1)
@@ -41,31 +42,39 @@ def test_mixed_matches_reference(gpu, monkeypatch, name, n_ev, reorth, resident)
     rel = np.abs(eigs[:n_ev] - ref) / np.abs(ref)
     assert rel.max() <= 1e-9, (eigs, ref, out["residuals"])
     assert np.all(out["residuals"][:n_ev] < 1e-3)
-    assert out["stats"]["passes"] == _passes(reorth, resident)
+    assert out["stats"]["passes"] == _passes(reorth, keep)
 
 
-def test_resident_and_stored_forms_agree(gpu, monkeypatch):
-    """Without full reorthogonalisation the stored and the resident form run
-    the same recurrence (the same T, so the same Ritz values bit for bit);
-    only the Ritz vectors' summation differs, by rounding."""
+def test_stored_partial_and_resident_forms_agree(gpu, monkeypatch):
+    """Without full reorthogonalisation every storage form runs the same
+    recurrence (the same T, so the same Ritz values bit for bit); only the
+    Ritz vectors' summation differs, by rounding."""
     sec = gpu.GpuSector(golden_model("tri6x4_k10", 0))
-    a = sec.solve_mixed(n_ev=2, iterations=200, reorth_every=0, seed=3)
-    monkeypatch.setenv("EDG_MIXED_RESIDENT", "1")
-    b = sec.solve_mixed(n_ev=2, iterations=200, reorth_every=0, seed=3)
-    assert a["stats"]["passes"] == 1 and b["stats"]["passes"] == 2
-    assert np.array_equal(a["ritz"], b["ritz"])
-    assert np.max(np.abs(a["eigs"] - b["eigs"]) / np.abs(b["eigs"])) <= 1e-12
+    runs = {}
+    for keep in (None, "57", "0"):
+        if keep is None:
+            monkeypatch.delenv("EDG_MIXED_KEEP", raising=False)
+        else:
+            monkeypatch.setenv("EDG_MIXED_KEEP", keep)
+        runs[keep] = sec.solve_mixed(n_ev=2, iterations=200, reorth_every=0, seed=3)
+    a = runs[None]
+    assert a["stats"]["passes"] == 1
+    for keep in ("57", "0"):
+        b = runs[keep]
+        assert b["stats"]["passes"] == 2
+        assert np.array_equal(a["ritz"], b["ritz"]), keep
+        assert np.max(np.abs(a["eigs"] - b["eigs"]) / np.abs(b["eigs"])) <= 1e-12, keep
 
 
-@pytest.mark.parametrize("reorth,resident", [(1, None), (0, None), (0, "1")])
-def test_mixed_eigenvectors(gpu, monkeypatch, reorth, resident):
-    """Stored vectors (reorth 1, or 0 when they fit) or the second pass over
-    resident vectors (0, resident form forced)."""
-    if resident:
-        monkeypatch.setenv("EDG_MIXED_RESIDENT", resident)
+@pytest.mark.parametrize("reorth,keep", [(1, None), (0, None), (0, "120"), (0, "0")])
+def test_mixed_eigenvectors(gpu, monkeypatch, reorth, keep):
+    """Stored vectors (reorth 1, or 0 when they fit), some stored and the rest
+    by a second pass, or all by the second pass."""
+    if keep is not None:
+        monkeypatch.setenv("EDG_MIXED_KEEP", keep)
     sec = gpu.GpuSector(golden_model("tri6x4_k10", 0))
     out = sec.solve_mixed(n_ev=2, iterations=250, reorth_every=reorth, want_vectors=True)
-    assert out["stats"]["passes"] == _passes(reorth, resident)
+    assert out["stats"]["passes"] == _passes(reorth, keep)
     X = out["evecs"]
     for k in range(len(out["eigs"])):
         assert abs(np.vdot(X[k], X[k]).real - 1.0) < 1e-12
