@@ -13,13 +13,15 @@
 //    reorth_every = 0 reorthogonalises w locally against the two latest
 //    vectors each step and removes the copies of converged levels
 //    afterwards; it keeps every vector when they fit with room to spare,
-//    else three resident (the 36-site case: 2 GB each) plus a small ring;
+//    else as many as fit (the 36-site case: 2 GB each) and the later ones in
+//    a ring of up to eight;
 //  * T's lowest eigenvalues by bisection and their eigenvectors by inverse
 //    iteration, in FP64 in one CTA on the GPU; Ritz values that T shares with
 //    T-without-its-first-row are copies produced by lost orthogonality and are
 //    dropped (Cullum and Willoughby's test);
-//  * Ritz vectors in FP64 -- from the stored vectors, or by re-running the
-//    recurrence with the same alpha/beta when only a few vectors are kept;
+//  * Ritz vectors in FP64 -- from the stored vectors, plus, when only the
+//    first k were stored, a re-run of the recurrence from v_{k-1} with the
+//    same alpha/beta for the later ones;
 //  * one FP64 H*v per Ritz vector x: the reported eigenvalue is the Rayleigh
 //    quotient <x|Hx>/<x|x>, and |Hx - theta x|/|x| is its residual.
 #include <cuda_runtime.h>
