@@ -201,6 +201,12 @@ void solve_sector(int kx, int ky, double cSz, int n_spins, double lambda, double
   std::vector<cplx> vecs((size_t)(nvec * n_p));
   int64_t n_eigs = 0;
   edg_solver_stats st{};
+  if (!dense) {
+    // the Lanczos path's H*v on stored rows with the row kernel timed on this
+    // sector; sectors whose rows do not fit (EDG_ERR_NOMEM) or that have ChCh
+    // terms (EDG_ERR_UNSUPPORTED) keep the matrix-free kernel
+    if (edg_sector_build_targets(sec, 0) == EDG_OK) edg_sector_tune(sec, 0, nullptr, nullptr);
+  }
   rc = edg_solve_plain(sec, &o, eigs.data(), cap, &n_eigs, nvec ? reinterpret_cast<double*>(vecs.data()) : nullptr,
                        nvec, &st);
   if (rc != EDG_OK) die(outfile, std::string("\nERROR: ") + edg_last_error() + "\n");
