@@ -145,6 +145,81 @@ __global__ void __launch_bounds__(kRedThreads) k_step(float2* __restrict__ w, co
   }
 }
 
+// Block sums of kQ complex float-float accumulators into part[(k*gridDim.x + b)*2 + {0,1}].
+template <int kQ>
+__device__ __forceinline__ void block_partials(const FFAcc (&r)[kQ], const FFAcc (&i)[kQ], double* part) {
+  __shared__ double rr[kRedThreads], ri[kRedThreads];
+  for (int k = 0; k < kQ; ++k) {
+    rr[threadIdx.x] = r[k].value();
+    ri[threadIdx.x] = i[k].value();
+    __syncthreads();
+    for (int h = kRedThreads / 2; h > 0; h >>= 1) {
+      if ((int)threadIdx.x < h) {
+        rr[threadIdx.x] += rr[threadIdx.x + h];
+        ri[threadIdx.x] += ri[threadIdx.x + h];
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      const int64_t o = ((int64_t)k * gridDim.x + blockIdx.x) * 2;
+      part[o] = rr[0];
+      part[o + 1] = ri[0];
+    }
+    __syncthreads();
+  }
+}
+
+// The local form's step in one pass: w = w - alpha v - beta vprev as k_step,
+// then the partials of <v|w> and <vprev|w> (0 without vprev) for the local
+// reorthogonalisation, k = 0 and 1 in k_finish's layout.
+__global__ void __launch_bounds__(kRedThreads) k_step_dots(float2* __restrict__ w, const float2* __restrict__ v,
+                                                           const float2* __restrict__ vprev,
+                                                           const double* __restrict__ alpha,
+                                                           const double* __restrict__ beta, int64_t n,
+                                                           double* __restrict__ part) {
+  const FFScalar a(*alpha), b(vprev ? *beta : 0.0);
+  FFAcc r[2], im[2];
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 wi = w[i], vi = v[i];
+    const float2 pi = vprev ? vprev[i] : make_float2(0.f, 0.f);
+    const float2 o = make_float2(ff_axpy2(wi.x, a, vi.x, b, pi.x), ff_axpy2(wi.y, a, vi.y, b, pi.y));
+    w[i] = o;
+    r[0].add_prod(vi.x, o.x);
+    r[0].add_prod(vi.y, o.y);
+    im[0].add_prod(vi.x, o.y);
+    im[0].sub_prod(vi.y, o.x);
+    r[1].add_prod(pi.x, o.x);
+    r[1].add_prod(pi.y, o.y);
+    im[1].add_prod(pi.x, o.y);
+    im[1].sub_prod(pi.y, o.x);
+  }
+  block_partials<2>(r, im, part);
+}
+
+// w -= q0 v + q1 vprev (q complex, device; FP32 arithmetic as k_sub32) and the
+// partials of |w|^2 in k_finish's layout.
+__global__ void __launch_bounds__(kRedThreads) k_sub2_norm(float2* __restrict__ w, const float2* __restrict__ v,
+                                                           const float2* __restrict__ vprev,
+                                                           const double* __restrict__ q, int64_t n,
+                                                           double* __restrict__ part) {
+  const float q0r = (float)q[0], q0i = (float)q[1], q1r = (float)q[2], q1i = (float)q[3];
+  FFAcc r[1], im[1];
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 y0 = w[i], vi = v[i];
+    float re = fmaf(-q0r, vi.x, fmaf(q0i, vi.y, y0.x));
+    float ii = fmaf(-q0r, vi.y, fmaf(-q0i, vi.x, y0.y));
+    if (vprev) {
+      const float2 pi = vprev[i];
+      re = fmaf(-q1r, pi.x, fmaf(q1i, pi.y, re));
+      ii = fmaf(-q1r, pi.y, fmaf(-q1i, pi.x, ii));
+    }
+    w[i] = make_float2(re, ii);
+    r[0].add_prod(re, re);
+    r[0].add_prod(ii, ii);
+  }
+  block_partials<1>(r, im, part);
+}
+
 // dst = src / beta (dst may be src); 1/beta as an FP32 head and tail
 __global__ void k_scale_inv(float2* dst, const float2* src, const double* __restrict__ beta, int64_t n) {
   const FFScalar s(1.0 / *beta);
@@ -468,7 +543,7 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
   const int64_t kparts = (int64_t)std::max(m + 1, 4) * kRedBlocks * 2;
   if ((e = D.alloc(&alpha, m + 1)) != cudaSuccess || (e = D.alloc(&beta, m + 2)) != cudaSuccess ||
       (e = D.alloc(&part, kparts)) != cudaSuccess || (e = D.alloc(&scal, 2 * (m + 2) + 2)) != cudaSuccess ||
-      (e = D.alloc(&lq, 2)) != cudaSuccess)
+      (e = D.alloc(&lq, 4)) != cudaSuccess)
     return fail(EDG_ERR_NOMEM, "mixed Lanczos: scratch");
   cudaMemsetAsync(beta, 0, sizeof(double) * (m + 2), st);
 
@@ -511,43 +586,46 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
         k_dot32<<<dim3(kRedBlocks, 1), kRedThreads, 0, st>>>(vec(j), 0, w, n, part);
         k_finish<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, alpha + j, 1);
       }
-      k_step<<<kRedBlocks, kRedThreads, 0, st>>>(w, vec(j), j > 0 ? vec(j - 1) : nullptr, alpha + j, beta + j, n, part);
-      if (!second && reorth && ((j + 1) % o.reorth_every == 0)) {
-        // Periodic reorthogonalisation in its two-vector form: between two
-        // reorthogonalisations v_j has drifted too, so it is cleaned against
-        // v_0..v_{j-1} first, then w against v_0..v_j; each classical
-        // Gram-Schmidt pass runs twice.  (Cleaning w alone lets the
-        // recurrence carry v_j's error into every later vector.)
-        auto cgs2 = [&](float2* x, int K) {
-          for (int pass = 0; pass < 2; ++pass)
-            for (int k0 = 0; k0 < K; k0 += 512) {
-              const int kk = std::min(512, K - k0);
-              k_dot32<<<dim3(kRedBlocks, kk), kRedThreads, 0, st>>>(V + (int64_t)k0 * n, n, x, n, part);
-              k_finish<<<kk, kRedThreads, 0, st>>>(part, kRedBlocks, scal, 0);
-              k_sub32<<<grid_n(n), 256, sizeof(float) * 2 * kk, st>>>(x, V + (int64_t)k0 * n, n, scal, kk, n);
-            }
-        };
-        if (o.reorth_every > 1 && j > 0) {
-          cgs2(vec(j), j);
-          norm_into(vec(j), scal + 2 * (m + 1));
-          k_scale_inv<<<grid_n(n), 256, 0, st>>>(vec(j), vec(j), scal + 2 * (m + 1), n);
-        }
-        cgs2(w, j + 1);
-        norm_into(w, beta + j + 1);
-      } else if (!reorth) {
+      if (!reorth) {
         // Local reorthogonalisation of w against v_j and v_{j-1}, the vectors
         // still resident: it slows the growth of the copies that FP32 vectors
-        // make without full reorthogonalisation.  The second pass repeats it
-        // (the kernels are deterministic, so with the same coefficients).
-        for (int b = 0; b < (j > 0 ? 2 : 1); ++b) {
-          const float2* vb = vec(j - b);
-          k_dot32<<<dim3(kRedBlocks, 1), kRedThreads, 0, st>>>(vb, 0, w, n, part);
-          k_finish<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, lq, 0);
-          k_sub32<<<grid_n(n), 256, sizeof(float) * 2, st>>>(w, vb, n, lq, 1, n);
+        // make without full reorthogonalisation.  Fused: the step and both
+        // coefficients in one pass, the subtraction and |w|^2 in another.
+        // The second pass repeats it (the kernels are deterministic, so with
+        // the same coefficients).
+        const float2* vp = j > 0 ? vec(j - 1) : nullptr;
+        k_step_dots<<<kRedBlocks, kRedThreads, 0, st>>>(w, vec(j), vp, alpha + j, beta + j, n, part);
+        k_finish<<<2, kRedThreads, 0, st>>>(part, kRedBlocks, lq, 0);
+        k_sub2_norm<<<kRedBlocks, kRedThreads, 0, st>>>(w, vec(j), vp, lq, n, part);
+        if (!second) k_finish<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, beta + j + 1, 2);
+      } else {
+        k_step<<<kRedBlocks, kRedThreads, 0, st>>>(w, vec(j), j > 0 ? vec(j - 1) : nullptr, alpha + j, beta + j, n,
+                                                   part);
+        if (!second && (j + 1) % o.reorth_every == 0) {
+          // Periodic reorthogonalisation in its two-vector form: between two
+          // reorthogonalisations v_j has drifted too, so it is cleaned against
+          // v_0..v_{j-1} first, then w against v_0..v_j; each classical
+          // Gram-Schmidt pass runs twice.  (Cleaning w alone lets the
+          // recurrence carry v_j's error into every later vector.)
+          auto cgs2 = [&](float2* x, int K) {
+            for (int pass = 0; pass < 2; ++pass)
+              for (int k0 = 0; k0 < K; k0 += 512) {
+                const int kk = std::min(512, K - k0);
+                k_dot32<<<dim3(kRedBlocks, kk), kRedThreads, 0, st>>>(V + (int64_t)k0 * n, n, x, n, part);
+                k_finish<<<kk, kRedThreads, 0, st>>>(part, kRedBlocks, scal, 0);
+                k_sub32<<<grid_n(n), 256, sizeof(float) * 2 * kk, st>>>(x, V + (int64_t)k0 * n, n, scal, kk, n);
+              }
+          };
+          if (o.reorth_every > 1 && j > 0) {
+            cgs2(vec(j), j);
+            norm_into(vec(j), scal + 2 * (m + 1));
+            k_scale_inv<<<grid_n(n), 256, 0, st>>>(vec(j), vec(j), scal + 2 * (m + 1), n);
+          }
+          cgs2(w, j + 1);
+          norm_into(w, beta + j + 1);
+        } else if (!second) {
+          k_finish<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, beta + j + 1, 2);
         }
-        if (!second) norm_into(w, beta + j + 1);
-      } else if (!second) {
-        k_finish<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, beta + j + 1, 2);
       }
       if (j + 1 < m || second) k_scale_inv<<<grid_n(n), 256, 0, st>>>(vec(j + 1), w, beta + j + 1, n);
       if ((ce = cudaGetLastError()) != cudaSuccess) return ce;
