@@ -403,7 +403,7 @@ def run_serve(args):
 
     torch.cuda.init()
     warm = serving.make_stream(4, rate=1e6, seed=99, sizes=(20,))
-    srv = serving.Server(max_iterations=300, res_tol=args.res_tol)
+    srv = serving.Server(max_iterations=300, res_tol=args.res_tol, tile_rows=args.serve_tile)
     srv.run(warm)
     stream = serving.make_stream(args.requests, rate=args.rate, seed=3)
     t0 = time.perf_counter()
@@ -442,6 +442,7 @@ def run_serve(args):
            "speedup_vs_sequential_plain": (summ["solves_per_s"] * seq_plain / len(stream)) if seq_plain else None,
            "peak_active": srv.peak_live, "create_seconds": t_create, "batch_timers": timers,
            "config": {"workload": f"poisson {args.rate}/s, {args.requests} requests, N in 20/24/28/32, seed 3",
+                      "tile_rows": args.serve_tile,
                       "res_tol": args.res_tol, "max_iterations": 300, "vectors": "c64 Krylov, f64 alpha/beta/RQ"}}
     print(json.dumps(out), flush=True)
     return 0
@@ -674,6 +675,7 @@ def main():
     ap.add_argument("--plain-sample", type=int, default=4)
     ap.add_argument("--momenta", type=int, default=30)
     ap.add_argument("--reorth", type=int, default=0)
+    ap.add_argument("--serve-tile", type=int, default=4096, help="serve: rows per tile of the batch kernels")
     ap.add_argument("--hint", type=int, choices=[0, 1], default=1,
                     help="gather-peak: 0 plain loads, 1 the H*v's L2 evict_last policy")
     args = ap.parse_args()

@@ -101,7 +101,7 @@ class Server:
     relative of the FP64 ones for these models (checked by the tests)."""
 
     def __init__(self, hbm_budget: Optional[int] = None, max_iterations: int = 300, res_tol: float = 1e-6,
-                 tile_rows: int = 1024, lanes_per_row: int = 8, check_every: int = 10, max_active: int = 4096):
+                 tile_rows: int = 4096, lanes_per_row: int = 8, check_every: int = 10, max_active: int = 4096):
         if hbm_budget is None:
             import torch
 

@@ -20,10 +20,13 @@ def stream(mods):
     return serving.make_stream(10, rate=400.0, seed=11, sizes=(20, 24))
 
 
+TILE = 4096  # rows per tile: a segment's sums depend on it, so alone and mixed share it
+
+
 @pytest.fixture(scope="module")
 def served(mods, stream):
     serving = mods[3]
-    srv = serving.Server(max_iterations=300, res_tol=1e-6)
+    srv = serving.Server(max_iterations=300, res_tol=1e-6, tile_rows=TILE)
     out = srv.run(stream)
     srv.close()
     return {s.rid: s for s in out}
@@ -44,7 +47,7 @@ def test_alone_equals_in_mix(served, stream, mods):
     for req in stream[:4]:
         sec = sector.GpuSector(lattice.make_model(req.spec, req.Sz, req.kx, req.ky))
         assert sec.build_targets()
-        B = batch.BatchSolver(tile_rows=1024, lanes_per_row=8, check_every=10)
+        B = batch.BatchSolver(tile_rows=TILE, lanes_per_row=8, check_every=10)
         B.add(sec, n_ev=req.n_ev, max_iterations=min(300, sec.n_p), tol=1e-6, seed=1 + req.rid, tag=req.rid)
         alone = B.run()[0]
         mixed = served[req.rid]
