@@ -1,5 +1,6 @@
-"""Host side of the serving loop: the seeded request stream and the footprint
-estimate (no GPU)."""
+"""Host side of the serving loop (no GPU): the seeded request stream, the
+footprint estimate, and the loop's admission and continuous batching run
+against a simulated batch and clock."""
 import math
 
 import numpy as np
@@ -54,3 +55,100 @@ def test_sweep_sort_matches_the_reference_rules():
     assert {s[0] for s in W.sector_list(W.L.TorusSpec("square", 4, 2), Sz=1.0)} == {5}
     txt = W.table(out, 8, 1.0, 0.0)
     assert "ID\tEnergies\tEnergies/site\tSz\tpx\tpy\tJz\tJ2\tEnergies-E0" in txt
+
+
+class _Clock:
+    """Simulated time: every call moves it on a little, batch steps move it
+    on by a step's length."""
+
+    def __init__(self):
+        self.t = 0.0
+
+    def __call__(self):
+        self.t += 1e-4
+        return self.t
+
+
+class _Sector:
+    def __init__(self, model):
+        self.n_p = 100
+        self.closed = False
+
+    def build_targets(self):
+        return True
+
+    def close(self):
+        self.closed = True
+
+
+def _fake_batch(clock, log):
+    class _Batch:
+        """Each segment finishes a fixed number of steps after it joins."""
+
+        def __init__(self, **kw):
+            self.left = {}
+
+        def add(self, sec, n_ev, max_iterations, tol, seed, tag):
+            self.left[tag] = 2 + tag % 3
+            log.append(("add", tag, len(self.left)))
+
+        def step(self, n):
+            clock.t += 0.05
+            for k in self.left:
+                self.left[k] -= 1
+
+        def poll(self):
+            out = []
+            for k in [k for k, v in self.left.items() if v <= 0]:
+                del self.left[k]
+                log.append(("done", k))
+                out.append({"tag": k, "eigs": np.array([-1.0 - k]), "residuals": np.array([1e-7]),
+                            "iterations": 30, "converged": True, "status": 0})
+            return out
+
+        def close(self):
+            pass
+
+    return _Batch
+
+
+def _run(monkeypatch, requests, budget):
+    clock, log = _Clock(), []
+    monkeypatch.setattr(serving, "GpuSector", _Sector)
+    monkeypatch.setattr(serving, "BatchSolver", _fake_batch(clock, log))
+    srv = serving.Server(hbm_budget=budget, max_iterations=300)
+    out = srv.run(requests, clock=clock)
+    return srv, out, log
+
+
+def test_loop_serves_every_request_once_in_arrival_order(monkeypatch):
+    reqs = serving.make_stream(24, rate=50.0, seed=7, sizes=(20, 24))
+    srv, out, log = _run(monkeypatch, reqs, budget=1 << 50)
+    assert sorted(s.rid for s in out) == [r.rid for r in reqs]
+    adds = [e[1] for e in log if e[0] == "add"]
+    assert adds == [r.rid for r in sorted(reqs, key=lambda r: r.arrival)]
+    for s in out:
+        assert s.finished >= s.admitted >= s.arrival - 1e-9 and s.status == 0
+        assert s.eigs[0] == -1.0 - s.rid
+
+
+def test_loop_batches_continuously_within_the_budget(monkeypatch):
+    reqs = serving.make_stream(30, rate=30.0, seed=8, sizes=(20, 24))
+    # requests join while others are still running, and after some finished
+    srv, out, log = _run(monkeypatch, reqs, budget=1 << 50)
+    assert max(e[2] for e in log if e[0] == "add") > 1
+    first_done = next(i for i, e in enumerate(log) if e[0] == "done")
+    assert any(e[0] == "add" for e in log[first_done:])
+    unlimited = srv.peak_live
+    # a budget of two of the largest requests: the estimated bytes of the live
+    # requests never exceed it, and it holds fewer live than no budget does
+    big = max(serving.estimate_bytes(r, 300) for r in reqs)
+    srv, out, _ = _run(monkeypatch, reqs, budget=2 * big)
+    assert len(out) == len(reqs)
+    assert srv.peak_bytes <= 2 * big and 1 <= srv.peak_live < unlimited
+
+
+def test_a_request_larger_than_the_budget_still_runs_alone(monkeypatch):
+    reqs = serving.make_stream(3, rate=100.0, seed=9, sizes=(24,))
+    srv, out, _ = _run(monkeypatch, reqs, budget=1)
+    assert len(out) == 3 and srv.peak_live == 1
