@@ -439,6 +439,11 @@ cudaError_t MixedFinish::reserve_x(int64_t n, int na) {
 }
 
 int MixedFinish::ritz_stored(cudaStream_t st, const float2* V, int64_t n, int m, int na, int cnt) {
+  // the coefficients of up to kRitzChunk Ritz vectors sit in shared memory:
+  // 64 bytes a Krylov vector, past the default 48 KB above 768 vectors
+  const size_t smem_max = sizeof(float2) * std::min(kRitzChunk, na) * cnt;
+  if (smem_max > 48 * 1024)
+    cudaFuncSetAttribute(k_ritz_vectors, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
   for (int q0 = 0; q0 < na; q0 += kRitzChunk) {
     const int qn = std::min(kRitzChunk, na - q0);
     k_ritz_vectors<<<grid_n(n), 256, sizeof(float2) * qn * cnt, st>>>(X, n, V, n, y, m, cnt, q0, qn);

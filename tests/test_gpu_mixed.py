@@ -98,3 +98,14 @@ def test_mixed_with_stored_targets(gpu):
     assert sec.build_targets()
     out = sec.solve_mixed(n_ev=2, iterations=300, reorth_every=1)
     assert np.max(np.abs(out["eigs"][:2] - ref) / np.abs(ref)) <= 1e-9
+
+
+def test_mixed_long_run_stored_ritz_vectors(gpu):
+    """1000 stored steps and 8 Ritz vectors at once: their coefficients take
+    64 KB of shared memory in the Ritz-vector kernel (past the default 48 KB)."""
+    ref = np.array(golden_cases()["tri6x4_k10"]["sectors"][0]["ed2_eigs"][:2])
+    sec = gpu.GpuSector(golden_model("tri6x4_k10", 0))
+    out = sec.solve_mixed(n_ev=8, iterations=1000, reorth_every=1, seed=5)
+    assert out["stats"]["passes"] == 1 and out["stats"]["stored_vectors"] == 1001
+    rel = np.abs(out["eigs"][:2] - ref) / np.abs(ref)
+    assert rel.max() <= 1e-9, (out["eigs"], ref)
