@@ -367,6 +367,9 @@ int solve_lanczos(Sector& S, const edg_solver_opts& o, double* eigs, int64_t cap
   if (how_many <= 0) return fail(EDG_ERR_INVALID, "n_ev must be positive");
   if (cap < how_many) return fail(EDG_ERR_INVALID, "eigs_capacity < n_ev");
   if (o.iterations <= 0 || o.ncycles <= 0) return fail(EDG_ERR_INVALID, "iterations and ncycles must be positive");
+  // a cycle's Ritz vector combines its stored Krylov vectors with
+  // coefficients held in a 2 * kMaxDots buffer
+  if (o.iterations > 2 * Blas::kMaxDots) return fail(EDG_ERR_UNSUPPORTED, "at most 2048 iterations per cycle");
   int iterations = o.iterations;
   cudaStream_t st = S.stream;
   Blas B;

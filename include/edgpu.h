@@ -189,7 +189,7 @@ int edg_count_offdiag(edg_sector* s, int64_t* nnz_off);
 /* Options of the plain (FP64) sector eigensolver. */
 typedef struct {
   int n_ev;                 /* eigenvalues wanted: Num_Eigenvalues */
-  int iterations;           /* Lanczos steps per cycle: Lanczos_iterations */
+  int iterations;           /* Lanczos steps per cycle: Lanczos_iterations (at most 2048) */
   int ncycles;              /* restarts: Lanczos_ncycles */
   double tol;               /* |E0 - E0_previous| < tol ends the middle cycles: tol */
   uint64_t seed;            /* start vector of eigenvalue k: splitmix64 stream seed + k */

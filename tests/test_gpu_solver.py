@@ -102,3 +102,13 @@ def test_three_d_momentum_out_of_range(cuda_device):
     m.kz = 2
     with pytest.raises(EdgError, match="Invalid kx or ky"):
         sector.GpuSector(m)
+
+
+def test_plain_solver_rejects_more_iterations_than_it_can_combine(gpu):
+    """A cycle's Ritz vector combines at most 2048 stored Krylov vectors: more
+    iterations per cycle are refused before any work."""
+    from ed_code_gb300._native import EdgError
+
+    sec = gpu.GpuSector(golden_model("tri4x3", 0))
+    with pytest.raises(EdgError):
+        sec.solve_plain(n_ev=1, iterations=4096, ncycles=1, tol=1e-12, dense_threshold=-1)
