@@ -16,9 +16,9 @@
 //    else as many as fit (the 36-site case: 2 GB each) and the later ones in
 //    a ring of up to eight;
 //  * T's lowest eigenvalues by bisection and their eigenvectors by inverse
-//    iteration, in FP64 in one CTA on the GPU; Ritz values that T shares with
-//    T-without-its-first-row are copies produced by lost orthogonality and are
-//    dropped (Cullum and Willoughby's test);
+//    iteration, in FP64 on the host (lanczos_common.cuh); Ritz values that
+//    T shares with T-without-its-first-row are copies produced by lost
+//    orthogonality and are dropped (Cullum and Willoughby's test);
 //  * Ritz vectors in FP64 -- from the stored vectors, plus, when only the
 //    first k were stored, a re-run of the recurrence from v_{k-1} with the
 //    same alpha/beta for the later ones;
