@@ -239,7 +239,7 @@ typedef struct {
 
 /* Lowest eigenvalues with FP32 Krylov vectors and FP32 H*v; FP64 for alpha/beta
  * (compensated sums), reorthogonalisation coefficients, the tridiagonal
- * eigensolve (on the GPU) and one FP64 H*v per Ritz vector.  Copies of
+ * eigensolve (on the host) and one FP64 H*v per Ritz vector.  Copies of
  * converged eigenvalues that lost orthogonality produces are removed, so each
  * level is returned once.  eigs: FP64 Rayleigh quotients; ritz: the Ritz
  * values of T; residuals: |Hx - eig x|/|x| in FP64; evecs (NULL allowed):
