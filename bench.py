@@ -54,16 +54,69 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
+TRAFFIC_FILE = os.path.join(ROOT, "profiles", "traffic.json")
+
+
 def profile_traffic(kernel_tag: str):
-    """DRAM bytes per launch recorded from an ncu capture in profiles/<tag>.md."""
-    path = os.path.join(ROOT, "profiles", f"{kernel_tag}.md")
+    """DRAM bytes per launch of the dominant kernel, as recorded by
+    `bench.py --ingest-ncu` from an ncu capture (profiles/traffic.json)."""
     try:
-        for line in open(path):
-            if line.strip().startswith("dram_bytes_per_launch:"):
-                return float(line.split(":", 1)[1].split()[0])
-    except OSError:
-        pass
-    return None
+        with open(TRAFFIC_FILE) as f:
+            rec = json.load(f).get(kernel_tag)
+    except (OSError, ValueError):
+        return None
+    return float(rec["dram_bytes_per_launch"]) if rec else None
+
+
+def ingest_ncu(csv_path: str, tag: str, kernel: str, scale: float, note: str) -> dict:
+    """Sum dram__bytes_read.sum + dram__bytes_write.sum per launch of `kernel`
+    from an ncu --csv log (--metrics or --page raw layout), average over the
+    launches, multiply by `scale` (units of a full launch / units captured) and
+    store it under `tag` in profiles/traffic.json."""
+    import csv
+
+    per = {}
+    with open(csv_path, newline="") as f:
+        rows = [r for r in csv.reader(f) if r]
+    head = None
+    for k, r in enumerate(rows):
+        if "Kernel Name" in r and ("Metric Name" in r or any(c.startswith("dram__bytes") for c in r)):
+            head = k
+            break
+    if head is None:
+        raise SystemExit(f"{csv_path}: no ncu CSV header found")
+    h = rows[head]
+    kname, lid = h.index("Kernel Name"), h.index("ID")
+    if "Metric Name" in h:  # --metrics layout: one row per (launch, metric)
+        mname, mval, munit = h.index("Metric Name"), h.index("Metric Value"), h.index("Metric Unit")
+        mult = {"byte": 1, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9, "Tbyte": 1e12}
+        for r in rows[head + 1:]:
+            if len(r) <= mval or kernel not in r[kname] or not r[mname].startswith("dram__bytes_"):
+                continue
+            per.setdefault(r[lid], 0.0)
+            per[r[lid]] += float(r[mval].replace(",", "")) * mult.get(r[munit], 1)
+    else:  # --page raw layout: one row per launch, a units row under the header
+        cols = [h.index(c) for c in ("dram__bytes_read.sum", "dram__bytes_write.sum")]
+        units = rows[head + 1]
+        mult = {"byte": 1, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9, "Tbyte": 1e12}
+        for r in rows[head + 2:]:
+            if len(r) <= max(cols) or kernel not in r[kname]:
+                continue
+            per[r[lid]] = sum(float(r[c].replace(",", "")) * mult.get(units[c], 1) for c in cols)
+    if not per:
+        raise SystemExit(f"{csv_path}: no dram__bytes rows for kernel {kernel!r}")
+    mean = sum(per.values()) / len(per)
+    try:
+        with open(TRAFFIC_FILE) as f:
+            data = json.load(f)
+    except (OSError, ValueError):
+        data = {}
+    data[tag] = {"dram_bytes_per_launch": mean * scale, "captured_bytes_per_launch": mean, "scale": scale,
+                 "launches": len(per), "kernel": kernel, "source": os.path.basename(csv_path), "note": note}
+    with open(TRAFFIC_FILE, "w") as f:
+        json.dump(data, f, indent=1, sort_keys=True)
+        f.write("\n")
+    return data[tag]
 
 
 class ClockSampler:
@@ -254,7 +307,7 @@ def run_device(args, world, rank, local_rank):
     # stored targets: the search done once, its results streamed every H*v
     mode = "matrix-free"
     t_tgt = None
-    lpr, tune_ms, t_pack = None, None, None
+    lpr, tune_ms = None, None
     if not args.matrix_free:
         t0 = time.perf_counter()
         if sec.build_targets():
@@ -268,14 +321,6 @@ def run_device(args, world, rank, local_rank):
                 lpr = lanes
             else:
                 lpr, tune_ms = sec.tune(0)
-            # column panels on request (measured slower than the tuned row
-            # kernel at 32 and 36 sites)
-            if args.panels > 0:
-                t0 = time.perf_counter()
-                sec.pack_panels(max(args.panels, 0))
-                torch.cuda.synchronize()
-                t_pack = time.perf_counter() - t0
-                mode = "panels"
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
             sec.hv(v, w, stream)
@@ -345,7 +390,6 @@ def run_device(args, world, rank, local_rank):
                    "matrix_free_ms_per_step": mf_ms,
                    "lanes_per_row": lpr, "cache_policy": sec.info.get("cache_policy"),
                    "ctas_per_sm": sec.info.get("ctas_per_sm"), "pipelined": sec.info.get("pipelined"),
-                   "panels": sec.info.get("panels"), "panel_pack_seconds": None if t_pack is None else round(t_pack, 3),
                    "row_kernel_ms": None if tune_ms is None else round(float(min(x for x in tune_ms if x > 0)), 3),
                    "tune_ms_lpr_8_16_32": None if tune_ms is None else [round(float(x), 3) for x in tune_ms],
                    "matrix_free_GBps": B_mf / (mf_ms / 1e3) / 1e9,
@@ -355,9 +399,9 @@ def run_device(args, world, rank, local_rank):
         "cpu_baseline": cpu,
         "e2e": e2e,
         "clocks": clocks,
-        # per step: the u = v/norm pass plus one row kernel, or one launch per
-        # panel; the matrix-free kernel is one launch
-        "gpu_launches": args.steps * ({"stored-rows": 2, "panels": 1 + (sec.info.get("panels") or 0)}.get(mode, 1)),
+        # per step: the u = v/norm pass plus one row kernel; the matrix-free
+        # kernel is one launch
+        "gpu_launches": args.steps * (2 if mode == "stored-rows" else 1),
     }
     if rank == 0:
         print(json.dumps(out), flush=True)
@@ -599,55 +643,6 @@ def run_solve36(args):
     return 0
 
 
-def run_gather_peak(args):
-    """Random single-entry loads from a vector of the 36-site sector's size
-    (edg_probe_gather): the ceiling of the stored-row H*v's far gathers."""
-    import ctypes as C
-
-    import torch
-
-    from ed_code_gb300 import _native as N
-    from ed_code_gb300.sector import fill_random
-
-    torch.cuda.init()
-    n = 252091362  # 6x6 triangular torus, Sz=0, k=Gamma
-    fp64 = args.dtype == "c128"
-    u = torch.empty(n, dtype=torch.complex128 if fp64 else torch.complex64, device="cuda")
-    out = torch.zeros(1, dtype=torch.float32, device="cuda")
-    st = torch.cuda.Stream()
-    fill_random(u, 5, st)
-    count = 4_000_000_000
-    code = N.EDG_C128 if fp64 else N.EDG_C64
-
-    def launch(seed):
-        N.check(N.lib().edg_probe_gather(C.c_void_p(u.data_ptr()), n, code, args.hint, count, seed,
-                                         C.c_void_p(out.data_ptr()), C.c_void_p(st.cuda_stream)))
-
-    for k in range(args.warmup):
-        launch(100 + k)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(st)
-    for k in range(args.steps):
-        launch(k)
-    e1.record(st)
-    torch.cuda.synchronize()
-    t = e0.elapsed_time(e1) / 1e3 / args.steps
-    elem = 16 if fp64 else 8
-    peak, peak_kind = measured_peak_hbm()
-    sector_gbs = count * 32 / t / 1e9
-    out = {"metric": "random single-entry loads", "mode": "gather-peak", "value": count / t / 1e9,
-           "unit": "G loads/s", "higher_is_better": True, "n_gpus": 1, "data": "synthetic",
-           "ms_per_launch": t * 1e3, "loads_per_launch": count, "entry_bytes": elem,
-           "sector_GBps": sector_gbs, "sector_frac_of_copy_peak": sector_gbs / peak, "useful_GBps": count * elem / t / 1e9,
-           "copy_peak_GBps": peak, "peak_kind": peak_kind,
-           "config": {"vector_entries": n, "vector_bytes": n * elem, "positions": "splitmix64-hashed, uniform",
-                      "l2_hint": ["none", "evict_last"][args.hint],
-                      "l2": "vector 2 GB (c64) or 4 GB (c128) against a 129 MB L2"}}
-    print(json.dumps(out), flush=True)
-    return 0
-
-
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -661,11 +656,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--rows", default=None,
                     help="LANES,POLICY[,CTAS_PER_SM[,PIPELINED]]: fix the stored-row kernel instead of timing it")
-    ap.add_argument("--panels", type=int, default=0,
-                    help="regroup the stored rows into this many column panels (0: keep the row kernel)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-step-seconds", type=float, default=4.0)
-    ap.add_argument("--mode", choices=["hv", "serve", "batch", "precision", "solve36", "gather-peak"], default="hv",
+    ap.add_argument("--mode", choices=["hv", "serve", "batch", "precision", "solve36"], default="hv",
                     help="hv: the headline H*v line; the others time the solver configurations")
     ap.add_argument("--requests", type=int, default=64)
     ap.add_argument("--rate", type=float, default=200.0)
@@ -676,12 +669,23 @@ def main():
     ap.add_argument("--momenta", type=int, default=30)
     ap.add_argument("--reorth", type=int, default=0)
     ap.add_argument("--serve-tile", type=int, default=4096, help="serve: rows per tile of the batch kernels")
-    ap.add_argument("--hint", type=int, choices=[0, 1], default=1,
-                    help="gather-peak: 0 plain loads, 1 the H*v's L2 evict_last policy")
+    ap.add_argument("--ingest-ncu", metavar="CSV", default=None,
+                    help="record the DRAM bytes per launch of --kernel from this ncu CSV in profiles/traffic.json "
+                         "under --tag, and exit")
+    ap.add_argument("--tag", default=None, help="--ingest-ncu: the record's key (hv_<mode>_<workload>_<dtype>)")
+    ap.add_argument("--kernel", default="k_hv_csr", help="--ingest-ncu: kernel name substring")
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="--ingest-ncu: units of a full launch / units of the captured launch")
+    ap.add_argument("--note", default="", help="--ingest-ncu: how the capture was made")
     args = ap.parse_args()
+    if args.ingest_ncu:
+        if not args.tag:
+            ap.error("--ingest-ncu needs --tag")
+        print(json.dumps(ingest_ncu(args.ingest_ncu, args.tag, args.kernel, args.scale, args.note)))
+        return 0
     if args.mode != "hv" and args.impl == "gb300":
         return {"serve": run_serve, "batch": run_batch, "precision": run_precision,
-                "solve36": run_solve36, "gather-peak": run_gather_peak}[args.mode](args)
+                "solve36": run_solve36}[args.mode](args)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

@@ -54,7 +54,7 @@ class edg_sector_info(C.Structure):
         ("n_sites", C.c_int), ("n_ones", C.c_int), ("L1", C.c_int), ("L2", C.c_int), ("kx", C.c_int),
         ("ky", C.c_int), ("torus", C.c_int), ("n_groups", C.c_int), ("n_p", C.c_int64), ("n_configs", C.c_int64),
         ("device_bytes", C.c_int64), ("n_targets", C.c_int64), ("lanes_per_row", C.c_int),
-        ("cache_policy", C.c_int), ("panels", C.c_int), ("L3", C.c_int), ("kz", C.c_int),
+        ("cache_policy", C.c_int), ("L3", C.c_int), ("kz", C.c_int),
         ("entry_bytes", C.c_int), ("n_values", C.c_int), ("ctas_per_sm", C.c_int), ("pipelined", C.c_int),
     ]
 
@@ -116,7 +116,6 @@ SIGNATURES = {
     "edg_hv": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "edg_hv_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
     "edg_sector_set_rows": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]),
-    "edg_sector_pack_panels": (C.c_int, [C.c_void_p, C.c_int]),
     "edg_batch_create": (C.c_int, [C.POINTER(edg_batch_opts), C.POINTER(C.c_void_p)]),
     "edg_batch_destroy": (C.c_int, [C.c_void_p]),
     "edg_batch_footprint": (C.c_int, [C.c_void_p, C.POINTER(edg_batch_request), C.POINTER(C.c_int64)]),
@@ -128,8 +127,6 @@ SIGNATURES = {
     "edg_hv_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "edg_count_offdiag": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
     "edg_fill_random": (C.c_int, [C.c_void_p, C.c_int64, C.c_int, C.c_uint64, C.c_void_p]),
-    "edg_probe_gather": (C.c_int, [C.c_void_p, C.c_int64, C.c_int, C.c_int, C.c_int64, C.c_uint64, C.c_void_p,
-                                   C.c_void_p]),
     "edg_sector_build_targets": (C.c_int, [C.c_void_p, C.c_int64]),
     "edg_sector_free_targets": (C.c_int, [C.c_void_p]),
     "edg_sector_tune": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.c_void_p]),

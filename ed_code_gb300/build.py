@@ -22,8 +22,8 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libedgpu.so")
 REF_LIB = os.path.join(HERE, "libedgpu_ref.so")
 
-CUDA_UNITS = ["capi.cu", "basis.cu", "hv.cu", "hv_torus.cu", "lanczos.cu", "lanczos_mixed.cu", "targets.cu",
-              "hv_noalloc.cu", "batch.cu", "probe.cu"]
+CUDA_UNITS = ["capi.cu", "basis.cu", "hv.cu", "lanczos.cu", "lanczos_mixed.cu", "targets.cu", "hv_noalloc.cu",
+              "batch.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -38,7 +38,7 @@ static void free_sector(Sector& S) {
   free_targets(S);
   void* ptrs[] = {S.dP,   S.reps,    S.lid,         S.recs,         S.vrecs,       S.Ia,    S.Ib,
                   S.groups, S.ch,   S.bows,    S.nk,          S.rots,         S.perms,       S.binom, S.host_in.ptr,
-                  S.host_out.ptr, S.lz_work.ptr, S.tplan, S.tgroups};
+                  S.host_out.ptr, S.lz_work.ptr};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (S.stream) cudaStreamDestroy(S.stream);
@@ -262,72 +262,6 @@ static int create_sector(const edg_model* m, int n_ones, int kx, int ky, int kz,
   }
   P.n_bowties = (int)bows.size();
 
-  // Torus plan: pairs filed by displacement class (see TorusPlan).
-  std::vector<TorusGroup> tgroups;
-  TorusPlan tplan;
-  std::memset(&tplan, 0, sizeof tplan);
-  bool torus_fast = P.torus && L1 <= 8 && L2 <= 8 && !P.use_chch && !groups.empty();
-  for (size_t g = 0; torus_fast && g < groups.size(); ++g)
-    if (group_ch[g].size() > 2) torus_fast = false;
-  if (torus_fast) {
-    const int Lx = L1, Ly = L2;
-    std::memset(tplan.gid, 0xFF, sizeof tplan.gid);
-    std::vector<std::pair<int, int>> cls;  // displacement (dx, dy) of each class
-    for (size_t g = 0; torus_fast && g < groups.size(); ++g) {
-      const int a = groups[g].a, b = groups[g].b;
-      const int dx = ((b % Lx) - (a % Lx) + Lx) % Lx, dy = ((b / Lx) - (a / Lx) + Ly) % Ly;
-      const int nx = (Lx - dx) % Lx, ny = (Ly - dy) % Ly;
-      int c = -1, site = a;
-      for (size_t k = 0; k < cls.size(); ++k) {
-        if (cls[k] == std::make_pair(dx, dy)) { c = (int)k; site = a; break; }
-        if (cls[k] == std::make_pair(nx, ny)) { c = (int)k; site = b; break; }
-      }
-      if (c < 0) {
-        if ((int)cls.size() == kMaxClasses) { torus_fast = false; break; }
-        cls.push_back({dx, dy});
-        c = (int)cls.size() - 1;
-        site = a;
-      }
-      if (tplan.gid[c][site] != 0xFFFF) { torus_fast = false; break; }
-      tplan.gid[c][site] = (uint16_t)g;
-      tplan.cls[c].classmask |= 1ull << site;
-    }
-    if (torus_fast) {
-      tplan.n_classes = (int)cls.size();
-      for (size_t k = 0; k < cls.size(); ++k) {
-        tplan.cls[k].rot_a = (Lx - cls[k].first) % Lx;   // T_{-d}: bit x+d lands on x
-        tplan.cls[k].rot_b = (Ly - cls[k].second) % Ly;
-      }
-      for (size_t g = 0; g < groups.size(); ++g) {
-        TorusGroup tg;
-        std::memset(&tg, 0, sizeof tg);
-        const TermGroup& gr = groups[g];
-        tg.mask = gr.mask;
-        tg.fac = gr.fac;
-        for (int cs = 0; cs < 2; ++cs) {
-          tg.B[2 * cs] = gr.Bre[cs];
-          tg.B[2 * cs + 1] = gr.Bim[cs];
-        }
-        const std::vector<ChTerm>& cv = group_ch[g];
-        if (cv.size() > 0) {
-          tg.z1 = (uint8_t)cv[0].z;
-          for (int cs = 0; cs < 2; ++cs) { tg.A1[2 * cs] = cv[0].Are[cs]; tg.A1[2 * cs + 1] = cv[0].Aim[cs]; }
-        }
-        if (cv.size() > 1) {
-          tg.z2 = (uint8_t)cv[1].z;
-          for (int cs = 0; cs < 2; ++cs) { tg.A2[2 * cs] = cv[1].Are[cs]; tg.A2[2 * cs + 1] = cv[1].Aim[cs]; }
-        }
-        tg.a = (uint8_t)gr.a;
-        tg.ya = (uint8_t)(gr.a / Lx);
-        tg.yb = (uint8_t)(gr.b / Lx);
-        tg.da = (uint8_t)(1u << (gr.a % Lx));
-        tg.db = (uint8_t)(1u << (gr.b % Lx));
-        tg.same_row = tg.ya == tg.yb;
-        tgroups.push_back(tg);
-      }
-    }
-  }
-
   // Lin tables (Lin_Tables.cpp:57-78; Ib as Momentum_Basis.cpp:731-737):
   // Ia = 1-based rank among half-words of equal popcount; Ib[l] = Lin index
   // of the first configuration with left half l, or -1 when there is none.
@@ -404,17 +338,11 @@ static int create_sector(const edg_model* m, int n_ones, int kx, int ky, int kz,
   if ((e = upload(&S.rots, rots.data(), rots.size(), bytes)) != cudaSuccess) return cuda_fail(e, "rots");
   if ((e = upload(&S.perms, perms.data(), perms.size(), bytes)) != cudaSuccess) return cuda_fail(e, "perms");
   if ((e = upload(&S.binom, binom.data(), binom.size(), bytes)) != cudaSuccess) return cuda_fail(e, "binom");
-  if (torus_fast) {
-    if ((e = upload(&S.tplan, &tplan, 1, bytes)) != cudaSuccess) return cuda_fail(e, "torus plan");
-    if ((e = upload(&S.tgroups, tgroups.data(), tgroups.size(), bytes)) != cudaSuccess)
-      return cuda_fail(e, "torus groups");
-  }
   e = cudaMalloc(&S.recs, sizeof(RankRec) * std::max<int64_t>(1, P.n_recs));
   if (e != cudaSuccess) return fail(EDG_ERR_NOMEM, "rank records: out of device memory");
   bytes += sizeof(RankRec) * std::max<int64_t>(1, P.n_recs);
   if ((e = upload(&S.dP, &P, 1, bytes)) != cudaSuccess) return cuda_fail(e, "params");
   S.device_bytes = bytes;
-  if (const char* hv = std::getenv("EDG_HV_VARIANT")) S.hv_variant = (std::string(hv) == "torus") ? 1 : 0;
 
   SectorView& V = S.V;
   V.params = S.dP;
@@ -516,8 +444,7 @@ int edg_sector_get_info(const edg_sector* s, edg_sector_info* info) {
   info->cache_policy = s->s.col ? s->s.csr_pol : 0;
   info->ctas_per_sm = s->s.col ? s->s.csr_cps : 0;
   info->pipelined = s->s.col ? s->s.csr_pipe : 0;
-  info->panels = s->s.pan_p;
-  info->entry_bytes = s->s.col ? (s->s.pack_cb ? 4 : 6) : (s->s.pan_ent ? 6 : 0);
+  info->entry_bytes = s->s.col ? (s->s.pack_cb ? 4 : 6) : 0;
   info->n_values = s->s.n_vals;
   return EDG_OK;
 }
@@ -702,14 +629,6 @@ int edg_sector_tune(edg_sector* s, int lanes_per_row, int* chosen, double* ms) {
   if (!s) return fail(EDG_ERR_INVALID, "NULL sector");
   const int rc = tune_rows(s->s, lanes_per_row, chosen, ms);
   if (rc != EDG_OK) return fail(rc, "tuning the stored-row kernel failed");
-  return EDG_OK;
-}
-
-int edg_sector_pack_panels(edg_sector* s, int n_panels) {
-  if (!s) return fail(EDG_ERR_INVALID, "NULL sector");
-  std::string err;
-  const int rc = pack_panels(s->s, n_panels, err);
-  if (rc != EDG_OK) return fail(rc, err);
   return EDG_OK;
 }
 

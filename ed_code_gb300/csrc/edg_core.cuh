@@ -123,31 +123,6 @@ struct SectorParams {
   int64_t n_targets;
 };
 
-// Torus plan: flip groups filed by displacement class.  Class c holds the
-// pairs (x, x+d_c); a state's anti-aligned pairs of class c are the set bits of
-// (s XOR T_{-d_c}(s)) & classmask, one 64-bit operation per class instead of
-// one test per pair.  Built only for row-major tori with Lx, Ly <= 8, at most
-// two chirality terms per pair and no ChCh terms.
-constexpr int kMaxClasses = 16;
-struct TorusClass {
-  uint64_t classmask;
-  int rot_a, rot_b;  // T_{-d}: rotate rows by rot_b, then within rows by rot_a
-};
-struct TorusGroup {
-  uint64_t mask;
-  double fac;
-  double B[4];   // bond coefficient: re/im for bit a of s = 0, then = 1
-  double A1[4];  // first chirality term (sign from bit z1 of s), same layout
-  double A2[4];  // second chirality term (bit z2)
-  uint8_t a, z1, z2, ya, yb, da, db, same_row;  // rows of the two sites and their bit in the row
-};
-struct TorusPlan {
-  int n_classes;
-  int pad[3];
-  TorusClass cls[kMaxClasses];
-  uint16_t gid[kMaxClasses][64];  // group of (class, site x), 0xFFFF when none
-};
-
 // --------------------------------------------------------------------------
 // Lin index and representative position
 // --------------------------------------------------------------------------

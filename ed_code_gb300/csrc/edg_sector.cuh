@@ -86,12 +86,6 @@ struct Sector {
   cudaEvent_t chunk_done[8] = {};
   // Lanczos work area (allocated on first use)
   DeviceBuffer lz_work;
-  // torus plan (null when the sector does not qualify)
-  TorusPlan* tplan = nullptr;
-  TorusGroup* tgroups = nullptr;
-  // H*v kernel: 0 = hv.cu (default), 1 = hv_torus.cu when the sector has a
-  // torus plan.  Chosen at sector creation from EDG_HV_VARIANT (for A/B timing).
-  int hv_variant = 0;
   // stored targets (targets.cu): CSR rows of (column, value id)
   uint64_t* row_ptr = nullptr;  // n_p + 1
   uint32_t* col = nullptr;      // column, or column | value id << pack_cb
@@ -107,14 +101,6 @@ struct Sector {
   int csr_pol = 1;              // cache policy of the CSR loads (1 or 2): edg_sector_tune
   int csr_cps = 0;              // CTAs per SM of the CSR kernel (0: as many as fit): edg_sector_tune
   int csr_pipe = 0;             // 1: the CSR kernel loads the next rows' entries ahead: edg_sector_tune
-  // column panels (edg_sector_pack_panels): the stored rows regrouped so that
-  // one H*v launch per panel gathers from one L2-sized slice of u
-  uint32_t* pan_ent = nullptr;  // (column - p*pan_c) | local row << 23
-  uint16_t* pan_vid = nullptr;
-  uint64_t* pan_off = nullptr;  // pan_p * pan_nb + 1 segment offsets, panel-major
-  int pan_p = 0;                // panels
-  int64_t pan_c = 0;            // columns per panel (< 2^23)
-  int64_t pan_nb = 0;           // row blocks of kPanRows rows
 };
 
 // basis.cu
@@ -150,13 +136,10 @@ struct MixedFinish {
 };
 void pick_levels(const std::vector<double>& rr, const std::vector<double>& th, const std::vector<int>& acc_h, int na,
                  int want, double* eigs, double* ritz, double* resid, std::vector<int>& keep);
-// hv_torus.cu
-cudaError_t launch_hv_torus(const Sector& S, const void* v, void* w, bool fp64, cudaStream_t st);
 cudaError_t count_offdiag(const Sector& S, unsigned long long* nnz_dev, cudaStream_t st);
 int build_targets(Sector& S, int64_t max_bytes, std::string& err);
 void free_targets(Sector& S);
 cudaError_t launch_hv_stored(const Sector& S, const void* v, void* w, bool fp64, cudaStream_t st);
-int pack_panels(Sector& S, int n_panels, std::string& err);
 // stored rows in row order: rows [r0, r1) of H*v, with the u = v/norm pass first when with_u
 cudaError_t launch_hv_rows(const Sector& S, const void* v, void* w, bool fp64, int64_t r0, int64_t r1, bool with_u,
                            cudaStream_t st);

@@ -185,8 +185,7 @@ cudaError_t launch_t(const Sector& S, const void* v, void* w, cudaStream_t st) {
 }  // namespace
 
 cudaError_t launch_hv(const Sector& S, const void* v, void* w, bool fp64, cudaStream_t st) {
-  if (S.col || S.pan_ent) return launch_hv_stored(S, v, w, fp64, st);
-  if (S.tplan && S.hv_variant == 1) return launch_hv_torus(S, v, w, fp64, st);
+  if (S.col) return launch_hv_stored(S, v, w, fp64, st);
   return launch_hv_generic(S, v, w, fp64, st);
 }
 

@@ -441,9 +441,18 @@ cudaError_t MixedFinish::reserve_x(int64_t n, int na) {
 int MixedFinish::ritz_stored(cudaStream_t st, const float2* V, int64_t n, int m, int na, int cnt) {
   // the coefficients of up to kRitzChunk Ritz vectors sit in shared memory:
   // 64 bytes a Krylov vector, past the default 48 KB above 768 vectors
+  // (the solvers cap the steps at 2000, i.e. 128 KB, within the opt-in limit)
   const size_t smem_max = sizeof(float2) * std::min(kRitzChunk, na) * cnt;
-  if (smem_max > 48 * 1024)
-    cudaFuncSetAttribute(k_ritz_vectors, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
+  if (smem_max > 48 * 1024) {
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (smem_max > (size_t)optin)
+      return fail(EDG_ERR_UNSUPPORTED, "mixed Lanczos: too many stored steps for the Ritz-vector kernel");
+    const cudaError_t ea = cudaFuncSetAttribute(k_ritz_vectors, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)smem_max);
+    if (ea != cudaSuccess) return cuda_fail(ea, "mixed Lanczos: Ritz-vector kernel shared memory");
+  }
   for (int q0 = 0; q0 < na; q0 += kRitzChunk) {
     const int qn = std::min(kRitzChunk, na - q0);
     k_ritz_vectors<<<grid_n(n), 256, sizeof(float2) * qn * cnt, st>>>(X, n, V, n, y, m, cnt, q0, qn);

@@ -430,241 +430,6 @@ cudaError_t launch_csr_t(const Sector& S, const void* v, void* w, cudaStream_t s
                         : launch_csr_p<Real, 1>(S, v, w, st, r0, r1, with_u);
 }
 
-// ---- column panels -------------------------------------------------------
-//
-// At 36 sites u is 2 GB against a 129 MB L2, and about 45% of the targets lie
-// far from their row in the representative order, so most gathers of the
-// row-ordered kernel miss L2 and move a 32-byte sector for an 8-byte entry.
-// Panels trade that for a pass over w per panel: the columns are cut into P
-// panels of at most 2^23 entries (63 MB of complex64 at 36 sites), the rows
-// into blocks of kPanRows, and segment (block b, panel p) holds the entries
-// of b's rows whose column lies in p, in row order, each as one u32
-// (column - p*C | local row << 23) plus the value id.  H*v runs one launch per
-// panel: a warp takes a row block, reduces its segment by row with a
-// segmented shuffle scan, and adds the row sums into w; the first launch also
-// adds the diagonal Ezz*u_i, the last one multiplies by norm_i, so w_i =
-// norm_i (sum_t vtab[vid_t] u_{col_t} + Ezz_i u_i), as in the row kernel.
-constexpr int kPanRows = 64;
-constexpr int kPanBits = 23;
-
-// entries per (block, panel), panel-major: counts[p * nb + b]
-__global__ void __launch_bounds__(kTgtThreads) k_pan_count(const uint64_t* __restrict__ row_ptr,
-                                                           const uint32_t* __restrict__ col, int cb, int64_t n,
-                                                           int64_t nb, int P, int64_t C, uint32_t* __restrict__ counts) {
-  const uint32_t cmask = cb ? (1u << cb) - 1u : 0xFFFFFFFFu;
-  extern __shared__ uint32_t hist[];  // kWarpsPerBlock x P
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  uint32_t* h = hist + wid * P;
-  const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t b = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < nb; b += n_warps) {
-    for (int k = lane; k < P; k += 32) h[k] = 0;
-    __syncwarp();
-    const uint64_t beg = row_ptr[b * kPanRows], end = row_ptr[min(n, (b + 1) * kPanRows)];
-    for (uint64_t t = beg + lane; t < end; t += 32) atomicAdd(&h[(int)((col[t] & cmask) / C)], 1u);
-    __syncwarp();
-    for (int k = lane; k < P; k += 32) counts[(int64_t)k * nb + b] = h[k];
-    __syncwarp();
-  }
-}
-
-// write each block's entries to their segments, keeping the row order: the
-// lanes of a 32-entry chunk that share a panel are ranked with match_any
-__global__ void __launch_bounds__(kTgtThreads) k_pan_scatter(const uint64_t* __restrict__ row_ptr,
-                                                             const uint32_t* __restrict__ col,
-                                                             const uint16_t* __restrict__ vid, int cb, int64_t n,
-                                                             int64_t nb, int P, int64_t C,
-                                                             const uint64_t* __restrict__ off,
-                                                             uint32_t* __restrict__ ent, uint16_t* __restrict__ evid) {
-  const uint32_t cmask = cb ? (1u << cb) - 1u : 0xFFFFFFFFu;
-  extern __shared__ uint32_t run[];  // kWarpsPerBlock x P running counts
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  uint32_t* rc = run + wid * P;
-  const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t b = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < nb; b += n_warps) {
-    for (int k = lane; k < P; k += 32) rc[k] = 0;
-    __syncwarp();
-    const int64_t r_end = min(n, (b + 1) * kPanRows);
-    for (int64_t r = b * kPanRows; r < r_end; ++r) {
-      const uint64_t beg = row_ptr[r], end = row_ptr[r + 1];
-      for (uint64_t t0 = beg; t0 < end; t0 += 32) {
-        const uint64_t t = t0 + lane;
-        const bool ok = t < end;
-        const uint32_t e = ok ? col[t] : 0u;
-        const uint32_t c = e & cmask;
-        const int p = ok ? (int)(c / C) : -1;
-        const unsigned valid = __ballot_sync(0xffffffffu, ok);
-        const unsigned same = __match_any_sync(0xffffffffu, p) & valid;
-        const uint32_t base = ok ? rc[p] : 0u;
-        __syncwarp();
-        if (ok) {
-          const uint64_t pos = off[(int64_t)p * nb + b] + base + __popc(same & ((1u << lane) - 1u));
-          ent[pos] = (uint32_t)(c - (int64_t)p * C) | ((uint32_t)(r - b * kPanRows) << kPanBits);
-          evid[pos] = cb ? (uint16_t)(e >> cb) : vid[t];
-          if ((same & ((1u << lane) - 1u)) == 0u) rc[p] = base + __popc(same);
-        }
-        __syncwarp();
-      }
-    }
-  }
-}
-
-// One panel of H*v (see above).  Partial sums per row block in shared memory.
-// A warp issues the loads of up to kPanQ chunks of 32 entries at once, then
-// all their gathers, so a segment costs about two memory round trips; the
-// block's w values and the next block's offsets are loaded ahead.
-constexpr int kPanQ = 4;
-template <typename Real, bool kSmemTab>
-__global__ void __launch_bounds__(kTgtThreads) k_hv_pan(const uint32_t* __restrict__ ent,
-                                                        const uint16_t* __restrict__ evid,
-                                                        const uint64_t* __restrict__ off, int64_t nb, int p,
-                                                        int P, int64_t C,
-                                                        const typename CT2<Real>::T* __restrict__ vtab, int n_vals,
-                                                        const double* __restrict__ ezz,
-                                                        const uint8_t* __restrict__ lid,
-                                                        const double* __restrict__ nrm_tab, int64_t n,
-                                                        const typename CT2<Real>::T* __restrict__ u,
-                                                        typename CT2<Real>::T* __restrict__ w) {
-  using CT = typename CT2<Real>::T;
-  extern __shared__ __align__(16) uint8_t sm[];
-  CT* tab = reinterpret_cast<CT*>(sm);
-  __shared__ Real nrm[65];
-  __shared__ CT part[kWarpsPerBlock][kPanRows];
-  for (int k = threadIdx.x; k < 65; k += blockDim.x) nrm[k] = (Real)nrm_tab[k];
-  if (kSmemTab)
-    for (int k = threadIdx.x; k < n_vals; k += blockDim.x) tab[k] = vtab[k];
-  __syncthreads();
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  CT* ps = part[wid];
-  const uint64_t pf = l2_evict_first(), pl = l2_evict_last();
-  const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  const CT* up = u + (int64_t)p * C;
-  const unsigned long long* op = reinterpret_cast<const unsigned long long*>(off) + (int64_t)p * nb;
-  int64_t b = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  uint64_t beg = 0, end = 0;
-  if (b < nb) {
-    beg = __ldg(op + b);
-    end = __ldg(op + b + 1);
-  }
-  for (; b < nb; b += n_warps) {
-    const int64_t bn = b + n_warps;
-    uint64_t nbeg = 0, nend = 0;
-    if (bn < nb) {
-      nbeg = __ldg(op + bn);
-      nend = __ldg(op + bn + 1);
-    }
-    // this block's rows: w (or the diagonal term) loaded ahead
-    CT acc[2];
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int64_t i = b * kPanRows + lane + 32 * h;
-      acc[h].x = acc[h].y = 0;
-      if (i < n) {
-        if (p == 0) {
-          const Real d = (Real)ezz[i];
-          const CT ui = u[i];
-          acc[h].x = d * ui.x;
-          acc[h].y = d * ui.y;
-        } else {
-          acc[h] = w[i];
-        }
-      }
-    }
-    ps[lane].x = ps[lane].y = 0;
-    ps[lane + 32].x = ps[lane + 32].y = 0;
-    unsigned lo = 0, hi = 0;  // rows touched
-    __syncwarp();
-    for (uint64_t t0 = beg; t0 < end; t0 += 32 * kPanQ) {
-      uint32_t e[kPanQ];
-      int id[kPanQ];
-#pragma unroll
-      for (int q = 0; q < kPanQ; ++q) {
-        const uint64_t t = t0 + 32 * q + lane;
-        e[q] = t < end ? ld_row<2>(ent + t, pf) : 0xFFFFFFFFu;
-        id[q] = t < end ? ld_row<2>(evid + t, pf) : 0;
-      }
-      CT x[kPanQ];
-#pragma unroll
-      for (int q = 0; q < kPanQ; ++q)
-        if (e[q] != 0xFFFFFFFFu) x[q] = ld_keep(up + (e[q] & ((1u << kPanBits) - 1u)), pl);
-#pragma unroll
-      for (int q = 0; q < kPanQ; ++q) {
-        if (t0 + 32 * q >= end) break;  // the same for the whole warp
-        const bool ok = e[q] != 0xFFFFFFFFu;
-        const int r = ok ? (int)(e[q] >> kPanBits) : kPanRows;
-        Real ar = 0, ai = 0;
-        if (ok) {
-          const CT c = kSmemTab ? tab[id[q]] : __ldg(vtab + id[q]);
-          ar = c.x * x[q].x - c.y * x[q].y;
-          ai = c.x * x[q].y + c.y * x[q].x;
-        }
-        // inclusive segmented scan over lanes with equal r (rows are contiguous)
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const Real br = __shfl_up_sync(0xffffffffu, ar, o), bi = __shfl_up_sync(0xffffffffu, ai, o);
-          const int rr = __shfl_up_sync(0xffffffffu, r, o);
-          if (lane >= o && rr == r) {
-            ar += br;
-            ai += bi;
-          }
-        }
-        const int rn = __shfl_down_sync(0xffffffffu, r, 1);
-        const bool tail = ok && (lane == 31 || rn != r);
-        if (tail) {
-          ps[r].x += ar;
-          ps[r].y += ai;
-        }
-        lo |= __reduce_or_sync(0xffffffffu, tail && r < 32 ? 1u << r : 0u);
-        hi |= __reduce_or_sync(0xffffffffu, tail && r >= 32 ? 1u << (r - 32) : 0u);
-        __syncwarp();
-      }
-    }
-    // add the row sums into w
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int rr = lane + 32 * h;
-      const int64_t i = b * kPanRows + rr;
-      if (i >= n) continue;
-      const bool touched = ((h ? hi : lo) >> lane) & 1u;
-      if (p != 0 && p != P - 1 && !touched) continue;
-      CT a = acc[h];
-      if (touched) {
-        a.x += ps[rr].x;
-        a.y += ps[rr].y;
-      }
-      if (p == P - 1) {
-        const Real ni = nrm[lid[i]];
-        a.x *= ni;
-        a.y *= ni;
-      }
-      w[i] = a;
-    }
-    __syncwarp();
-    beg = nbeg;
-    end = nend;
-  }
-}
-
-template <typename Real>
-cudaError_t launch_pan_t(const Sector& S, const void* v, void* w, cudaStream_t st) {
-  using CT = typename CT2<Real>::T;
-  const int64_t n = S.P.n_p;
-  k_u_scale<Real><<<(int)std::min<int64_t>((n + 255) / 256, 152 * 32), 256, 0, st>>>(
-      reinterpret_cast<const CT*>(v), S.lid, params_field(S, offsetof(SectorParams, nrm_inv)), n,
-      reinterpret_cast<CT*>(S.ubuf.ptr));
-  const CT* tab = reinterpret_cast<const CT*>(sizeof(Real) == 8 ? (const void*)S.vtab64 : (const void*)S.vtab32);
-  const size_t tab_bytes = sizeof(CT) * S.n_vals;
-  const double* nrm = params_field(S, offsetof(SectorParams, nrm));
-  const bool smem_tab = tab_bytes <= 64 * 1024;
-  auto kern = smem_tab ? k_hv_pan<Real, true> : k_hv_pan<Real, false>;
-  const size_t dyn = smem_tab ? tab_bytes : 0;
-  const int grid = grid_for(kern, dyn, S.pan_nb * 32, kTgtThreads);
-  for (int p = 0; p < S.pan_p; ++p)
-    kern<<<grid, kTgtThreads, dyn, st>>>(S.pan_ent, S.pan_vid, S.pan_off, S.pan_nb, p, S.pan_p, S.pan_c, tab,
-                                         S.n_vals, S.ezz, S.lid, nrm, n, reinterpret_cast<const CT*>(S.ubuf.ptr),
-                                         reinterpret_cast<CT*>(w));
-  return cudaGetLastError();
-}
-
 int64_t gcd64(int64_t a, int64_t b) {
   while (b) {
     const int64_t t = a % b;
@@ -677,13 +442,9 @@ int64_t gcd64(int64_t a, int64_t b) {
 }  // namespace
 
 void free_targets(Sector& S) {
-  void* ptrs[] = {S.row_ptr, S.col, S.vid, S.ezz, S.vtab64, S.vtab32, S.ubuf.ptr, S.pan_ent, S.pan_vid, S.pan_off};
+  void* ptrs[] = {S.row_ptr, S.col, S.vid, S.ezz, S.vtab64, S.vtab32, S.ubuf.ptr};
   for (void* p : ptrs)
     if (p) cudaFree(p);
-  S.pan_ent = nullptr;
-  S.pan_vid = nullptr;
-  S.pan_off = nullptr;
-  S.pan_p = 0;
   S.row_ptr = nullptr;
   S.col = nullptr;
   S.vid = nullptr;
@@ -700,92 +461,6 @@ void free_targets(Sector& S) {
 
 // Returns EDG_OK, or a reason (EDG_ERR_NOMEM / EDG_ERR_UNSUPPORTED) with the
 // sector left on the matrix-free kernels.
-// Regroup the stored rows into column panels (see k_hv_pan).  n_panels <= 0
-// picks the smallest count whose panels hold at most 2^23 columns and 64 MB
-// of complex64 u.  The row arrays are freed afterwards.
-int pack_panels(Sector& S, int n_panels, std::string& err) {
-  if (S.pan_ent) return EDG_OK;
-  if (!S.col) {
-    err = "pack_panels needs stored rows (edg_sector_build_targets)";
-    return EDG_ERR_INVALID;
-  }
-  const int64_t n = S.P.n_p;
-  const int64_t by_bits = (n + (1ll << kPanBits) - 1) >> kPanBits;
-  const int64_t by_l2 = (n * 8 + (64ll << 20) - 1) / (64ll << 20);
-  int64_t P = n_panels > 0 ? n_panels : std::max<int64_t>(1, std::max(by_bits, by_l2));
-  P = std::max<int64_t>(P, by_bits);
-  if (P > 1024) {
-    err = "pack_panels: more than 1024 panels";
-    return EDG_ERR_UNSUPPORTED;
-  }
-  const int64_t C = (n + P - 1) / P;
-  const int64_t nb = (n + kPanRows - 1) / kPanRows;
-  const uint64_t nnz = S.P.n_targets;
-  cudaStream_t st = S.stream;
-  uint32_t* counts = nullptr;
-  uint64_t* off = nullptr;
-  unsigned long long *sums = nullptr, *tot = nullptr;
-  uint32_t* ent = nullptr;
-  uint16_t* evid = nullptr;
-  const int64_t nc = P * nb;
-  const int64_t n_chunks = (nc + kChunk - 1) / kChunk;
-  cudaError_t e = cudaMalloc(&counts, sizeof(uint32_t) * std::max<int64_t>(nc, 1));
-  if (e == cudaSuccess) e = cudaMalloc(&off, sizeof(uint64_t) * (nc + 1));
-  if (e == cudaSuccess) e = cudaMalloc(&sums, sizeof(unsigned long long) * std::max<int64_t>(n_chunks, 1));
-  if (e == cudaSuccess) e = cudaMalloc(&tot, sizeof(unsigned long long));
-  if (e == cudaSuccess) e = cudaMalloc(&ent, sizeof(uint32_t) * std::max<uint64_t>(nnz, 1));
-  if (e == cudaSuccess) e = cudaMalloc(&evid, sizeof(uint16_t) * std::max<uint64_t>(nnz, 1));
-  auto cleanup = [&] {
-    void* q[] = {counts, off, sums, tot, ent, evid};
-    for (void* x : q)
-      if (x) cudaFree(x);
-  };
-  if (e != cudaSuccess) {
-    cudaGetLastError();
-    cleanup();
-    err = "pack_panels: the panel arrays do not fit next to the rows";
-    return EDG_ERR_NOMEM;
-  }
-  const size_t hist = sizeof(uint32_t) * kWarpsPerBlock * P;
-  const int g1 = grid_for(k_pan_count, hist, nb * 32, kTgtThreads);
-  k_pan_count<<<g1, kTgtThreads, hist, st>>>(S.row_ptr, S.col, S.pack_cb, n, nb, (int)P, C, counts);
-  k_scan64_chunks<<<(unsigned)n_chunks, kScan, 0, st>>>(counts, nc, sums);
-  k_scan64_sums<<<1, kScan, 0, st>>>(sums, n_chunks, tot);
-  k_scan64_apply<<<(unsigned)n_chunks, kScan, 0, st>>>(counts, nc, sums, tot, off);
-  const int g2 = grid_for(k_pan_scatter, hist, nb * 32, kTgtThreads);
-  k_pan_scatter<<<g2, kTgtThreads, hist, st>>>(S.row_ptr, S.col, S.vid, S.pack_cb, n, nb, (int)P, C, off, ent,
-                                                evid);
-  unsigned long long total = 0;
-  e = cudaMemcpyAsync(&total, tot, sizeof(total), cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-  if (e != cudaSuccess || total != nnz) {
-    cleanup();
-    err = e != cudaSuccess ? std::string("pack_panels: ") + cudaGetErrorString(e) : "pack_panels: entry count mismatch";
-    return e != cudaSuccess ? EDG_ERR_CUDA : EDG_ERR_INVALID;
-  }
-  cudaFree(counts);
-  cudaFree(sums);
-  cudaFree(tot);
-  cudaFree(S.row_ptr);
-  cudaFree(S.col);
-  cudaFree(S.vid);
-  const size_t entry = S.pack_cb ? 4 : 6;
-  S.row_ptr = nullptr;
-  S.col = nullptr;
-  S.vid = nullptr;
-  S.pack_cb = 0;
-  S.pan_ent = ent;
-  S.pan_vid = evid;
-  S.pan_off = off;
-  S.pan_p = (int)P;
-  S.pan_c = C;
-  S.pan_nb = nb;
-  const size_t before = S.targets_bytes;
-  S.targets_bytes = nnz * 6 + sizeof(uint64_t) * (nc + 1) + (before - (size_t)nnz * entry - sizeof(uint64_t) * (n + 1));
-  S.device_bytes += S.targets_bytes - before;
-  return EDG_OK;
-}
-
 int build_targets(Sector& S, int64_t max_bytes, std::string& err) {
   SectorParams& P = S.P;
   if (S.col) return EDG_OK;
@@ -1076,7 +751,6 @@ cudaError_t launch_hv_rows(const Sector& S, const void* v, void* w, bool fp64, i
 }
 
 cudaError_t launch_hv_stored(const Sector& S, const void* v, void* w, bool fp64, cudaStream_t st) {
-  if (S.pan_ent) return fp64 ? launch_pan_t<double>(S, v, w, st) : launch_pan_t<float>(S, v, w, st);
   return fp64 ? launch_csr_t<double>(S, v, w, st) : launch_csr_t<float>(S, v, w, st);
 }
 

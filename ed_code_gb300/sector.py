@@ -88,11 +88,6 @@ class GpuSector:
                                             int(pipelined)))
         self.refresh_info()
 
-    def pack_panels(self, n_panels: int = 0) -> None:
-        """Regroup the stored rows into column panels (edg_sector_pack_panels)."""
-        N.check(N.lib().edg_sector_pack_panels(self._h, int(n_panels)))
-        self.refresh_info()
-
     def free_targets(self) -> None:
         N.check(N.lib().edg_sector_free_targets(self._h))
         self.refresh_info()

@@ -17,7 +17,7 @@
 extern "C" {
 #endif
 
-#define EDGPU_ABI_VERSION 5
+#define EDGPU_ABI_VERSION 6
 
 enum {
   EDG_OK = 0,
@@ -69,7 +69,6 @@ typedef struct {
   int64_t n_targets;     /* stored nonzeros (0: H*v searches on the fly) */
   int lanes_per_row;     /* stored-row H*v: lanes of a warp per row (edg_sector_tune) */
   int cache_policy;      /* stored-row H*v: 1 streaming row loads, 2 L2 evict-first row loads */
-  int panels;            /* column panels of the stored rows (0: row order) */
   int L3, kz;            /* third translation's cycle length and momentum (1, 0 in 2-D) */
   int entry_bytes;       /* bytes of one stored nonzero: 4 (column and value id packed in one
                             u32), 6 (u32 column + u16 value id), 0 without stored rows */
@@ -148,17 +147,6 @@ int edg_sector_tune(edg_sector* s, int lanes_per_row, int* chosen, double* ms);
  * cache_policy 1 or 2, ctas_per_sm 0 (as many as fit) to 32, pipelined 0 or
  * 1.  Results do not depend on them, bit for bit; only the speed does. */
 int edg_sector_set_rows(edg_sector* s, int lanes_per_row, int cache_policy, int ctas_per_sm, int pipelined);
-
-/* Regroup the stored rows into column panels: rows in blocks of 64, columns
- * in n_panels slices (<= 0: enough for each slice of u to fit in 64 MB of L2
- * at complex64), entries stored per (block, panel), in row order.  edg_hv
- * then makes one pass per panel, gathering from one L2-resident slice of u
- * and adding the row sums into w.  Same bytes per nonzero as the rows; the
- * row arrays are freed.  Measured slower than the tuned row kernel at 32 and
- * 36 sites (a panel holds ~2 entries per row, so the per-entry segmented
- * reduction and the per-panel pass over w outweigh the L2 hits); kept as an
- * option.  Batch segments and edg_hv_noalloc need the row form. */
-int edg_sector_pack_panels(edg_sector* s, int n_panels);
 
 /* Same with host buffers: copies v in, applies H, returns w, synchronises.
  * When w is page-locked memory the device can address (cudaHostAlloc,
@@ -308,15 +296,6 @@ int edg_batch_timers(const edg_batch* b, double* seconds);
 /* Deterministic complex test vector (splitmix64, entries uniform in [-1,1)^2)
  * written to device memory; the same generator as the test suite's. */
 int edg_fill_random(void* dst, int64_t n, int dtype, uint64_t seed, void* stream);
-
-/* Measurement helper, no counterpart in the reference: `count` loads of single
- * entries (EDG_C64: 8 bytes, EDG_C128: 16 bytes) from the device vector u of n
- * entries at hashed random positions, enqueued on `stream`; time it with
- * events.  hint 0: plain loads; 1: with the L2 evict_last policy of the H*v's
- * gathers.  This bounds the stored-row H*v's far gathers.  *out (device
- * memory) is written only if the loaded sum is NaN. */
-int edg_probe_gather(const void* u, int64_t n, int dtype, int hint, int64_t count, uint64_t seed, float* out,
-                     void* stream);
 
 #ifdef __cplusplus
 }

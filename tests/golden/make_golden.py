@@ -1,7 +1,7 @@
 """Generate the golden fixtures from the reference itself.
 
 Runs in a container where the reference sources are present: builds the
-reference (``make -C oracle ref``: ED2 plus the table/sHv dump harness,
+reference (``make -C oracle ref REF_SRC=...``: ED2 plus the table/sHv dump harness,
 compiled from the read-only sources), writes one reference input file per
 case with ``ed_code_gb300.lattice``, and records what the reference prints or
 dumps:
@@ -181,7 +181,14 @@ def run_case(name: str, workdir: str) -> dict:
 
 def main(argv):
     names = argv or list(CASES)
-    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True, stdout=subprocess.DEVNULL)
+    sys.path.insert(0, ROOT)
+    import __graft_entry__ as G
+
+    ref = G.reference_src()
+    if not ref:
+        raise SystemExit("the reference sources are not mounted (set EDG_REFERENCE_SRC to its src/ directory)")
+    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF_SRC={ref}"], check=True,
+                   stdout=subprocess.DEVNULL)
     cases_path = os.path.join(HERE, "cases.json")
     allmeta = json.load(open(cases_path)) if os.path.exists(cases_path) else {}
     with tempfile.TemporaryDirectory() as tmp:

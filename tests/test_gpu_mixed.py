@@ -82,16 +82,6 @@ def test_mixed_eigenvectors(gpu, monkeypatch, reorth, keep):
         assert np.linalg.norm(r) <= 2 * out["residuals"][k] + 1e-12
 
 
-@pytest.mark.parametrize("reorth", [1, 0])
-def test_mixed_with_column_panels(gpu, reorth):
-    sec = gpu.GpuSector(golden_model("sq6x4_k00", 0))
-    ref = np.array(golden_cases()["sq6x4_k00"]["sectors"][0]["ed2_eigs"][:2])
-    assert sec.build_targets()
-    sec.pack_panels(6)
-    out = sec.solve_mixed(n_ev=2, iterations=300, reorth_every=reorth)
-    assert np.max(np.abs(out["eigs"][:2] - ref) / np.abs(ref)) <= 1e-9
-
-
 def test_mixed_with_stored_targets(gpu):
     sec = gpu.GpuSector(golden_model("tri6x4_k10", 0))
     ref = np.array(golden_cases()["tri6x4_k10"]["sectors"][0]["ed2_eigs"][:2])

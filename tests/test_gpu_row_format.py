@@ -3,8 +3,8 @@
 build_targets deduplicates the value table and packs each nonzero into one
 u32 (column below, value id above) when both fit, else keeps a u32 column
 array and a u16 value-id array.  EDG_ROW_FORMAT=split forces the second
-format.  Both read the same table values in the same order, so H*v, the batch
-and column panels must agree bit for bit, and each must still match the
+format.  Both read the same table values in the same order, so H*v and the
+batch must agree bit for bit, and each must still match the
 reference (the golden fixtures) within the H*v tolerances.
 """
 import numpy as np
@@ -109,18 +109,3 @@ def test_batch_mixes_formats(mods, monkeypatch):
     assert np.array_equal(res[0]["residuals"], res[1]["residuals"])
     ref = golden_cases()["tri6x4_k10"]["sectors"][0]["ed2_eigs"][0]
     assert abs(res[0]["eigs"][0] - ref) <= 1e-9 * abs(ref)
-
-
-@pytest.mark.parametrize("panels", [1, 3])
-def test_panels_from_either_format(mods, monkeypatch, panels):
-    _, L, sector = mods
-    model = _models(L)[3]
-    packed, split = _pair(sector, model, monkeypatch)
-    v = O.splitmix_vector(packed.n_p, 9)
-    w0 = packed.sHv(v)
-    packed.pack_panels(panels)
-    split.pack_panels(panels)
-    assert packed.info["panels"] == split.info["panels"] == panels
-    a, b = packed.sHv(v), split.sHv(v)
-    assert np.array_equal(a, b)
-    assert np.abs(a - w0).max() <= FP64_TOL * max(1.0, np.abs(w0).max())
