@@ -40,7 +40,6 @@
 #include <cstddef>
 #include <cstring>
 #include <string>
-#include <thread>
 #include <vector>
 
 #include "../../include/edgpu.h"
@@ -505,6 +504,9 @@ struct Batch {
   cudaGraphExec_t graph = nullptr;
   int64_t device_bytes = 0, steps = 0;
   MixedFinish fin;
+  TdScratch td;                // device Ritz selection of the stopped segments
+  double* ybuf = nullptr;      // their Ritz coefficients
+  size_t ybuf_n = 0;
   // host seconds: add, step (graph replays and waits), finish (T, Ritz
   // vectors, Rayleigh quotients), release, rebuild (tables and graph capture)
   double timers[5] = {0, 0, 0, 0, 0};
@@ -518,6 +520,7 @@ struct Batch {
     cudaFree(d_tiles);
     cudaFree(d_tb);
     cudaFree(d_part);
+    cudaFree(ybuf);
     if (st) cudaStreamDestroy(st);
   }
 };
@@ -542,23 +545,9 @@ cudaError_t pull_state(Batch& B) {
 using Clock = std::chrono::steady_clock;
 double since(Clock::time_point t0) { return std::chrono::duration<double>(Clock::now() - t0).count(); }
 
-template <class F>
-void parallel_for(int n, F f) {
-  const int nt = std::max(1, std::min<int>(n, (int)std::thread::hardware_concurrency()));
-  if (nt <= 1) {
-    for (int i = 0; i < n; ++i) f(i);
-    return;
-  }
-  std::vector<std::thread> th;
-  for (int t = 0; t < nt; ++t)
-    th.emplace_back([&, t] {
-      for (int i = t; i < n; i += nt) f(i);
-    });
-  for (auto& x : th) x.join();
-}
-
-// Finish every stopped segment: its alpha/beta come back in one wait, the
-// Ritz selection of T runs on host threads, then each segment's FP64 Ritz
+// Finish every stopped segment: the Ritz selection of every stopped
+// segment's T runs on the device in one batched launch (tridiag_dev.cu) and
+// its kept values come back in one wait, then each segment's FP64 Ritz
 // vectors and Rayleigh quotients are queued and read back in one more wait.
 void finish_stopped(Batch& B) {
   const auto tf = Clock::now();
@@ -567,36 +556,65 @@ void finish_stopped(Batch& B) {
     if (B.segs[k].st.status != kRunning) idx.push_back((int)k);
   if (idx.empty()) return;
   const int ns = (int)idx.size();
-  std::vector<std::vector<double>> ah(ns), bh(ns);
+  std::vector<int> status(ns, EDG_OK);
+  std::vector<TdProb> probs(ns);
+  std::vector<size_t> y_at(ns, 0);
+  int tm_max = 1, nv_max = 1, want_max = 1;
+  size_t y_total = 0;
   for (int i = 0; i < ns; ++i) {
     const Segment& g = B.segs[idx[i]];
-    ah[i].resize(g.st.j);
-    bh[i].resize(g.st.j + 1);
-    cudaMemcpyAsync(ah[i].data(), g.d.alpha, sizeof(double) * g.st.j, cudaMemcpyDeviceToHost, B.st);
-    cudaMemcpyAsync(bh[i].data(), g.d.beta, sizeof(double) * (g.st.j + 1), cudaMemcpyDeviceToHost, B.st);
+    const int m = g.st.j;
+    if (m < 1) {
+      status[i] = fail(EDG_ERR_INVALID, "batch: a segment stopped before its first step");
+      continue;
+    }
+    const int n_try = std::min(kMaxEv, std::min(g.req.n_ev + 4, m));
+    const int nc = std::min(m, std::max(2 * n_try + 8, n_try)), nh = std::max(0, std::min(m - 1, nc + 2));
+    probs[i] = TdProb{g.d.alpha, 1, g.d.beta, m, nc, nh, n_try, 1, nullptr, nullptr, nullptr};
+    y_at[i] = y_total;
+    y_total += (size_t)n_try * m;
+    tm_max = std::max(tm_max, m);
+    nv_max = std::max(nv_max, nc + nh);
+    want_max = std::max(want_max, n_try);
   }
-  std::vector<int> status(ns, EDG_OK);
-  cudaError_t e = cudaStreamSynchronize(B.st);
-  if (e != cudaSuccess) std::fill(status.begin(), status.end(), cuda_fail(e, "batch: T"));
-  std::vector<RitzSel> sel(ns);
-  parallel_for(ns, [&](int i) {
-    const Segment& g = B.segs[idx[i]];
-    const int m = g.st.j, n_try = std::min(kMaxEv, std::min(g.req.n_ev + 4, m));
-    if (status[i] == EDG_OK) ritz_select(ah[i].data(), bh[i].data(), m, n_try, 2 * n_try + 8, sel[i]);
-  });
+  std::vector<TdOut> sel(ns);
+  cudaError_t e = B.td.reserve(ns, tm_max, nv_max, want_max);
+  if (e == cudaSuccess && y_total > B.ybuf_n) {
+    cudaFree(B.ybuf);
+    B.ybuf = nullptr;
+    B.ybuf_n = 0;
+    if ((e = cudaMalloc(&B.ybuf, sizeof(double) * y_total)) == cudaSuccess) B.ybuf_n = y_total;
+  }
+  if (e == cudaSuccess) {
+    for (int i = 0; i < ns; ++i) {
+      probs[i].vals = B.td.vals + (size_t)i * nv_max;
+      probs[i].y = B.ybuf + y_at[i];
+      probs[i].work = B.td.work + (size_t)i * 5 * tm_max * want_max;
+      if (status[i] != EDG_OK) probs[i].m = 0, probs[i].nc = probs[i].nh = probs[i].want = 0;
+    }
+    e = cudaMemcpyAsync(B.td.probs, probs.data(), sizeof(TdProb) * ns, cudaMemcpyHostToDevice, B.st);
+    if (e == cudaSuccess) e = td_select_async(B.td.probs, ns, tm_max, nv_max, B.td.out, true, B.st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(sel.data(), B.td.out, sizeof(TdOut) * ns, cudaMemcpyDeviceToHost, B.st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(B.st);
+  }
+  if (e != cudaSuccess) {
+    const int rc = cuda_fail(e, "batch: Ritz selection");
+    for (int& s : status)
+      if (s == EDG_OK) s = rc;
+  }
   int64_t n_max = 1, x_max = 1;
   int m_max = 1, total = 0;
   std::vector<int> off(ns, 0);
   for (int i = 0; i < ns; ++i) {
     const Segment& g = B.segs[idx[i]];
-    const int na = (int)sel[i].acc.size();
+    const int na = status[i] == EDG_OK ? sel[i].na : 0;
     if (status[i] == EDG_OK && na == 0)
       status[i] = fail(EDG_ERR_NOT_CONVERGED, "batch: no Ritz value survived the copy test");
     n_max = std::max(n_max, g.d.n);
     x_max = std::max(x_max, g.d.n * na);
     m_max = std::max(m_max, g.st.j);
     off[i] = total;
-    total += na;
+    total += status[i] == EDG_OK ? na : 0;
   }
   if (B.fin.reserve(n_max, m_max, total) != cudaSuccess || B.fin.reserve_x(x_max, 1) != cudaSuccess) {
     cudaGetLastError();
@@ -606,9 +624,8 @@ void finish_stopped(Batch& B) {
   for (int i = 0; i < ns; ++i) {
     if (status[i] != EDG_OK) continue;
     Segment& g = B.segs[idx[i]];
-    const int m = g.st.j, na = (int)sel[i].acc.size();
-    cudaMemcpyAsync(B.fin.y, sel[i].y.data(), sizeof(double) * na * m, cudaMemcpyHostToDevice, B.st);
-    status[i] = B.fin.ritz_stored(B.st, g.d.V, g.d.n, m, na, m);
+    const int m = g.st.j, na = sel[i].na;
+    status[i] = B.fin.ritz_stored(B.st, g.d.V, g.d.n, m, na, m, B.ybuf + y_at[i]);
     if (status[i] == EDG_OK && (e = B.fin.rayleigh_async(g.sec->s, B.st, g.d.n, na, B.fin.res + 4 * off[i])) != cudaSuccess)
       status[i] = cuda_fail(e, "batch: FP64 H*v");
   }
@@ -626,10 +643,12 @@ void finish_stopped(Batch& B) {
     r.converged = g.st.status == kConverged;
     r.status = status[i];
     if (status[i] == EDG_OK) {
-      const int na = (int)sel[i].acc.size();
+      const int na = sel[i].na;
       std::vector<double> ri(rr.begin() + 4 * off[i], rr.begin() + 4 * (off[i] + na));
-      std::vector<int> keep;
-      pick_levels(ri, sel[i].theta, sel[i].acc, na, g.req.n_ev, r.eigs, r.ritz, r.residuals, keep);
+      std::vector<double> th(sel[i].theta, sel[i].theta + na);
+      std::vector<int> acc(na), keep;
+      for (int q = 0; q < na; ++q) acc[q] = q;
+      pick_levels(ri, th, acc, na, g.req.n_ev, r.eigs, r.ritz, r.residuals, keep);
       r.n_found = (int)keep.size();
     }
     B.done.push_back(r);

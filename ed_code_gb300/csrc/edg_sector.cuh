@@ -128,8 +128,10 @@ struct MixedFinish {
   cudaError_t reserve(int64_t n, int m, int n_res);
   cudaError_t reserve_x(int64_t n, int na);
   // X_q = sum_{j < cnt} y_q[j] V_j from the first cnt stored FP32 vectors
-  // (y_q holds m coefficients; the vectors' leading dimension is n)
-  int ritz_stored(cudaStream_t st, const float2* V, int64_t n, int m, int na, int cnt);
+  // (y_q holds m coefficients, from ycoef or else this object's y; the
+  // vectors' leading dimension is n)
+  int ritz_stored(cudaStream_t st, const float2* V, int64_t n, int m, int na, int cnt,
+                  const double* ycoef = nullptr);
   // res[4q..4q+3] = |x_q|^2, <x_q|H x_q>, Rayleigh quotient, residual, queued
   // on st (no wait)
   cudaError_t rayleigh_async(Sector& S, cudaStream_t st, int64_t n, int na, double* res_dev);

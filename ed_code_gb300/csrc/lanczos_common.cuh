@@ -1,10 +1,7 @@
-// Ritz selection shared by the single-sector and batched mixed-precision
-// solvers, run on the host: T is at most a few hundred rows, and GB300's FP64
-// rate makes a one-CTA bisection slower than one host core.
+// Ritz selection of the Lanczos T matrix on the device (tridiag_dev.cu),
+// shared by the single-sector solvers and the batch.
 #pragma once
-#include <algorithm>
-#include <cmath>
-#include <vector>
+#include <cuda_runtime.h>
 
 #include "tridiag.cuh"
 
@@ -13,51 +10,43 @@ namespace edg {
 constexpr int kMaxEv = 32;             // Ritz pairs returned
 constexpr int kCand = 2 * kMaxEv + 8;  // eigenvalues of T examined when copies are many
 
-struct RitzSel {
-  std::vector<double> theta;  // lowest eigenvalues of T, ascending
-  std::vector<int> acc;       // indices into theta of the accepted Ritz values
-  std::vector<double> y;      // acc.size() x m: their eigenvectors of T
+// One tridiagonal problem for the device kernels (tridiag_dev.cu).  T has
+// diagonal alpha[i * astride] (the real part when alpha is complex, astride 2)
+// and off-diagonal beta[1..m-1].  vals receives the nc lowest eigenvalues of T
+// then the nh lowest of T-hat; y the eigenvectors of the kept ones (m each);
+// work holds 5 m doubles per kept vector.
+struct TdProb {
+  const double* alpha;
+  int astride;
+  const double* beta;
+  int m;
+  int nc, nh, want, filter;  // filter 1: Cullum-Willoughby copy test; 0: the lowest `want`
+  double* vals;
+  double* y;
+  double* work;
 };
-
-// Lowest n_cand eigenvalues of T (diag alpha[0..m-1], off-diagonal
-// beta[1..m-1]) and of T-hat (first row and column removed); the first `want`
-// that pass the copy test, with their eigenvectors.  Without
-// reorthogonalisation FP32 vectors make many copies of each converged level,
-// so n_cand must leave room for them (kCand); with full reorthogonalisation
-// 2 want + 8 is plenty.
-inline void ritz_select(const double* alpha, const double* beta, int m, int want, int n_cand, RitzSel& out) {
-  std::vector<double> d(alpha, alpha + m), e(m, 0.0);
-  for (int i = 1; i < m; ++i) e[i] = beta[i];
-  const int nc = std::min(m, std::max(n_cand, want)), nh = std::min(m - 1, nc + 2);
-  out.theta.resize(nc);
-  std::vector<double> hat(std::max(nh, 0));
-  for (int k = 0; k < nc; ++k) out.theta[k] = tridiag_eigenvalue(d.data(), e.data(), m, k);
-  for (int k = 0; k < nh; ++k) hat[k] = tridiag_eigenvalue(d.data() + 1, e.data() + 1, m - 1, k);
-  // Cullum-Willoughby: a simple eigenvalue of T that T-hat also has is a copy
-  // made by lost orthogonality.  Copies of a converged level built from FP32
-  // vectors agree only to about the FP32 backward error, ~1e-7 |T|; T and
-  // T-hat share a spurious value to FP64 accuracy.
-  double scale = 0;
-  for (int i = 0; i < m; ++i) scale = std::max(scale, std::fabs(d[i]) + std::fabs(e[i]) + (i + 1 < m ? std::fabs(e[i + 1]) : 0.0));
-  scale = std::max(scale, 1.0);
-  const double tol_cluster = 1e-7 * scale, tol_hat = 1e-10 * scale;
-  out.acc.clear();
-  const std::vector<double>& th = out.theta;
-  for (int k = 0; k < nc && (int)out.acc.size() < want; ++k) {
-    const bool prev_close = k > 0 && std::fabs(th[k] - th[k - 1]) < tol_cluster;
-    const bool next_close = k + 1 < nc && std::fabs(th[k + 1] - th[k]) < tol_cluster;
-    bool in_hat = false;
-    for (int q = 0; q < nh; ++q)
-      if (std::fabs(hat[q] - th[k]) < tol_hat) in_hat = true;
-    if (in_hat && !prev_close && !next_close) continue;  // spurious copy
-    if (prev_close) continue;                            // keep one per cluster
-    out.acc.push_back(k);
-  }
-  const int na = (int)out.acc.size();
-  out.y.assign((size_t)na * m, 0.0);
-  std::vector<double> work(5 * (size_t)m);
-  for (int q = 0; q < na; ++q)
-    tridiag_eigenvector(d.data(), e.data(), m, th[out.acc[q]], out.y.data() + (size_t)q * m, work.data());
-}
+struct TdOut {
+  int na;                 // Ritz values kept (<= want)
+  int acc[kMaxEv];        // their indices among the nc eigenvalues of T
+  double theta[kMaxEv];   // their values
+};
+// Device scratch of the selection, grown on demand.
+struct TdScratch {
+  TdProb* probs = nullptr;
+  TdOut* out = nullptr;
+  double* vals = nullptr;
+  double* work = nullptr;
+  size_t probs_b = 0, out_b = 0, vals_b = 0, work_b = 0;
+  ~TdScratch();
+  cudaError_t reserve(int n_probs, int m_max, int nvals_max, int want_max);
+};
+// Queue the selection of n_probs problems (device table probs_dev) on st:
+// eigenvalues, kept values into out_dev, and their eigenvectors when asked.
+cudaError_t td_select_async(const TdProb* probs_dev, int n_probs, int m_max, int nvals_max, TdOut* out_dev,
+                            bool vectors, cudaStream_t st);
+// ritz_select on the device for one T held in device memory: the kept Ritz
+// values in sel, their eigenvectors (want x m) in y_dev.  Waits for the result.
+int ritz_select_device(const double* alpha, const double* beta, int m, int want, int n_cand, double* y_dev,
+                       cudaStream_t st, TdOut& sel);
 
 }  // namespace edg

@@ -16,9 +16,10 @@
 //    else as many as fit (the 36-site case: 2 GB each) and the later ones in
 //    a ring of up to eight;
 //  * T's lowest eigenvalues by bisection and their eigenvectors by inverse
-//    iteration, in FP64 on the host (lanczos_common.cuh); Ritz values that
-//    T shares with T-without-its-first-row are copies produced by lost
-//    orthogonality and are dropped (Cullum and Willoughby's test);
+//    iteration, in FP64 on the device (tridiag_dev.cu), T read where the
+//    recurrence wrote it; Ritz values that T shares with
+//    T-without-its-first-row are copies produced by lost orthogonality and
+//    are dropped (Cullum and Willoughby's test);
 //  * Ritz vectors in FP64 -- from the stored vectors, plus, when only the
 //    first k were stored, a re-run of the recurrence from v_{k-1} with the
 //    same alpha/beta for the later ones;
@@ -438,7 +439,9 @@ cudaError_t MixedFinish::reserve_x(int64_t n, int na) {
   return grow((void**)&X, sizeof(double2) * n * na, x_bytes);
 }
 
-int MixedFinish::ritz_stored(cudaStream_t st, const float2* V, int64_t n, int m, int na, int cnt) {
+int MixedFinish::ritz_stored(cudaStream_t st, const float2* V, int64_t n, int m, int na, int cnt,
+                             const double* ycoef) {
+  const double* yc = ycoef ? ycoef : y;
   // the coefficients of up to kRitzChunk Ritz vectors sit in shared memory:
   // 64 bytes a Krylov vector, past the default 48 KB above 768 vectors
   // (the solvers cap the steps at 2000, i.e. 128 KB, within the opt-in limit)
@@ -455,7 +458,7 @@ int MixedFinish::ritz_stored(cudaStream_t st, const float2* V, int64_t n, int m,
   }
   for (int q0 = 0; q0 < na; q0 += kRitzChunk) {
     const int qn = std::min(kRitzChunk, na - q0);
-    k_ritz_vectors<<<grid_n(n), 256, sizeof(float2) * qn * cnt, st>>>(X, n, V, n, y, m, cnt, q0, qn);
+    k_ritz_vectors<<<grid_n(n), 256, sizeof(float2) * qn * cnt, st>>>(X, n, V, n, yc, m, cnt, q0, qn);
   }
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? EDG_OK : cuda_fail(e, "mixed Lanczos: Ritz vectors");
@@ -648,25 +651,24 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
     return cudaStreamSynchronize(st);
   };
   if ((e = run(false, nullptr, 0, nullptr)) != cudaSuccess) return cuda_fail(e, "mixed Lanczos");
-  // Ritz values and coefficients of T on the host
+  // Ritz values and coefficients of T, on the device
   MixedFinish F;
   const int n_try = std::min(kMaxEv, std::min(want + 4, m));
   if ((e = F.reserve(n, m, n_try)) != cudaSuccess) return fail(EDG_ERR_NOMEM, "mixed Lanczos: scratch");
-  std::vector<double> ah(m), bh(m + 1);
-  cudaMemcpyAsync(ah.data(), alpha, sizeof(double) * m, cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(bh.data(), beta, sizeof(double) * (m + 1), cudaMemcpyDeviceToHost, st);
-  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "mixed Lanczos: T");
-  RitzSel sel;
-  ritz_select(ah.data(), bh.data(), m, n_try, kCand, sel);
-  const int na = (int)sel.acc.size();
-  const std::vector<int>& acc_h = sel.acc;
-  const std::vector<double>& th = sel.theta;
+  TdOut sel{};
+  int rc = ritz_select_device(alpha, beta, m, n_try, kCand, F.y, st, sel);
+  if (rc != EDG_OK) return rc;
+  const int na = sel.na;
+  std::vector<int> acc_h(na);
+  std::vector<double> th(na);
+  for (int q = 0; q < na; ++q) {
+    acc_h[q] = q;
+    th[q] = sel.theta[q];
+  }
   if (na == 0) return fail(EDG_ERR_NOT_CONVERGED, "mixed Lanczos: no Ritz value survived the copy test");
-  cudaMemcpyAsync(F.y, sel.y.data(), sizeof(double) * na * m, cudaMemcpyHostToDevice, st);
   // Ritz vectors in FP64
   if ((e = F.reserve_x(n, na)) != cudaSuccess) return fail(EDG_ERR_NOMEM, "mixed Lanczos: FP64 Ritz vectors do not fit");
   int passes = 1;
-  int rc = EDG_OK;
   if (store) {
     if ((rc = F.ritz_stored(st, V, n, m, na, m)) != EDG_OK) return rc;
   } else {

@@ -227,7 +227,8 @@ typedef struct {
 
 /* Lowest eigenvalues with FP32 Krylov vectors and FP32 H*v; FP64 for alpha/beta
  * (compensated sums), reorthogonalisation coefficients, the tridiagonal
- * eigensolve (on the host) and one FP64 H*v per Ritz vector.  Copies of
+ * eigensolve (on the device, edg_tridiag_lowest's kernels) and one FP64 H*v
+ * per Ritz vector.  Copies of
  * converged eigenvalues that lost orthogonality produces are removed, so each
  * level is returned once.  eigs: FP64 Rayleigh quotients; ritz: the Ritz
  * values of T; residuals: |Hx - eig x|/|x| in FP64; evecs (NULL allowed):
@@ -292,6 +293,21 @@ int edg_batch_info(const edg_batch* b, int* n_active, int64_t* device_bytes, int
  * replays up to the waits of the convergence tests), finishing segments,
  * releasing their memory, rebuilding the step graph. */
 int edg_batch_timers(const edg_batch* b, double* seconds);
+
+/* The k (1..32) lowest eigenpairs of the real symmetric tridiagonal matrix
+ * with diagonal d[0..m-1] and off-diagonal e[1..m-1] (e[0] unused), m <= 4096,
+ * computed on the current device by the kernels the solvers use for their
+ * Lanczos T (bisection on Sturm counts, inverse iteration, FP64).  With
+ * copy_filter = 0: eigs[0..k-1] ascending, vecs (NULL allowed) k x m,
+ * *n_out = k.  With copy_filter = 1: the Ritz values the mixed-precision
+ * solvers keep -- among the lowest 72, a simple eigenvalue that the matrix
+ * without its first row and column shares is dropped as a copy made by lost
+ * orthogonality, and one value is kept per cluster -- at most k of them,
+ * *n_out of them returned.
+ * Replaces: zMatrix_Diagonalize_Hermitian -> zheev on T (lanczos.cpp:271-286,
+ * Matrix_Functions.cpp:28-48). */
+int edg_tridiag_lowest(const double* d, const double* e, int m, int k, int copy_filter, double* eigs, double* vecs,
+                       int* n_out);
 
 /* Deterministic complex test vector (splitmix64, entries uniform in [-1,1)^2)
  * written to device memory; the same generator as the test suite's. */

@@ -20,9 +20,15 @@
 // (read_input_file.cpp:443) and goes through the 3-D pConstruct_States
 // (Momentum_Basis.cpp:781) and sHv (H_v.cpp:360); meta.txt then ends with L3 kz.
 //
-// usage: ref_harness <input-file> <out-dir> [tables|notables] [nvec] [reps]
+//   T.f64             Lanczos T matrix of m steps from vT.c128         [if tsteps > 0]
+//                     (alpha as m complex pairs, then beta_0..beta_m)
+//
+// usage: ref_harness <input-file> <out-dir> [tables|notables] [nvec] [reps] [tsteps]
 // The v<k>.c128 inputs are read from <out-dir>.  With reps > 1 each sHv call
 // is repeated and the mean wall time per call is written to hv_time.txt.
+// With tsteps > 0 the reference's three-term recurrence of its first Lanczos
+// cycle (lanczos.cpp:196-254: reference sHv, zdotc, zaxpyk, zscalk, normalize;
+// no reorthogonalisation) runs tsteps steps from vT.c128 and T is dumped.
 #include <sys/stat.h>
 
 #include <cstdio>
@@ -35,6 +41,14 @@
 #include "Lanczos_sector.h"
 #include "Momentum_Basis.h"
 #include "read_input_file.h"
+
+// The reference's BLAS-1 helpers (lanczos.cpp:8-55), linked from lanczos.o.
+std::complex<double> zdotc(const int64_t& size, const std::vector<std::complex<double>>& v1,
+                           const std::vector<std::complex<double>>& v2);
+void zaxpyk(const int64_t size, std::complex<double> a, std::vector<std::complex<double>>& x,
+            std::vector<std::complex<double>>& y);
+void zscalk(const int64_t size, std::complex<double> a, std::vector<std::complex<double>>& x);
+void normalize(std::vector<std::complex<double>>& v);
 
 template <class T>
 static void dump(const std::string& path, const std::vector<T>& a) {
@@ -60,6 +74,7 @@ int main(int argc, char** argv) {
   bool tables = argc < 4 || std::string(argv[3]) == "tables";
   int nvec = argc > 4 ? std::atoi(argv[4]) : 0;
   int reps = argc > 5 ? std::atoi(argv[5]) : 1;
+  int tsteps = argc > 6 ? std::atoi(argv[6]) : 0;
   mkdir(out.c_str(), 0755);
   std::ofstream log((out + "/ref_log.txt").c_str());
 
@@ -151,6 +166,33 @@ int main(int argc, char** argv) {
     FILE* t = std::fopen((out + "/hv_time.txt").c_str(), "w");
     std::fprintf(t, "%.9f %d\n", t_hv / calls, calls);
     std::fclose(t);
+  }
+  std::vector<std::complex<double>> vp;
+  if (tsteps > 0 && !three_d && read_vec(out + "/vT.c128", vp, n_p)) {
+    const int64_t size = n_p;
+    std::vector<std::complex<double>> w(size, 0.0);
+    std::vector<std::vector<std::complex<double>>> vs;
+    std::vector<double> T;  // alpha (re, im) x m, then beta_0 .. beta_m
+    std::vector<double> betas(1, 0.0);
+    double beta = 0.0;
+    normalize(vp);
+    for (int it = 0; it < tsteps && it < size; ++it) {
+      sHv(&*vp.begin(), &*w.begin(), states, norm, norm_inv, rep_loc, state_ph, Jz, adj, Ch, chl, ChCh, chch, n_spins,
+          Ia, Ib, bits_right, T1, T2, px, py, log);
+      if (it != 0) zaxpyk(size, -beta, vs[it - 1], w);
+      const std::complex<double> alpha = std::conj(zdotc(size, w, vp));
+      T.push_back(alpha.real());
+      T.push_back(alpha.imag());
+      zaxpyk(size, -alpha, vp, w);
+      vs.push_back(vp);
+      beta = std::sqrt(std::real(zdotc(size, w, w)));
+      vp = w;
+      zscalk(size, 1.0 / beta, vp);
+      betas.push_back(beta);
+      zscalk(size, 0.0, w);
+    }
+    T.insert(T.end(), betas.begin(), betas.end());
+    dump(out + "/T.f64", T);
   }
   return 0;
 }
