@@ -16,7 +16,7 @@ LIB_PATH = os.path.join(HERE, "libedgpu.so")
 EDG_OK = 0
 EDG_ERR = {
     1: "EDG_ERR_INVALID", 2: "EDG_ERR_MOMENTUM", 3: "EDG_ERR_EMPTY", 4: "EDG_ERR_CUDA", 5: "EDG_ERR_NOMEM",
-    6: "EDG_ERR_UNSUPPORTED", 7: "EDG_ERR_NOT_CONVERGED",
+    6: "EDG_ERR_UNSUPPORTED", 7: "EDG_ERR_NOT_CONVERGED", 8: "EDG_ERR_CANCELLED",
 }
 EDG_C128 = 0
 EDG_C64 = 1
@@ -93,7 +93,7 @@ class edg_solver_stats(C.Structure):
 
 class edg_mixed_opts(C.Structure):
     _fields_ = [("n_ev", C.c_int), ("iterations", C.c_int), ("reorth_every", C.c_int), ("seed", C.c_uint64),
-                ("want_vectors", C.c_int)]
+                ("want_vectors", C.c_int), ("fp64_vectors", C.c_int)]
 
 
 class edg_mixed_stats(C.Structure):
@@ -123,6 +123,7 @@ SIGNATURES = {
     "edg_batch_step": (C.c_int, [C.c_void_p, C.c_int]),
     "edg_batch_poll": (C.c_int, [C.c_void_p, C.POINTER(edg_batch_result), C.c_int, C.POINTER(C.c_int)]),
     "edg_batch_timers": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "edg_batch_cancel": (C.c_int, [C.c_void_p, C.c_int64]),
     "edg_batch_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "edg_hv_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "edg_count_offdiag": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),

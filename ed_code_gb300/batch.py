@@ -50,6 +50,11 @@ class BatchSolver:
     def step(self, n_steps: int = 1) -> None:
         N.check(N.lib().edg_batch_step(self._h, int(n_steps)))
 
+    def cancel(self, tag: int) -> None:
+        """Withdraw a live segment (edg_batch_cancel); its result comes back
+        from poll() with status EDG_ERR_CANCELLED."""
+        N.check(N.lib().edg_batch_cancel(self._h, int(tag)))
+
     def poll(self) -> List[dict]:
         out = []
         buf = (N.edg_batch_result * 64)()

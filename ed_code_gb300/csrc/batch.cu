@@ -66,7 +66,7 @@ constexpr int kMaxSteps = 511;  // Krylov vectors per segment: kMaxSteps + 1
 constexpr int kCgsY = 8;        // CTAs per tile over the Krylov index k
 constexpr int kBatchMaxEv = 32;
 
-enum { kRunning = 0, kConverged = 1, kMaxedOut = 2 };
+enum { kRunning = 0, kConverged = 1, kMaxedOut = 2, kCancelled = 3 };
 
 struct SegDev {
   const uint64_t* row_ptr;
@@ -93,7 +93,7 @@ struct SegDev {
 
 struct SegState {
   int j;       // steps taken
-  int status;  // kRunning, kConverged, kMaxedOut
+  int status;  // kRunning, kConverged, kMaxedOut, kCancelled (set on the host)
   int redo;    // this step's second Gram-Schmidt pass is needed
   int pad;
 };
@@ -477,6 +477,7 @@ struct Segment {
   SegDev d{};
   SegState st{};
   int64_t bytes = 0;
+  bool cancelled = false;  // edg_batch_cancel: released at the next settle, no result values
 };
 
 void release(Segment& g) {
@@ -538,7 +539,10 @@ cudaError_t pull_state(Batch& B) {
   cudaError_t e = cudaMemcpyAsync(h.data(), B.d_state, sizeof(SegState) * B.n_dev, cudaMemcpyDeviceToHost, B.st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(B.st);
   if (e != cudaSuccess) return e;
-  for (int k = 0; k < B.n_dev; ++k) B.segs[k].st = h[k];
+  for (int k = 0; k < B.n_dev; ++k) {
+    B.segs[k].st = h[k];
+    if (B.segs[k].cancelled) B.segs[k].st.status = kCancelled;
+  }
   return cudaSuccess;
 }
 
@@ -564,6 +568,10 @@ void finish_stopped(Batch& B) {
   for (int i = 0; i < ns; ++i) {
     const Segment& g = B.segs[idx[i]];
     const int m = g.st.j;
+    if (g.cancelled) {
+      status[i] = EDG_ERR_CANCELLED;
+      continue;
+    }
     if (m < 1) {
       status[i] = fail(EDG_ERR_INVALID, "batch: a segment stopped before its first step");
       continue;
@@ -892,6 +900,19 @@ int edg_batch_step(edg_batch* bh, int n_steps) {
   }
   if (rc == EDG_OK) rc = settle(B);
   return rc;
+}
+
+int edg_batch_cancel(edg_batch* bh, int64_t tag) {
+  if (!bh) return fail(EDG_ERR_INVALID, "NULL batch");
+  Batch& B = bh->b;
+  Segment* g = nullptr;
+  for (Segment& x : B.segs)
+    if (x.req.tag == tag && !x.cancelled) g = &x;
+  if (!g) return fail(EDG_ERR_INVALID, "batch: no live segment with tag " + std::to_string(tag));
+  g->cancelled = true;
+  g->st.status = kCancelled;
+  B.dirty = true;
+  return settle(B);
 }
 
 int edg_batch_poll(edg_batch* bh, edg_batch_result* out, int cap, int* n_out) {

@@ -638,9 +638,9 @@ int edg_sector_set_rows(edg_sector* s, int lanes_per_row, int cache_policy, int 
     return fail(EDG_ERR_INVALID, "lanes_per_row must be 8, 16 or 32");
   if (cache_policy != 1 && cache_policy != 2) return fail(EDG_ERR_INVALID, "cache_policy must be 1 or 2");
   if (ctas_per_sm < 0 || ctas_per_sm > 32) return fail(EDG_ERR_INVALID, "ctas_per_sm must be 0 to 32");
+  if (pipelined != 0 && pipelined != 1) return fail(EDG_ERR_INVALID, "pipelined must be 0 or 1");
   s->s.csr_lpr = lanes_per_row;
   s->s.csr_pol = cache_policy;
-  if (pipelined != 0 && pipelined != 1) return fail(EDG_ERR_INVALID, "pipelined must be 0 or 1");
   s->s.csr_cps = ctas_per_sm;
   s->s.csr_pipe = pipelined;
   return EDG_OK;

@@ -132,6 +132,8 @@ struct MixedFinish {
   // vectors' leading dimension is n)
   int ritz_stored(cudaStream_t st, const float2* V, int64_t n, int m, int na, int cnt,
                   const double* ycoef = nullptr);
+  int ritz_stored(cudaStream_t st, const double2* V, int64_t n, int m, int na, int cnt,
+                  const double* ycoef = nullptr);
   // res[4q..4q+3] = |x_q|^2, <x_q|H x_q>, Rayleigh quotient, residual, queued
   // on st (no wait)
   cudaError_t rayleigh_async(Sector& S, cudaStream_t st, int64_t n, int na, double* res_dev);

@@ -50,16 +50,66 @@ int cuda_fail(cudaError_t e, const char* what);
 namespace {
 
 
-// partial sums of sum conj(a) b over FP32 vectors: exact products summed in
-// float-float per thread, FP64 across threads;
-// part[(k*gridDim.x + b)*2 + {0,1}], k = blockIdx.y selects a = V + k*ld
-__global__ void __launch_bounds__(kRedThreads) k_dot32(const float2* __restrict__ V, int64_t ld,
-                                                       const float2* __restrict__ x, int64_t n,
-                                                       double* __restrict__ part) {
-  const float2* a = V + (int64_t)blockIdx.y * ld;
-  FFAcc sr, si;
+// Precision policies of the vector kernels.  Both keep the scalars of the
+// recurrence in FP64 on the device.
+//   P32: FP32 complex vectors; sums of exact products in float-float, the
+//        three-term update with FP64 scalars split into FP32 heads and tails
+//        and rounded once to the FP32 storage (ff.cuh);
+//   P64: FP64 complex vectors and plain FP64 arithmetic (compensated sums),
+//        the same algorithm with nothing reduced -- the FP64 arm that the
+//        FP32 form is compared with.
+__device__ __forceinline__ float fmr(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fmr(double a, double b, double c) { return fma(a, b, c); }
+
+struct DAcc {  // FP64 products into a compensated FP64 sum
+  Acc a;
+  __device__ __forceinline__ void add_prod(double x, double y) { a.add(x * y); }
+  __device__ __forceinline__ void sub_prod(double x, double y) { a.add(-(x * y)); }
+  __device__ __forceinline__ double value() const { return a.value(); }
+};
+struct DScalar {
+  double v;
+  __device__ __forceinline__ explicit DScalar(double x) : v(x) {}
+};
+struct P32 {
+  using V = float2;
+  using Real = float;
+  using A = FFAcc;
+  using S = FFScalar;
+  static constexpr bool kFp64 = false;
+  static __device__ __forceinline__ float axpy2(float x, S a, float u, S b, float w) { return ff_axpy2(x, a, u, b, w); }
+  static __device__ __forceinline__ float scale(float x, S s) { return fmaf(x, s.l, __fmul_rn(x, s.h)); }
+};
+struct P64 {
+  using V = double2;
+  using Real = double;
+  using A = DAcc;
+  using S = DScalar;
+  static constexpr bool kFp64 = true;
+  static __device__ __forceinline__ double axpy2(double x, S a, double u, S b, double w) {
+    return fma(-b.v, w, fma(-a.v, u, x));
+  }
+  static __device__ __forceinline__ double scale(double x, S s) { return x * s.v; }
+};
+template <class P>
+__device__ __forceinline__ typename P::V mk(typename P::Real x, typename P::Real y) {
+  typename P::V r;
+  r.x = x;
+  r.y = y;
+  return r;
+}
+
+// partial sums of sum conj(a) b: exact (P32) or FP64 (P64) products summed per
+// thread, FP64 across threads; part[(k*gridDim.x + b)*2 + {0,1}], k =
+// blockIdx.y selects a = V + k*ld
+template <class P>
+__global__ void __launch_bounds__(kRedThreads) k_dot(const typename P::V* __restrict__ V, int64_t ld,
+                                                     const typename P::V* __restrict__ x, int64_t n,
+                                                     double* __restrict__ part) {
+  const typename P::V* a = V + (int64_t)blockIdx.y * ld;
+  typename P::A sr, si;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const float2 p = a[i], q = x[i];
+    const typename P::V p = a[i], q = x[i];
     sr.add_prod(p.x, q.x);
     sr.add_prod(p.y, q.y);
     si.add_prod(p.x, q.y);
@@ -116,19 +166,21 @@ __global__ void __launch_bounds__(kRedThreads) k_finish(const double* __restrict
   }
 }
 
-// w = w - alpha v - beta vprev (float-float with FP64 alpha/beta, one final
+// w = w - alpha v - beta vprev (FP64 alpha/beta; P32: float-float, one final
 // rounding to the FP32 storage), and partial sums of |w|^2 of the stored values.
-__global__ void __launch_bounds__(kRedThreads) k_step(float2* __restrict__ w, const float2* __restrict__ v,
-                                                      const float2* __restrict__ vprev,
+template <class P>
+__global__ void __launch_bounds__(kRedThreads) k_step(typename P::V* __restrict__ w, const typename P::V* __restrict__ v,
+                                                      const typename P::V* __restrict__ vprev,
                                                       const double* __restrict__ alpha,
                                                       const double* __restrict__ beta, int64_t n,
                                                       double* __restrict__ part) {
-  const FFScalar a(*alpha), b(vprev ? *beta : 0.0);
-  FFAcc s;
+  using V = typename P::V;
+  const typename P::S a(*alpha), b(vprev ? *beta : 0.0);
+  typename P::A s;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const float2 wi = w[i], vi = v[i];
-    const float2 pi = vprev ? vprev[i] : make_float2(0.f, 0.f);
-    const float2 o = make_float2(ff_axpy2(wi.x, a, vi.x, b, pi.x), ff_axpy2(wi.y, a, vi.y, b, pi.y));
+    const V wi = w[i], vi = v[i];
+    const V pi = vprev ? vprev[i] : mk<P>(0, 0);
+    const V o = mk<P>(P::axpy2(wi.x, a, vi.x, b, pi.x), P::axpy2(wi.y, a, vi.y, b, pi.y));
     w[i] = o;
     s.add_prod(o.x, o.x);
     s.add_prod(o.y, o.y);
@@ -146,9 +198,9 @@ __global__ void __launch_bounds__(kRedThreads) k_step(float2* __restrict__ w, co
   }
 }
 
-// Block sums of kQ complex float-float accumulators into part[(k*gridDim.x + b)*2 + {0,1}].
-template <int kQ>
-__device__ __forceinline__ void block_partials(const FFAcc (&r)[kQ], const FFAcc (&i)[kQ], double* part) {
+// Block sums of kQ complex accumulators into part[(k*gridDim.x + b)*2 + {0,1}].
+template <int kQ, class A>
+__device__ __forceinline__ void block_partials(const A (&r)[kQ], const A (&i)[kQ], double* part) {
   __shared__ double rr[kRedThreads], ri[kRedThreads];
   for (int k = 0; k < kQ; ++k) {
     rr[threadIdx.x] = r[k].value();
@@ -173,17 +225,20 @@ __device__ __forceinline__ void block_partials(const FFAcc (&r)[kQ], const FFAcc
 // The local form's step in one pass: w = w - alpha v - beta vprev as k_step,
 // then the partials of <v|w> and <vprev|w> (0 without vprev) for the local
 // reorthogonalisation, k = 0 and 1 in k_finish's layout.
-__global__ void __launch_bounds__(kRedThreads) k_step_dots(float2* __restrict__ w, const float2* __restrict__ v,
-                                                           const float2* __restrict__ vprev,
+template <class P>
+__global__ void __launch_bounds__(kRedThreads) k_step_dots(typename P::V* __restrict__ w,
+                                                           const typename P::V* __restrict__ v,
+                                                           const typename P::V* __restrict__ vprev,
                                                            const double* __restrict__ alpha,
                                                            const double* __restrict__ beta, int64_t n,
                                                            double* __restrict__ part) {
-  const FFScalar a(*alpha), b(vprev ? *beta : 0.0);
-  FFAcc r[2], im[2];
+  using V = typename P::V;
+  const typename P::S a(*alpha), b(vprev ? *beta : 0.0);
+  typename P::A r[2], im[2];
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const float2 wi = w[i], vi = v[i];
-    const float2 pi = vprev ? vprev[i] : make_float2(0.f, 0.f);
-    const float2 o = make_float2(ff_axpy2(wi.x, a, vi.x, b, pi.x), ff_axpy2(wi.y, a, vi.y, b, pi.y));
+    const V wi = w[i], vi = v[i];
+    const V pi = vprev ? vprev[i] : mk<P>(0, 0);
+    const V o = mk<P>(P::axpy2(wi.x, a, vi.x, b, pi.x), P::axpy2(wi.y, a, vi.y, b, pi.y));
     w[i] = o;
     r[0].add_prod(vi.x, o.x);
     r[0].add_prod(vi.y, o.y);
@@ -197,96 +252,122 @@ __global__ void __launch_bounds__(kRedThreads) k_step_dots(float2* __restrict__ 
   block_partials<2>(r, im, part);
 }
 
-// w -= q0 v + q1 vprev (q complex, device; FP32 arithmetic as k_sub32) and the
-// partials of |w|^2 in k_finish's layout.
-__global__ void __launch_bounds__(kRedThreads) k_sub2_norm(float2* __restrict__ w, const float2* __restrict__ v,
-                                                           const float2* __restrict__ vprev,
+// w -= q0 v + q1 vprev (q complex, device; arithmetic in the vectors'
+// precision, as k_sub) and the partials of |w|^2 in k_finish's layout.
+template <class P>
+__global__ void __launch_bounds__(kRedThreads) k_sub2_norm(typename P::V* __restrict__ w,
+                                                           const typename P::V* __restrict__ v,
+                                                           const typename P::V* __restrict__ vprev,
                                                            const double* __restrict__ q, int64_t n,
                                                            double* __restrict__ part) {
-  const float q0r = (float)q[0], q0i = (float)q[1], q1r = (float)q[2], q1i = (float)q[3];
-  FFAcc r[1], im[1];
+  using V = typename P::V;
+  using R = typename P::Real;
+  const R q0r = (R)q[0], q0i = (R)q[1], q1r = (R)q[2], q1i = (R)q[3];
+  typename P::A r[1], im[1];
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const float2 y0 = w[i], vi = v[i];
-    float re = fmaf(-q0r, vi.x, fmaf(q0i, vi.y, y0.x));
-    float ii = fmaf(-q0r, vi.y, fmaf(-q0i, vi.x, y0.y));
+    const V y0 = w[i], vi = v[i];
+    R re = fmr(-q0r, vi.x, fmr(q0i, vi.y, y0.x));
+    R ii = fmr(-q0r, vi.y, fmr(-q0i, vi.x, y0.y));
     if (vprev) {
-      const float2 pi = vprev[i];
-      re = fmaf(-q1r, pi.x, fmaf(q1i, pi.y, re));
-      ii = fmaf(-q1r, pi.y, fmaf(-q1i, pi.x, ii));
+      const V pi = vprev[i];
+      re = fmr(-q1r, pi.x, fmr(q1i, pi.y, re));
+      ii = fmr(-q1r, pi.y, fmr(-q1i, pi.x, ii));
     }
-    w[i] = make_float2(re, ii);
+    w[i] = mk<P>(re, ii);
     r[0].add_prod(re, re);
     r[0].add_prod(ii, ii);
   }
   block_partials<1>(r, im, part);
 }
 
-// dst = src / beta (dst may be src); 1/beta as an FP32 head and tail
-__global__ void k_scale_inv(float2* dst, const float2* src, const double* __restrict__ beta, int64_t n) {
-  const FFScalar s(1.0 / *beta);
+// dst = src / beta (dst may be src); P32: 1/beta as an FP32 head and tail
+template <class P>
+__global__ void k_scale_inv(typename P::V* dst, const typename P::V* src, const double* __restrict__ beta, int64_t n) {
+  const typename P::S s(1.0 / *beta);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const float2 x = src[i];
-    dst[i] = make_float2(fmaf(x.x, s.l, __fmul_rn(x.x, s.h)), fmaf(x.y, s.l, __fmul_rn(x.y, s.h)));
+    const typename P::V x = src[i];
+    dst[i] = mk<P>(P::scale(x.x, s), P::scale(x.y, s));
   }
 }
 
-// y -= sum_k q_k V_k with q (complex, device) read into shared memory.  The
-// q_k are tiny against |y| once the vectors are nearly orthogonal, so FP32
-// arithmetic adds errors far below the FP32 rounding of y itself.
-__global__ void k_sub32(float2* __restrict__ y, const float2* __restrict__ V, int64_t ld,
-                        const double* __restrict__ q, int K, int64_t n) {
-  extern __shared__ float sqf[];
-  for (int k = threadIdx.x; k < 2 * K; k += blockDim.x) sqf[k] = (float)q[k];
+// y -= sum_k q_k V_k with q (complex, device) read into shared memory in the
+// vectors' precision.  The q_k are tiny against |y| once the vectors are
+// nearly orthogonal, so P32's FP32 arithmetic adds errors far below the FP32
+// rounding of y itself.
+template <class P>
+__global__ void k_sub(typename P::V* __restrict__ y, const typename P::V* __restrict__ V, int64_t ld,
+                      const double* __restrict__ q, int K, int64_t n) {
+  using R = typename P::Real;
+  extern __shared__ __align__(16) unsigned char sraw[];
+  R* sq = reinterpret_cast<R*>(sraw);
+  for (int k = threadIdx.x; k < 2 * K; k += blockDim.x) sq[k] = (R)q[k];
   __syncthreads();
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const float2 y0 = y[i];
-    float re = y0.x, im = y0.y;
+    const typename P::V y0 = y[i];
+    R re = y0.x, im = y0.y;
     for (int k = 0; k < K; ++k) {
-      const float2 vv = V[(int64_t)k * ld + i];
-      const float qr = sqf[2 * k], qi = sqf[2 * k + 1];
-      re = fmaf(-qr, vv.x, fmaf(qi, vv.y, re));
-      im = fmaf(-qr, vv.y, fmaf(-qi, vv.x, im));
+      const typename P::V vv = V[(int64_t)k * ld + i];
+      const R qr = sq[2 * k], qi = sq[2 * k + 1];
+      re = fmr(-qr, vv.x, fmr(qi, vv.y, re));
+      im = fmr(-qr, vv.y, fmr(-qi, vv.x, im));
     }
-    y[i] = make_float2(re, im);
+    y[i] = mk<P>(re, im);
   }
 }
 
 // Second pass of the resident-vector mode: X_e += sum_t y[e*m + j0 + t] V_{j0+t}
 // over a window of cnt <= kRing vectors still resident in the ring, so each
 // FP64 Ritz vector is read and written once per window instead of once per
-// step.  The window sum is float-float; the add to X is FP64.
+// step.  P32: the window sum is float-float; the add to X is FP64.
 constexpr int kRing = 8;
+template <class P>
 struct RingPtrs {
-  const float2* v[kRing];
+  const typename P::V* v[kRing];
 };
-__global__ void __launch_bounds__(256) k_ritz_window(double2* __restrict__ X, int64_t n, RingPtrs ring, int cnt,
+template <class P>
+__global__ void __launch_bounds__(256) k_ritz_window(double2* __restrict__ X, int64_t n, RingPtrs<P> ring, int cnt,
                                                      const double* __restrict__ y, int m, int j0, int E) {
-  __shared__ float2 sc[kMaxEv * kRing];  // (head, tail) of y[e*m + j0 + t] at e*kRing + t
+  __shared__ double sc[kMaxEv * kRing];  // y[e*m + j0 + t] at e*kRing + t
   for (int k = threadIdx.x; k < E * cnt; k += blockDim.x) {
     const int e = k / cnt, t = k % cnt;
-    const FFScalar c(y[(int64_t)e * m + j0 + t]);
-    sc[e * kRing + t] = make_float2(c.h, c.l);
+    sc[e * kRing + t] = y[(int64_t)e * m + j0 + t];
   }
   __syncthreads();
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    float2 v[kRing];
+    typename P::V v[kRing];
 #pragma unroll
     for (int t = 0; t < kRing; ++t)
       if (t < cnt) v[t] = ring.v[t][i];
     for (int e = 0; e < E; ++e) {
-      FFAcc ar, ai;
+      double sr, si;
+      if (P::kFp64) {
+        Acc ar, ai;
 #pragma unroll
-      for (int t = 0; t < kRing; ++t)
-        if (t < cnt) {
-          const float2 c = sc[e * kRing + t];
-          ar.add_prod(c.x, v[t].x);
-          ar.lo = fmaf(c.y, v[t].x, ar.lo);
-          ai.add_prod(c.x, v[t].y);
-          ai.lo = fmaf(c.y, v[t].y, ai.lo);
-        }
+        for (int t = 0; t < kRing; ++t)
+          if (t < cnt) {
+            const double c = sc[e * kRing + t];
+            ar.add(c * (double)v[t].x);
+            ai.add(c * (double)v[t].y);
+          }
+        sr = ar.value();
+        si = ai.value();
+      } else {
+        FFAcc ar, ai;
+#pragma unroll
+        for (int t = 0; t < kRing; ++t)
+          if (t < cnt) {
+            const FFScalar c(sc[e * kRing + t]);
+            ar.add_prod(c.h, (float)v[t].x);
+            ar.lo = fmaf(c.l, (float)v[t].x, ar.lo);
+            ai.add_prod(c.h, (float)v[t].y);
+            ai.lo = fmaf(c.l, (float)v[t].y, ai.lo);
+          }
+        sr = ar.value();
+        si = ai.value();
+      }
       double2 x = X[(int64_t)e * n + i];
-      x.x += ar.value();
-      x.y += ai.value();
+      x.x += sr;
+      x.y += si;
       X[(int64_t)e * n + i] = x;
     }
   }
@@ -327,36 +408,60 @@ __global__ void __launch_bounds__(kRedThreads) k_rq_partial(const double2* __res
 }
 
 // X_q = sum_{j < cnt} y[q*m + j] V_j for q in [q0, q0 + qn), qn <= kRitzChunk:
-// each V_j is read once per chunk of Ritz vectors.  The coefficients are split
-// into FP32 heads and tails and the sums kept in float-float (ff.cuh), written
-// out in FP64.
+// each V_j is read once per chunk of Ritz vectors.  P32: the coefficients are
+// split into FP32 heads and tails and the sums kept in float-float (ff.cuh);
+// P64: FP64 products in compensated FP64 sums.  Written out in FP64.
 constexpr int kRitzChunk = 8;
+template <class P>
 __global__ void __launch_bounds__(256) k_ritz_vectors(double2* __restrict__ X, int64_t n,
-                                                      const float2* __restrict__ V, int64_t ldv,
+                                                      const typename P::V* __restrict__ V, int64_t ldv,
                                                       const double* __restrict__ y, int m, int cnt, int q0, int qn) {
-  extern __shared__ float2 sy2[];  // qn * cnt (head, tail)
-  for (int k = threadIdx.x; k < qn * cnt; k += blockDim.x) {
-    const FFScalar c(y[(int64_t)(q0 + k / cnt) * m + k % cnt]);
-    sy2[k] = make_float2(c.h, c.l);
-  }
-  __syncthreads();
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    FFAcc ar[kRitzChunk], ai[kRitzChunk];
-    for (int j = 0; j < cnt; ++j) {
-      const float2 v = V[(int64_t)j * ldv + i];
+  extern __shared__ __align__(16) unsigned char sraw[];
+  if (P::kFp64) {
+    double* sy = reinterpret_cast<double*>(sraw);  // qn * cnt coefficients
+    for (int k = threadIdx.x; k < qn * cnt; k += blockDim.x) sy[k] = y[(int64_t)(q0 + k / cnt) * m + k % cnt];
+    __syncthreads();
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+      Acc ar[kRitzChunk], ai[kRitzChunk];
+      for (int j = 0; j < cnt; ++j) {
+        const typename P::V v = V[(int64_t)j * ldv + i];
+#pragma unroll
+        for (int q = 0; q < kRitzChunk; ++q)
+          if (q < qn) {
+            const double c = sy[q * cnt + j];
+            ar[q].add(c * (double)v.x);
+            ai[q].add(c * (double)v.y);
+          }
+      }
 #pragma unroll
       for (int q = 0; q < kRitzChunk; ++q)
-        if (q < qn) {
-          const float2 c = sy2[q * cnt + j];
-          ar[q].add_prod(c.x, v.x);
-          ar[q].lo = fmaf(c.y, v.x, ar[q].lo);
-          ai[q].add_prod(c.x, v.y);
-          ai[q].lo = fmaf(c.y, v.y, ai[q].lo);
-        }
+        if (q < qn) X[(int64_t)(q0 + q) * n + i] = make_double2(ar[q].value(), ai[q].value());
     }
+  } else {
+    float2* sy2 = reinterpret_cast<float2*>(sraw);  // qn * cnt (head, tail)
+    for (int k = threadIdx.x; k < qn * cnt; k += blockDim.x) {
+      const FFScalar c(y[(int64_t)(q0 + k / cnt) * m + k % cnt]);
+      sy2[k] = make_float2(c.h, c.l);
+    }
+    __syncthreads();
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+      FFAcc ar[kRitzChunk], ai[kRitzChunk];
+      for (int j = 0; j < cnt; ++j) {
+        const typename P::V v = V[(int64_t)j * ldv + i];
 #pragma unroll
-    for (int q = 0; q < kRitzChunk; ++q)
-      if (q < qn) X[(int64_t)(q0 + q) * n + i] = make_double2(ar[q].value(), ai[q].value());
+        for (int q = 0; q < kRitzChunk; ++q)
+          if (q < qn) {
+            const float2 c = sy2[q * cnt + j];
+            ar[q].add_prod(c.x, (float)v.x);
+            ar[q].lo = fmaf(c.y, (float)v.x, ar[q].lo);
+            ai[q].add_prod(c.x, (float)v.y);
+            ai[q].lo = fmaf(c.y, (float)v.y, ai[q].lo);
+          }
+      }
+#pragma unroll
+      for (int q = 0; q < kRitzChunk; ++q)
+        if (q < qn) X[(int64_t)(q0 + q) * n + i] = make_double2(ar[q].value(), ai[q].value());
+    }
   }
 }
 
@@ -439,29 +544,40 @@ cudaError_t MixedFinish::reserve_x(int64_t n, int na) {
   return grow((void**)&X, sizeof(double2) * n * na, x_bytes);
 }
 
-int MixedFinish::ritz_stored(cudaStream_t st, const float2* V, int64_t n, int m, int na, int cnt,
-                             const double* ycoef) {
-  const double* yc = ycoef ? ycoef : y;
+template <class P>
+static int ritz_stored_t(MixedFinish& F, cudaStream_t st, const typename P::V* V, int64_t n, int m, int na, int cnt,
+                         const double* ycoef) {
+  const double* yc = ycoef ? ycoef : F.y;
   // the coefficients of up to kRitzChunk Ritz vectors sit in shared memory:
   // 64 bytes a Krylov vector, past the default 48 KB above 768 vectors
   // (the solvers cap the steps at 2000, i.e. 128 KB, within the opt-in limit)
-  const size_t smem_max = sizeof(float2) * std::min(kRitzChunk, na) * cnt;
+  const size_t smem_max = 8 * std::min(kRitzChunk, na) * (size_t)cnt;
   if (smem_max > 48 * 1024) {
     int dev = 0, optin = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (smem_max > (size_t)optin)
       return fail(EDG_ERR_UNSUPPORTED, "mixed Lanczos: too many stored steps for the Ritz-vector kernel");
-    const cudaError_t ea = cudaFuncSetAttribute(k_ritz_vectors, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    const cudaError_t ea = cudaFuncSetAttribute(k_ritz_vectors<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                 (int)smem_max);
     if (ea != cudaSuccess) return cuda_fail(ea, "mixed Lanczos: Ritz-vector kernel shared memory");
   }
   for (int q0 = 0; q0 < na; q0 += kRitzChunk) {
     const int qn = std::min(kRitzChunk, na - q0);
-    k_ritz_vectors<<<grid_n(n), 256, sizeof(float2) * qn * cnt, st>>>(X, n, V, n, yc, m, cnt, q0, qn);
+    k_ritz_vectors<P><<<grid_n(n), 256, 8 * (size_t)qn * cnt, st>>>(F.X, n, V, n, yc, m, cnt, q0, qn);
   }
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? EDG_OK : cuda_fail(e, "mixed Lanczos: Ritz vectors");
+}
+
+int MixedFinish::ritz_stored(cudaStream_t st, const float2* V, int64_t n, int m, int na, int cnt,
+                             const double* ycoef) {
+  return ritz_stored_t<P32>(*this, st, V, n, m, na, cnt, ycoef);
+}
+
+int MixedFinish::ritz_stored(cudaStream_t st, const double2* V, int64_t n, int m, int na, int cnt,
+                             const double* ycoef) {
+  return ritz_stored_t<P64>(*this, st, V, n, m, na, cnt, ycoef);
 }
 
 cudaError_t MixedFinish::rayleigh_async(Sector& S, cudaStream_t st, int64_t n, int na, double* res_dev) {
@@ -496,8 +612,11 @@ void pick_levels(const std::vector<double>& rr, const std::vector<double>& th, c
   }
 }
 
-int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, double* resid, int64_t* n_out,
-                double* evecs, edg_mixed_stats* stats) {
+template <class P>
+static int solve_mixed_t(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, double* resid,
+                         int64_t* n_out, double* evecs, edg_mixed_stats* stats) {
+  using Vt = typename P::V;
+  constexpr size_t kVB = sizeof(Vt);
   const int64_t n = S.P.n_p;
   const int m = (int)std::min<int64_t>(o.iterations, n);
   const int want = std::min(std::min(o.n_ev, kMaxEv), m);
@@ -508,14 +627,14 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
   using clk = std::chrono::steady_clock;
   const auto t_start = clk::now();
   Dev D;
-  float2 *V = nullptr, *w = nullptr, *buf[kRing] = {};
+  Vt *V = nullptr, *w = nullptr, *buf[kRing] = {};
   int ring = 3;  // resident vectors past the stored ones: the recurrence needs 3
   int kept = 0;   // v_0 .. v_{kept-1} stored in V; the later ones live in the ring
   double *alpha, *beta, *part, *scal, *lq;
   cudaError_t e = cudaSuccess;
   if (reorth) {
     if ((e = D.alloc(&V, (size_t)n * (m + 1))) != cudaSuccess)
-      return fail(EDG_ERR_NOMEM, "mixed Lanczos: the stored FP32 Krylov vectors do not fit (use reorth_every=0)");
+      return fail(EDG_ERR_NOMEM, "mixed Lanczos: the stored Krylov vectors do not fit (use reorth_every=0)");
     kept = m + 1;
   } else {
     // Without full reorthogonalisation the vectors are still stored, as many
@@ -526,7 +645,7 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
     const int n_try = std::min(kMaxEv, std::min(want + 4, m));
-    const double vb = 8.0 * (double)n;
+    const double vb = (double)kVB * (double)n;
     const double rest = 16.0 * n * n_try + vb * (kRing + 2) + double(1 << 30);
     const double fit = std::floor((0.9 * (double)free_b - rest) / vb);
     int k = fit >= (double)(m + 1) ? m + 1 : (int)std::max(0.0, fit);
@@ -550,7 +669,7 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
     // then adds them to the Ritz vectors a window at a time
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
-    const size_t vb = sizeof(float2) * (size_t)n;
+    const size_t vb = kVB * (size_t)n;
     while (ring < kRing && free_b > vb * (size_t)(kRing - ring + 8) &&
            D.alloc(&buf[ring], (size_t)n) == cudaSuccess)
       ++ring;
@@ -564,9 +683,9 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
     return fail(EDG_ERR_NOMEM, "mixed Lanczos: scratch");
   cudaMemsetAsync(beta, 0, sizeof(double) * (m + 2), st);
 
-  auto vec = [&](int j) -> float2* { return j < kept ? V + (int64_t)j * n : buf[(j - kept) % ring]; };
-  auto norm_into = [&](const float2* x, double* dst) {  // dst = |x| in FP64
-    k_dot32<<<dim3(kRedBlocks, 1), kRedThreads, 0, st>>>(x, 0, x, n, part);
+  auto vec = [&](int j) -> Vt* { return j < kept ? V + (int64_t)j * n : buf[(j - kept) % ring]; };
+  auto norm_into = [&](const Vt* x, double* dst) {  // dst = |x| in FP64
+    k_dot<P><<<dim3(kRedBlocks, 1), kRedThreads, 0, st>>>(x, 0, x, n, part);
     k_finish<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, dst, 2);
   };
   double t_hv = 0;
@@ -579,28 +698,29 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
     cudaError_t ce = cudaSuccess;
     const int j0 = second && kept > 0 ? kept - 1 : 0;
     if (j0 == 0) {
-      ce = edg_fill_random(w, n, EDG_C64, o.seed, st) == EDG_OK ? cudaSuccess : cudaErrorUnknown;
+      ce = edg_fill_random(w, n, P::kFp64 ? EDG_C128 : EDG_C64, o.seed, st) == EDG_OK ? cudaSuccess
+                                                                                    : cudaErrorUnknown;
       if (ce != cudaSuccess) return ce;
       norm_into(w, scal);                                     // |v0 unnormalised|
-      k_scale_inv<<<grid_n(n), 256, 0, st>>>(vec(0), w, scal, n);
+      k_scale_inv<P><<<grid_n(n), 256, 0, st>>>(vec(0), w, scal, n);
     }
     const int win = std::max(1, ring - 2);  // vectors V_j0..V_j still resident at step j
     int acc_from = second ? kept : 0;
     for (int j = j0; j < m; ++j) {
       if (second) {
         if (j - acc_from + 1 == win || j + 1 == m) {
-          RingPtrs rp{};
+          RingPtrs<P> rp{};
           for (int t = 0; t <= j - acc_from; ++t) rp.v[t] = vec(acc_from + t);
-          k_ritz_window<<<grid_n(n), 256, 0, st>>>(X, n, rp, j - acc_from + 1, yd, m, acc_from, E);
+          k_ritz_window<P><<<grid_n(n), 256, 0, st>>>(X, n, rp, j - acc_from + 1, yd, m, acc_from, E);
           acc_from = j + 1;
         }
         if (j + 1 == m) break;
       }
       auto t0 = clk::now();
-      if ((ce = launch_hv(S, vec(j), w, false, st)) != cudaSuccess) return ce;
+      if ((ce = launch_hv(S, vec(j), w, P::kFp64, st)) != cudaSuccess) return ce;
       ++hv_calls;
       if (!second) {
-        k_dot32<<<dim3(kRedBlocks, 1), kRedThreads, 0, st>>>(vec(j), 0, w, n, part);
+        k_dot<P><<<dim3(kRedBlocks, 1), kRedThreads, 0, st>>>(vec(j), 0, w, n, part);
         k_finish<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, alpha + j, 1);
       }
       if (!reorth) {
@@ -610,33 +730,34 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
         // coefficients in one pass, the subtraction and |w|^2 in another.
         // The second pass repeats it (the kernels are deterministic, so with
         // the same coefficients).
-        const float2* vp = j > 0 ? vec(j - 1) : nullptr;
-        k_step_dots<<<kRedBlocks, kRedThreads, 0, st>>>(w, vec(j), vp, alpha + j, beta + j, n, part);
+        const Vt* vp = j > 0 ? vec(j - 1) : nullptr;
+        k_step_dots<P><<<kRedBlocks, kRedThreads, 0, st>>>(w, vec(j), vp, alpha + j, beta + j, n, part);
         k_finish<<<2, kRedThreads, 0, st>>>(part, kRedBlocks, lq, 0);
-        k_sub2_norm<<<kRedBlocks, kRedThreads, 0, st>>>(w, vec(j), vp, lq, n, part);
+        k_sub2_norm<P><<<kRedBlocks, kRedThreads, 0, st>>>(w, vec(j), vp, lq, n, part);
         if (!second) k_finish<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, beta + j + 1, 2);
       } else {
-        k_step<<<kRedBlocks, kRedThreads, 0, st>>>(w, vec(j), j > 0 ? vec(j - 1) : nullptr, alpha + j, beta + j, n,
-                                                   part);
+        k_step<P><<<kRedBlocks, kRedThreads, 0, st>>>(w, vec(j), j > 0 ? vec(j - 1) : nullptr, alpha + j, beta + j,
+                                                      n, part);
         if (!second && (j + 1) % o.reorth_every == 0) {
           // Periodic reorthogonalisation in its two-vector form: between two
           // reorthogonalisations v_j has drifted too, so it is cleaned against
           // v_0..v_{j-1} first, then w against v_0..v_j; each classical
           // Gram-Schmidt pass runs twice.  (Cleaning w alone lets the
           // recurrence carry v_j's error into every later vector.)
-          auto cgs2 = [&](float2* x, int K) {
+          auto cgs2 = [&](Vt* x, int K) {
             for (int pass = 0; pass < 2; ++pass)
               for (int k0 = 0; k0 < K; k0 += 512) {
                 const int kk = std::min(512, K - k0);
-                k_dot32<<<dim3(kRedBlocks, kk), kRedThreads, 0, st>>>(V + (int64_t)k0 * n, n, x, n, part);
+                k_dot<P><<<dim3(kRedBlocks, kk), kRedThreads, 0, st>>>(V + (int64_t)k0 * n, n, x, n, part);
                 k_finish<<<kk, kRedThreads, 0, st>>>(part, kRedBlocks, scal, 0);
-                k_sub32<<<grid_n(n), 256, sizeof(float) * 2 * kk, st>>>(x, V + (int64_t)k0 * n, n, scal, kk, n);
+                k_sub<P><<<grid_n(n), 256, sizeof(typename P::Real) * 2 * kk, st>>>(x, V + (int64_t)k0 * n, n, scal,
+                                                                                    kk, n);
               }
           };
           if (o.reorth_every > 1 && j > 0) {
             cgs2(vec(j), j);
             norm_into(vec(j), scal + 2 * (m + 1));
-            k_scale_inv<<<grid_n(n), 256, 0, st>>>(vec(j), vec(j), scal + 2 * (m + 1), n);
+            k_scale_inv<P><<<grid_n(n), 256, 0, st>>>(vec(j), vec(j), scal + 2 * (m + 1), n);
           }
           cgs2(w, j + 1);
           norm_into(w, beta + j + 1);
@@ -644,7 +765,7 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
           k_finish<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, beta + j + 1, 2);
         }
       }
-      if (j + 1 < m || second) k_scale_inv<<<grid_n(n), 256, 0, st>>>(vec(j + 1), w, beta + j + 1, n);
+      if (j + 1 < m || second) k_scale_inv<P><<<grid_n(n), 256, 0, st>>>(vec(j + 1), w, beta + j + 1, n);
       if ((ce = cudaGetLastError()) != cudaSuccess) return ce;
       t_hv += std::chrono::duration<double>(clk::now() - t0).count();
     }
@@ -709,6 +830,12 @@ int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, 
     stats->total_seconds = std::chrono::duration<double>(clk::now() - t_start).count();
   }
   return EDG_OK;
+}
+
+int solve_mixed(Sector& S, const edg_mixed_opts& o, double* eigs, double* ritz, double* resid, int64_t* n_out,
+                double* evecs, edg_mixed_stats* stats) {
+  return o.fp64_vectors ? solve_mixed_t<P64>(S, o, eigs, ritz, resid, n_out, evecs, stats)
+                        : solve_mixed_t<P32>(S, o, eigs, ritz, resid, n_out, evecs, stats);
 }
 
 }  // namespace edg

@@ -260,6 +260,9 @@ __global__ void k_u_scale(const typename CT2<Real>::T* __restrict__ v, const uin
 //   0: the next group's offsets;
 //   1: also the next group's head entries, so their DRAM latency overlaps
 //      the current group's gathers instead of preceding them.
+// (Prefetching the next group's gather targets into L2 as well
+// (prefetch.global.L2) measured 121 ms against 60.6 ms at 36 sites: the
+// extra L2 requests cost more than the earlier start gains.)
 // The sums are the same bits either way.  (Loading the next group's gathers
 // as well, two groups' gathers in flight per warp, measured slower at 36
 // sites: 74.7 ms against 60.6 ms at 2 CTAs per SM.)

@@ -167,15 +167,17 @@ class GpuSector:
         return eigs[: n_out.value], evecs, stats
 
     def solve_mixed(self, n_ev: int = 6, iterations: int = 300, reorth_every: int = 1, seed: int = 1,
-                    want_vectors: bool = False):
-        """Lowest eigenvalues with FP32 Krylov vectors (edg_solve_mixed).
+                    want_vectors: bool = False, fp64_vectors: bool = False):
+        """Lowest eigenvalues with FP32 Krylov vectors (edg_solve_mixed); with
+        fp64_vectors the same algorithm in FP64 throughout.
         Returns dict(eigs, ritz, residuals, evecs, stats)."""
         k = min(n_ev, 32)
         eigs = np.empty(k, np.float64)
         ritz = np.empty(k, np.float64)
         res = np.empty(k, np.float64)
         evecs = np.empty((k, self.n_p), np.complex128) if want_vectors else None
-        opts = N.edg_mixed_opts(int(n_ev), int(iterations), int(reorth_every), int(seed), int(bool(want_vectors)))
+        opts = N.edg_mixed_opts(int(n_ev), int(iterations), int(reorth_every), int(seed), int(bool(want_vectors)),
+                                int(bool(fp64_vectors)))
         n_out = C.c_int64()
         st = N.edg_mixed_stats()
         N.check(N.lib().edg_solve_mixed(self._h, C.byref(opts), eigs.ctypes.data, ritz.ctypes.data, res.ctypes.data,

@@ -17,7 +17,7 @@
 extern "C" {
 #endif
 
-#define EDGPU_ABI_VERSION 6
+#define EDGPU_ABI_VERSION 7
 
 enum {
   EDG_OK = 0,
@@ -27,7 +27,8 @@ enum {
   EDG_ERR_CUDA = 4,         /* a CUDA call failed */
   EDG_ERR_NOMEM = 5,        /* not enough device memory for the sector */
   EDG_ERR_UNSUPPORTED = 6,  /* outside what this library implements (N > 40, too many terms) */
-  EDG_ERR_NOT_CONVERGED = 7 /* eigensolver stopped without meeting its tolerance */
+  EDG_ERR_NOT_CONVERGED = 7, /* eigensolver stopped without meeting its tolerance */
+  EDG_ERR_CANCELLED = 8      /* a batch segment withdrawn by edg_batch_cancel */
 };
 
 enum { EDG_C128 = 0, EDG_C64 = 1 };
@@ -216,6 +217,8 @@ typedef struct {
                                pass from the last stored vector */
   uint64_t seed;            /* start vector: splitmix64 stream */
   int want_vectors;         /* copy the FP64 eigenvectors out */
+  int fp64_vectors;         /* 0: FP32 Krylov vectors and H*v (the precision form); 1: the same
+                               algorithm with FP64 vectors, FP64 H*v and FP64 arithmetic throughout */
 } edg_mixed_opts;
 
 typedef struct {
@@ -286,6 +289,11 @@ int edg_batch_add(edg_batch* b, edg_sector* s, const edg_batch_request* req);
 /* Run up to n_steps steps of every live segment (fewer when none is left);
  * segments that stop are finished before this returns or at the next call. */
 int edg_batch_step(edg_batch* b, int n_steps);
+/* Withdraw the live segment with this tag: its memory is released now and its
+ * result (status EDG_ERR_CANCELLED, no levels) comes back through
+ * edg_batch_poll.  The other segments' arithmetic is unchanged.
+ * EDG_ERR_INVALID when no live segment has the tag. */
+int edg_batch_cancel(edg_batch* b, int64_t tag);
 /* Move up to cap finished results into out; *n_out receives how many. */
 int edg_batch_poll(edg_batch* b, edg_batch_result* out, int cap, int* n_out);
 int edg_batch_info(const edg_batch* b, int* n_active, int64_t* device_bytes, int64_t* steps);

@@ -70,12 +70,16 @@ class _Clock:
 
 
 class _Sector:
+    """Stand-in for GpuSector: models whose Jz is exactly 1.25 do not fit
+    (their stored rows fail like a full device), everything else builds."""
+
     def __init__(self, model):
         self.n_p = 100
         self.closed = False
+        self.fits = model.Jz != 1.25
 
     def build_targets(self):
-        return True
+        return self.fits
 
     def close(self):
         self.closed = True
@@ -87,9 +91,10 @@ def _fake_batch(clock, log):
 
         def __init__(self, **kw):
             self.left = {}
+            self.cancelled = set()
 
         def add(self, sec, n_ev, max_iterations, tol, seed, tag):
-            self.left[tag] = 2 + tag % 3
+            self.left[tag] = 40 if tag == 5 else 2 + tag % 3  # request 5 runs long
             log.append(("add", tag, len(self.left)))
 
         def step(self, n):
@@ -97,13 +102,20 @@ def _fake_batch(clock, log):
             for k in self.left:
                 self.left[k] -= 1
 
+        def cancel(self, tag):
+            self.left[tag] = 0  # reported by the next poll
+            self.cancelled.add(tag)
+            log.append(("cancel", tag))
+
         def poll(self):
             out = []
             for k in [k for k, v in self.left.items() if v <= 0]:
-                del self.left[k]
+                self.left.pop(k)
+                cancelled = k in self.cancelled
                 log.append(("done", k))
-                out.append({"tag": k, "eigs": np.array([-1.0 - k]), "residuals": np.array([1e-7]),
-                            "iterations": 30, "converged": True, "status": 0})
+                out.append({"tag": k, "eigs": np.zeros(0) if cancelled else np.array([-1.0 - k]),
+                            "residuals": np.array([1e-7]), "iterations": 30, "converged": not cancelled,
+                            "status": serving.CANCELLED if cancelled else 0})
             return out
 
         def close(self):
@@ -112,12 +124,14 @@ def _fake_batch(clock, log):
     return _Batch
 
 
-def _run(monkeypatch, requests, budget):
+def _run(monkeypatch, requests, budget, build_ahead=True, on_result=None, setup=None):
     clock, log = _Clock(), []
     monkeypatch.setattr(serving, "GpuSector", _Sector)
     monkeypatch.setattr(serving, "BatchSolver", _fake_batch(clock, log))
-    srv = serving.Server(hbm_budget=budget, max_iterations=300)
-    out = srv.run(requests, clock=clock)
+    srv = serving.Server(hbm_budget=budget, max_iterations=300, build_ahead=build_ahead)
+    if setup:
+        setup(srv, log)
+    out = srv.run(requests, clock=clock, on_result=on_result)
     return srv, out, log
 
 
@@ -152,3 +166,73 @@ def test_a_request_larger_than_the_budget_still_runs_alone(monkeypatch):
     reqs = serving.make_stream(3, rate=100.0, seed=9, sizes=(24,))
     srv, out, _ = _run(monkeypatch, reqs, budget=1)
     assert len(out) == 3 and srv.peak_live == 1
+
+
+def _bad(rid, arrival, **kw):
+    base = dict(spec=serving.L.TorusSpec("square", 5, 4), Sz=0.0, kx=0, ky=0, n_ev=1)
+    base.update(kw)
+    return serving.Request(rid, arrival, **base)
+
+
+def test_malformed_and_oversized_requests_are_rejected_alone(monkeypatch):
+    """Odd N, |Sz| > N/2, a momentum out of range, nev out of range and a
+    request whose stored rows do not fit come back rejected with a reason;
+    every other request is served exactly as in a stream without them."""
+    good = serving.make_stream(12, rate=40.0, seed=11, sizes=(20, 24))
+    _, ref, _ = _run(monkeypatch, good, budget=1 << 50)
+    t = good[3].arrival
+    bad = [
+        _bad(100, t, spec=serving.L.TorusSpec("square", 5, 3)),                 # 15 sites
+        _bad(101, t + 1e-3, Sz=11.0),                                             # |Sz| > N/2
+        _bad(102, t + 2e-3, Sz=0.5),                                              # not an allowed Sz for even N
+        _bad(103, t + 3e-3, kx=5),                                                # kx >= Lx
+        _bad(104, t + 4e-3, n_ev=0),
+        _bad(105, t + 5e-3, spec=serving.L.TorusSpec("square", 5, 4, Jz=1.25)),  # rows do not fit
+    ]
+    for build_ahead in (True, False):
+        _, out, log = _run(monkeypatch, good + bad, budget=1 << 50, build_ahead=build_ahead)
+        by = {s.rid: s for s in out}
+        assert sorted(by) == sorted(r.rid for r in good + bad)
+        for r in bad[:5]:
+            assert by[r.rid].status == serving.REJECTED_INVALID and by[r.rid].reason, by[r.rid]
+            assert ("add", r.rid) not in [e[:2] for e in log]
+        assert by[105].status == serving.REJECTED_NOMEM and "fit" in by[105].reason
+        for s in ref:
+            assert by[s.rid].ok and np.array_equal(by[s.rid].eigs, s.eigs)
+        summ = serving.summarize(out)
+        assert summ["solved"] == len(good) and summ["rejected"] == len(bad) and summ["cancelled"] == 0
+
+
+def test_cancel_queued_and_running_requests(monkeypatch):
+    """cancel() withdraws a request still queued (before it arrived) and one
+    already in the batch; both come back as CANCELLED, the rest are unchanged."""
+    reqs = serving.make_stream(16, rate=40.0, seed=12, sizes=(20,))
+    _, ref, _ = _run(monkeypatch, reqs, budget=1 << 50)
+    ref_by = {s.rid: s for s in ref}
+    late = reqs[-1].rid
+    holder = {}
+
+    def on_result(s):
+        # once two requests run together, cancel one of them at the next
+        # result, and one that has not arrived yet
+        log = holder["log"]
+        added = [e[1] for e in log if e[0] == "add"]
+        if "running" not in holder and 5 in added:  # request 5 runs for 40 steps
+            holder["running"] = 5
+            holder["srv"].cancel(5)
+            holder["srv"].cancel(late)
+
+    def setup(srv, log):
+        holder["srv"] = srv
+        holder["log"] = log
+
+    _, out, log = _run(monkeypatch, reqs, budget=1 << 50, on_result=on_result, setup=setup)
+    by = {s.rid: s for s in out}
+    assert sorted(by) == [r.rid for r in reqs]
+    assert by[late].status == serving.CANCELLED and ("add", late) not in [e[:2] for e in log]
+    assert by[holder["running"]].status == serving.CANCELLED
+    assert ("cancel", holder["running"]) in log
+    for rid, s in by.items():
+        if rid not in (late, holder["running"]):
+            assert s.ok and np.array_equal(s.eigs, ref_by[rid].eigs)
+    assert serving.summarize(out)["cancelled"] == 2
