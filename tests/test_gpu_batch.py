@@ -128,3 +128,27 @@ def test_large_segment_matches_single_sector_solver(mods):
     assert r["status"] == 0 and r["n_found"] >= 3, r
     rel = np.abs(r["eigs"][:3] - ref[:3]) / np.abs(ref[:3])
     assert rel.max() <= REL_TOL, (r["eigs"], ref)
+
+
+def test_cancel_releases_a_segment_and_leaves_the_others(mods):
+    """edg_batch_cancel: the withdrawn segment comes back as EDG_ERR_CANCELLED
+    with no levels and its memory released; the segments beside it finish
+    with the bits they have without it."""
+    batch, sector = mods
+    a = stored_sector(sector, "sq6x4_k00", 0)
+    b = stored_sector(sector, "tri6x4_k10", 0)
+    B1 = batch.BatchSolver(tile_rows=512)
+    B1.add(a, n_ev=2, max_iterations=120, tol=0.0, seed=7, tag=0)
+    alone = B1.run()[0]
+    B2 = batch.BatchSolver(tile_rows=512)
+    B2.add(a, n_ev=2, max_iterations=120, tol=0.0, seed=7, tag=0)
+    B2.add(b, n_ev=2, max_iterations=120, tol=0.0, seed=8, tag=1)
+    B2.step(30)
+    before = B2.info()["device_bytes"]
+    B2.cancel(1)
+    assert B2.info()["device_bytes"] < before and B2.info()["active"] == 1
+    res = {r["tag"]: r for r in B2.run()}
+    assert res[1]["status"] == 8 and res[1]["n_found"] == 0
+    assert res[0]["status"] == 0 and np.array_equal(res[0]["eigs"], alone["eigs"])
+    with pytest.raises(Exception):
+        B2.cancel(5)

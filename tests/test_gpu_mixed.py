@@ -99,3 +99,17 @@ def test_mixed_long_run_stored_ritz_vectors(gpu):
     assert out["stats"]["passes"] == 1 and out["stats"]["stored_vectors"] == 1001
     rel = np.abs(out["eigs"][:2] - ref) / np.abs(ref)
     assert rel.max() <= 1e-9, (out["eigs"], ref)
+
+
+def test_fp64_vector_arm_matches_reference(gpu):
+    """fp64_vectors: the same algorithm with FP64 vectors and arithmetic
+    reaches the reference's eigenvalues to 1e-10 and agrees with the FP32
+    form to 1e-9."""
+    ref = np.array(golden_cases()["tri6x4_k10"]["sectors"][0]["ed2_eigs"][:2])
+    sec = gpu.GpuSector(golden_model("tri6x4_k10", 0))
+    assert sec.build_targets()
+    r64 = sec.solve_mixed(n_ev=2, iterations=300, reorth_every=0, seed=1, fp64_vectors=True)
+    r32 = sec.solve_mixed(n_ev=2, iterations=300, reorth_every=0, seed=1)
+    assert np.max(np.abs(r64["eigs"][:2] - ref) / np.abs(ref)) <= 1e-10, (r64["eigs"], ref)
+    assert np.max(np.abs(r32["eigs"][:2] - r64["eigs"][:2]) / np.abs(ref)) <= 1e-9
+    assert max(r64["residuals"][:2]) < max(r32["residuals"][:2])

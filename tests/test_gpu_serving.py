@@ -80,3 +80,19 @@ def test_admission_keeps_to_the_budget(mods, stream):
     srv.close()
     assert len(out) == 6
     assert srv.peak_live == 1 and srv.peak_bytes <= one
+
+
+def test_bad_requests_are_reported_and_the_rest_unchanged(served, stream, mods):
+    """A malformed request and a cancelled one inside the stream come back
+    with their status; every other request has the bits it has without them."""
+    serving = mods[3]
+    bad = serving.Request(900, stream[2].arrival, serving.L.TorusSpec("square", 5, 4), 0.0, 9, 0, 1)  # kx >= Lx
+    extra = serving.Request(901, stream[3].arrival, stream[3].spec, stream[3].Sz, stream[3].kx, stream[3].ky, 1)
+    srv = serving.Server(max_iterations=300, res_tol=1e-6, tile_rows=TILE)
+    srv.cancel(901)  # withdrawn before it arrives
+    out = {s.rid: s for s in srv.run(list(stream) + [bad, extra])}
+    srv.close()
+    assert out[900].status == serving.REJECTED_INVALID and "momentum" in out[900].reason
+    assert out[901].status == serving.CANCELLED
+    for rid, s in served.items():
+        assert out[rid].ok and np.array_equal(out[rid].eigs, s.eigs)
