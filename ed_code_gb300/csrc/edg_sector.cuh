@@ -109,6 +109,9 @@ cudaError_t export_walk_tables(const Sector& S, int64_t* rep_loc_dev, int32_t* g
 // hv.cu
 cudaError_t launch_hv(const Sector& S, const void* v, void* w, bool fp64, cudaStream_t st);
 cudaError_t launch_hv_generic(const Sector& S, const void* v, void* w, bool fp64, cudaStream_t st);
+// dense.cu: exact_evecs on the device (all eigenvalues, the first evecs_cap eigenvectors)
+int solve_dense_device(Sector& S, double* eigs, int64_t cap, int64_t* n_out, double* evecs, int64_t evecs_cap,
+                       edg_solver_stats* stats);
 // lanczos.cu
 int solve_plain(Sector& S, const edg_solver_opts& o, double* eigs, int64_t cap, int64_t* n_out, double* evecs,
                 int64_t evecs_cap, edg_solver_stats* stats);

@@ -2,9 +2,8 @@
 //
 // solve_plain(): the reference's sector eigensolver in FP64 on the GPU --
 //   * n_p <= dense_threshold: exact_evecs (lanczos.cpp:81-131): the dense
-//     sector matrix (makeH, H_v.cpp:21-190, here assembled column by column
-//     from H*e_j) diagonalised by a dense Hermitian eigensolver, all
-//     eigenvalues returned;
+//     sector matrix (makeH, H_v.cpp:21-190) diagonalised on the device
+//     (dense.cu), all eigenvalues returned;
 //   * otherwise lanczos_evecs (lanczos.cpp:133-349), step for step: one
 //     eigenvalue at a time with deflation against the earlier eigenvectors,
 //     `ncycles` restarts of `iterations` steps, three-term recurrence
@@ -18,7 +17,6 @@
 //   (tridiag_dev.cu).  The host reads back only that eigenvalue each step,
 //   for the reference's log lines and convergence test.
 #include <cuda_runtime.h>
-#include <dlfcn.h>
 
 #include <algorithm>
 #include <chrono>
@@ -137,19 +135,6 @@ __global__ void k_scale_dev(T* __restrict__ y, const T* __restrict__ x, const do
   }
 }
 
-// y = a*x + b*y  (complex scalars by value)
-template <typename T>
-__global__ void k_axpby(T* __restrict__ y, const T* __restrict__ x, cd a, cd b, int64_t n) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const cd xv = x ? VecTraits<T>::load(x, i) : cd{0, 0};
-    const cd yv = VecTraits<T>::load(y, i);
-    cd r;
-    r.re = a.re * xv.re - a.im * xv.im + b.re * yv.re - b.im * yv.im;
-    r.im = a.re * xv.im + a.im * xv.re + b.re * yv.im + b.im * yv.re;
-    VecTraits<T>::store(y, i, r);
-  }
-}
-
 // y -= sum_k q_k V_k  (q: K complex on device)
 template <typename T>
 __global__ void k_sub_multi(T* __restrict__ y, const T* __restrict__ V, int64_t ld, const double* __restrict__ q,
@@ -185,11 +170,6 @@ __global__ void k_combine(T* __restrict__ out, const T* __restrict__ V, int64_t 
     }
     VecTraits<T>::store(out, i, r);
   }
-}
-
-__global__ void k_unit(double2* e, int64_t n, int64_t j) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    e[i] = make_double2(i == j ? 1.0 : 0.0, 0.0);
 }
 
 int grid_of(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16)); }
@@ -255,109 +235,6 @@ void orth(Blas& B, double2* v, const double2* V, int64_t ld, int K, int64_t n) {
 void normalize(Blas& B, double2* v, int64_t n) {
   B.norm(v, n, B.scal, 2);
   k_scale_dev<double2><<<grid_of(n), 256, 0, B.st>>>(v, v, B.scal, false, n);
-}
-
-// -------------------------------------------------- dense eigensolver (lib) --
-// cuSOLVER is loaded on first use, so the library does not depend on it unless
-// the dense path runs.
-struct Cusolver {
-  void* lib = nullptr;
-  int (*create)(void**) = nullptr;
-  int (*destroy)(void*) = nullptr;
-  int (*set_stream)(void*, cudaStream_t) = nullptr;
-  int (*zheevd_bufsize)(void*, int, int, int, const void*, int, const double*, int*) = nullptr;
-  int (*zheevd)(void*, int, int, int, void*, int, double*, void*, int, int*) = nullptr;
-  bool load(std::string& err) {
-    if (lib) return true;
-    const char* names[] = {"libcusolver.so", "libcusolver.so.12", "libcusolver.so.11", "libcusolver.so.13"};
-    for (const char* nm : names)
-      if ((lib = dlopen(nm, RTLD_NOW | RTLD_LOCAL))) break;
-    if (!lib) {
-      err = "dense path: libcusolver could not be loaded";
-      return false;
-    }
-    create = (int (*)(void**))dlsym(lib, "cusolverDnCreate");
-    destroy = (int (*)(void*))dlsym(lib, "cusolverDnDestroy");
-    set_stream = (int (*)(void*, cudaStream_t))dlsym(lib, "cusolverDnSetStream");
-    zheevd_bufsize = (int (*)(void*, int, int, int, const void*, int, const double*, int*))dlsym(
-        lib, "cusolverDnZheevd_bufferSize");
-    zheevd = (int (*)(void*, int, int, int, void*, int, double*, void*, int, int*))dlsym(lib, "cusolverDnZheevd");
-    if (!create || !destroy || !set_stream || !zheevd_bufsize || !zheevd) {
-      err = "dense path: cusolverDn symbols missing";
-      return false;
-    }
-    return true;
-  }
-};
-Cusolver g_cusolver;
-
-constexpr int kEigModeNoVector = 0, kEigModeVector = 1, kFillUpper = 1;  // cusolverEigMode_t, cublasFillMode_t
-
-int solve_dense(Sector& S, const edg_solver_opts& o, double* eigs, int64_t cap, int64_t* n_out, double* evecs,
-                int64_t evecs_cap, edg_solver_stats* stats) {
-  const int64_t n = S.P.n_p;
-  if (cap < n) return fail(EDG_ERR_INVALID, "dense path returns all n_p eigenvalues: eigs_capacity too small");
-  std::string err;
-  if (!g_cusolver.load(err)) return fail(EDG_ERR_UNSUPPORTED, err);
-  cudaStream_t st = S.stream;
-  double2 *H = nullptr, *e = nullptr, *work = nullptr;
-  double* W = nullptr;
-  int* info = nullptr;
-  auto cleanup = [&]() {
-    cudaFree(H);
-    cudaFree(e);
-    cudaFree(work);
-    cudaFree(W);
-    cudaFree(info);
-  };
-  cudaError_t ce = cudaMalloc(&H, sizeof(double2) * n * n);
-  if (ce == cudaSuccess) ce = cudaMalloc(&e, sizeof(double2) * n);
-  if (ce == cudaSuccess) ce = cudaMalloc(&W, sizeof(double) * n);
-  if (ce == cudaSuccess) ce = cudaMalloc(&info, sizeof(int));
-  if (ce != cudaSuccess) {
-    cleanup();
-    return fail(EDG_ERR_NOMEM, "dense path: out of device memory");
-  }
-  const auto t0 = std::chrono::steady_clock::now();
-  // column j of H = H e_j (makeH writes the same matrix elements)
-  for (int64_t j = 0; j < n && ce == cudaSuccess; ++j) {
-    k_unit<<<grid_of(n), 256, 0, st>>>(e, n, j);
-    ce = launch_hv(S, e, H + j * n, true, st);
-  }
-  if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
-  const auto t1 = std::chrono::steady_clock::now();
-  if (ce != cudaSuccess) {
-    cleanup();
-    return cuda_fail(ce, "dense path: assembling H");
-  }
-  void* h = nullptr;
-  int lwork = 0, hinfo = 0;
-  const int jobz = (evecs && evecs_cap > 0) ? kEigModeVector : kEigModeNoVector;
-  int rc = g_cusolver.create(&h);
-  if (rc == 0) rc = g_cusolver.set_stream(h, st);
-  if (rc == 0) rc = g_cusolver.zheevd_bufsize(h, jobz, kFillUpper, (int)n, H, (int)n, W, &lwork);
-  if (rc == 0 && cudaMalloc(&work, sizeof(double2) * std::max(1, lwork)) != cudaSuccess) rc = -1;
-  if (rc == 0) rc = g_cusolver.zheevd(h, jobz, kFillUpper, (int)n, H, (int)n, W, work, lwork, info);
-  if (rc == 0) ce = cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, st);
-  if (rc == 0 && ce == cudaSuccess) ce = cudaMemcpyAsync(eigs, W, sizeof(double) * n, cudaMemcpyDeviceToHost, st);
-  if (rc == 0 && ce == cudaSuccess && jobz == kEigModeVector) {
-    const int64_t nv = std::min<int64_t>(evecs_cap, n);
-    ce = cudaMemcpyAsync(evecs, H, sizeof(double2) * n * nv, cudaMemcpyDeviceToHost, st);
-  }
-  if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
-  if (h) g_cusolver.destroy(h);
-  cleanup();
-  if (rc != 0) return fail(EDG_ERR_CUDA, "dense path: cusolverDnZheevd failed (status " + std::to_string(rc) + ")");
-  if (ce != cudaSuccess) return cuda_fail(ce, "dense path");
-  if (hinfo != 0) return fail(EDG_ERR_NOT_CONVERGED, "dense path: zheevd info " + std::to_string(hinfo));
-  *n_out = n;
-  if (stats) {
-    stats->path = 1;
-    stats->hv_calls = n;
-    stats->hv_seconds = std::chrono::duration<double>(t1 - t0).count();
-    stats->total_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-  }
-  return EDG_OK;
 }
 
 void log_line(const edg_solver_opts& o, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
@@ -519,7 +396,7 @@ int solve_plain(Sector& S, const edg_solver_opts& o, double* eigs, int64_t cap, 
                 int64_t evecs_cap, edg_solver_stats* stats) {
   if (stats) std::memset(stats, 0, sizeof(*stats));
   if (o.dense_threshold >= 0 && S.P.n_p <= o.dense_threshold)
-    return solve_dense(S, o, eigs, cap, n_out, evecs, evecs_cap, stats);
+    return solve_dense_device(S, eigs, cap, n_out, evecs, evecs_cap, stats);
   return solve_lanczos(S, o, eigs, cap, n_out, evecs, evecs_cap, stats);
 }
 

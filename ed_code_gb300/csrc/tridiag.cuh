@@ -62,8 +62,19 @@ TD_HD double tridiag_eigenvalue(const double* d, const double* e, int m, int k) 
 
 // Eigenvector of eigenvalue lam, normalised, written to x[0..m-1].  Work
 // arrays: 5*m doubles in `wk`.  The sign is fixed so that the largest
-// component is positive.
+// component is positive.  For a level of a cluster of (nearly) equal
+// eigenvalues, `prev` holds the n_prev unit vectors already computed for the
+// cluster (m doubles each, consecutive): each sweep's iterate is
+// orthogonalised against them (modified Gram-Schmidt), and `seed` > 0 varies
+// the start vector, so the cluster's vectors come out orthonormal (the
+// approach of LAPACK's inverse iteration for clustered eigenvalues).
+TD_HD void tridiag_eigenvector_ex(const double* d, const double* e, int m, double lam, double* x, double* wk,
+                                  const double* prev, int n_prev, int seed);
 TD_HD void tridiag_eigenvector(const double* d, const double* e, int m, double lam, double* x, double* wk) {
+  tridiag_eigenvector_ex(d, e, m, lam, x, wk, nullptr, 0, 0);
+}
+TD_HD void tridiag_eigenvector_ex(const double* d, const double* e, int m, double lam, double* x, double* wk,
+                                  const double* prev, int n_prev, int seed) {
   double* u0 = wk;          // main diagonal of U
   double* u1 = wk + m;      // first superdiagonal of U
   double* u2 = wk + 2 * m;  // second superdiagonal of U (fill-in from pivoting)
@@ -100,7 +111,7 @@ TD_HD void tridiag_eigenvector(const double* d, const double* e, int m, double l
     }
   }
   if (u0[m - 1] == 0.0) u0[m - 1] = tiny;
-  for (int i = 0; i < m; ++i) x[i] = 1.0;
+  for (int i = 0; i < m; ++i) x[i] = seed > 0 ? 1.0 + 0.25 * (double)((i * (2 * seed + 1) + seed) % 7) / 7.0 : 1.0;
   for (int sweep = 0; sweep < 3; ++sweep) {
     // forward: apply the row operations to the right-hand side
     for (int k = 0; k + 1 < m; ++k) {
@@ -119,6 +130,12 @@ TD_HD void tridiag_eigenvector(const double* d, const double* e, int m, double l
       double p = u0[i];
       if (fabs(p) < tiny) p = p < 0 ? -tiny : tiny;
       x[i] = s / p;
+    }
+    for (int q = 0; q < n_prev; ++q) {
+      const double* pq = prev + (int64_t)q * m;
+      double dot = 0.0;
+      for (int i = 0; i < m; ++i) dot += pq[i] * x[i];
+      for (int i = 0; i < m; ++i) x[i] -= dot * pq[i];
     }
     double nrm = 0.0, big = 0.0;
     int arg = 0;
