@@ -124,6 +124,7 @@ SIGNATURES = {
     "edg_batch_poll": (C.c_int, [C.c_void_p, C.POINTER(edg_batch_result), C.c_int, C.POINTER(C.c_int)]),
     "edg_batch_timers": (C.c_int, [C.c_void_p, C.c_void_p]),
     "edg_batch_cancel": (C.c_int, [C.c_void_p, C.c_int64]),
+    "edg_batch_tune": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_void_p]),
     "edg_batch_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "edg_hv_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "edg_count_offdiag": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),

@@ -50,6 +50,17 @@ class BatchSolver:
     def step(self, n_steps: int = 1) -> None:
         N.check(N.lib().edg_batch_step(self._h, int(n_steps)))
 
+    def tune(self, steps: int = 3) -> dict:
+        """edg_batch_tune: time the tile sizes and lanes per row on the
+        segments added so far (before the first step), keep the fastest.
+        Returns {"tile_rows", "lanes_per_row", "ms_per_step": {"RxL": ms}}."""
+        t, l = C.c_int(), C.c_int()
+        ms = np.zeros(8, np.float64)
+        N.check(N.lib().edg_batch_tune(self._h, int(steps), C.byref(t), C.byref(l), ms.ctypes.data))
+        trials = {f"{r}x{k}": round(float(ms[2 * i + j]), 3)
+                  for i, r in enumerate((256, 1024, 4096, 16384)) for j, k in enumerate((8, 16))}
+        return {"tile_rows": t.value, "lanes_per_row": l.value, "ms_per_step": trials}
+
     def cancel(self, tag: int) -> None:
         """Withdraw a live segment (edg_batch_cancel); its result comes back
         from poll() with status EDG_ERR_CANCELLED."""

@@ -121,28 +121,52 @@ __device__ __forceinline__ void block_sum2(double& a, double& b) {
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(kThreads) k_b_u(const SegDev* __restrict__ segs, const SegState* __restrict__ ss,
-                                                  const TileDev* __restrict__ tiles) {
-  const TileDev t = tiles[blockIdx.x];
-  if (ss[t.seg].status != kRunning) return;
-  const SegDev& S = segs[t.seg];
-  const float2* v = S.V + (int64_t)ss[t.seg].j * S.n;
-  for (int r = threadIdx.x; r < t.rows; r += blockDim.x) {
-    const int64_t i = t.row0 + r;
-    const float s = (float)S.nrm_inv[S.lid[i]];
-    const float2 x = v[i];
-    S.u[i] = make_float2(x.x * s, x.y * s);
+// The fused kernels close a segment's reduction in whichever of its CTAs
+// finishes last: every CTA writes its partial, then takes a ticket; the CTA
+// holding the last ticket sums all the segment's partials in tile order (the
+// same order for any timing, so the result is deterministic) and resets the
+// counter for the next step.  No CTA waits for another.
+__device__ __forceinline__ bool last_cta(int* cnt, int total) {
+  __shared__ int is_last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const int t = atomicAdd(cnt, 1);
+    is_last = t == total - 1;
+    if (is_last) *cnt = 0;
   }
+  __syncthreads();
+  if (is_last) __threadfence();
+  return is_last != 0;
 }
+
+// sum of the tile partials part[2k], part[2k+1], k in [k0, k1), in order
+__device__ __forceinline__ void seg_sum(const double* part, int k0, int k1, double& a, double& b) {
+  a = 0;
+  b = 0;
+  for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+    a += __ldcg(part + 2 * k);
+    b += __ldcg(part + 2 * k + 1);
+  }
+  block_sum2(a, b);
+}
+
+// ticket counters of a segment, one per fused reduction
+enum { kCntAlpha = 0, kCntNorm = 1, kCntDecide = 2, kCntBeta = 3, kCntAdvance = 4, kCnts = 8 };
 
 // w = H V_j on the tile's rows: 32/LPR rows per warp, LPR lanes per row, each
 // row summed by the single-sector kernel's routines (unrolled entry loads,
 // streaming hint on the row data, L2 evict_last on u).  Pipelined like the
 // single-sector kernel: a warp loads the head entries of its next rows (and
 // the offsets of the rows after) before it gathers for the current ones.
+//
+// Then alpha_j = Re<V_j|w>: the tile's partial (exact products summed in
+// float-float per thread, FP64 across the CTA), closed per segment by the
+// last CTA.
 template <int LPR>
 __global__ void __launch_bounds__(kThreads) k_b_hv(const SegDev* __restrict__ segs, const SegState* __restrict__ ss,
-                                                   const TileDev* __restrict__ tiles) {
+                                                   const TileDev* __restrict__ tiles, const int* __restrict__ tb,
+                                                   double* __restrict__ part, int* __restrict__ cnt) {
   const TileDev t = tiles[blockIdx.x];
   if (ss[t.seg].status != kRunning) return;
   const SegDev& S = segs[t.seg];
@@ -193,66 +217,34 @@ __global__ void __launch_bounds__(kThreads) k_b_hv(const SegDev* __restrict__ se
       h[q] = hn[q];
     }
   }
-}
-
-// tile partials of <V_j|w> (mode 0) or |w|^2 (mode 1): exact products summed
-// in float-float per thread (ff.cuh), FP64 across the CTA
-__global__ void __launch_bounds__(kThreads) k_b_dot(const SegDev* __restrict__ segs, const SegState* __restrict__ ss,
-                                                    const TileDev* __restrict__ tiles, double* __restrict__ part,
-                                                    int mode) {
-  const TileDev t = tiles[blockIdx.x];
-  double a = 0, b = 0;
-  if (ss[t.seg].status == kRunning) {
-    const SegDev& S = segs[t.seg];
-    const float2* v = S.V + (int64_t)ss[t.seg].j * S.n;
-    FFAcc sr, si;
-    for (int r = threadIdx.x; r < t.rows; r += blockDim.x) {
-      const int64_t i = t.row0 + r;
-      const float2 y = S.w[i];
-      if (mode == 0) {
-        const float2 x = v[i];
-        sr.add_prod(x.x, y.x);
-        sr.add_prod(x.y, y.y);
-        si.add_prod(x.x, y.y);
-        si.sub_prod(x.y, y.x);
-      } else {
-        sr.add_prod(y.x, y.x);
-        sr.add_prod(y.y, y.y);
-      }
-    }
-    a = sr.value();
-    b = si.value();
+  __syncthreads();  // the tile's w rows are written
+  FFAcc sr, si;
+  for (int rr = threadIdx.x; rr < t.rows; rr += blockDim.x) {
+    const int64_t i = t.row0 + rr;
+    const float2 y = S.w[i], x = v[i];
+    sr.add_prod(x.x, y.x);
+    sr.add_prod(x.y, y.y);
+    si.add_prod(x.x, y.y);
+    si.sub_prod(x.y, y.x);
   }
+  double a = sr.value(), b = si.value();
   block_sum2(a, b);
   if (threadIdx.x == 0) {
     part[2 * blockIdx.x] = a;
     part[2 * blockIdx.x + 1] = b;
   }
-}
-
-// one CTA per segment sums its tiles' partials in order:
-// mode 0 -> alpha_j, mode 1 -> beta_{j+1} = sqrt, mode 2 -> aux[0] = |w|^2
-__global__ void __launch_bounds__(kThreads) k_b_finish(const SegDev* __restrict__ segs,
-                                                       const SegState* __restrict__ ss, const int* __restrict__ tb,
-                                                       const double* __restrict__ part, int mode) {
-  if (ss[blockIdx.x].status != kRunning) return;
-  const SegDev& S = segs[blockIdx.x];
-  const int j = ss[blockIdx.x].j;
-  double a = 0, b = 0;
-  for (int k = tb[blockIdx.x] + threadIdx.x; k < tb[blockIdx.x + 1]; k += blockDim.x) {
-    a += part[2 * k];
-    b += part[2 * k + 1];
-  }
-  block_sum2(a, b);
-  if (threadIdx.x == 0) {
-    if (mode == 0) S.alpha[j] = a;
-    else if (mode == 1) S.beta[j + 1] = sqrt(a);
-    else S.aux[0] = a;
+  const int k0 = tb[t.seg], k1 = tb[t.seg + 1];
+  if (last_cta(cnt + kCnts * t.seg + kCntAlpha, k1 - k0)) {
+    seg_sum(part, k0, k1, a, b);
+    if (threadIdx.x == 0) S.alpha[ss[t.seg].j] = a;
   }
 }
 
+// w -= alpha_j V_j + beta_j V_{j-1}, and |w|^2 (tile partials of the stored
+// values, closed per segment by the last CTA into aux[0])
 __global__ void __launch_bounds__(kThreads) k_b_step(const SegDev* __restrict__ segs, const SegState* __restrict__ ss,
-                                                     const TileDev* __restrict__ tiles) {
+                                                     const TileDev* __restrict__ tiles, const int* __restrict__ tb,
+                                                     double* __restrict__ part, int* __restrict__ cnt) {
   const TileDev t = tiles[blockIdx.x];
   if (ss[t.seg].status != kRunning) return;
   const SegDev& S = segs[t.seg];
@@ -260,11 +252,26 @@ __global__ void __launch_bounds__(kThreads) k_b_step(const SegDev* __restrict__ 
   const FFScalar a(S.alpha[j]), b(j > 0 ? S.beta[j] : 0.0);
   const float2* v = S.V + (int64_t)j * S.n;
   const float2* vp = j > 0 ? v - S.n : nullptr;
+  FFAcc sr;
   for (int r = threadIdx.x; r < t.rows; r += blockDim.x) {
     const int64_t i = t.row0 + r;
     const float2 y = S.w[i], x = v[i];
     const float2 p = vp ? vp[i] : make_float2(0.f, 0.f);
-    S.w[i] = make_float2(ff_axpy2(y.x, a, x.x, b, p.x), ff_axpy2(y.y, a, x.y, b, p.y));
+    const float2 o = make_float2(ff_axpy2(y.x, a, x.x, b, p.x), ff_axpy2(y.y, a, x.y, b, p.y));
+    S.w[i] = o;
+    sr.add_prod(o.x, o.x);
+    sr.add_prod(o.y, o.y);
+  }
+  double s2 = sr.value(), z = 0;
+  block_sum2(s2, z);
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = s2;
+    part[2 * blockIdx.x + 1] = 0.0;
+  }
+  const int k0 = tb[t.seg], k1 = tb[t.seg + 1];
+  if (last_cta(cnt + kCnts * t.seg + kCntNorm, k1 - k0)) {
+    seg_sum(part, k0, k1, s2, z);
+    if (threadIdx.x == 0) S.aux[0] = s2;
   }
 }
 
@@ -348,10 +355,16 @@ __global__ void __launch_bounds__(kThreads) k_b_cgs_dot(const SegDev* __restrict
 }
 
 // CTA (segment, y): q_k = sum of the segment's tile partials, k = y, y + kCgsY, ...
+// After the first pass the last of the segment's kCgsY CTAs also decides
+// whether the second pass is needed (Daniel, Gragg, Kaufman and Stewart's
+// test): the first pass removed sum |q_k|^2 from |w|^2; when that is below
+// 1e-4 |w|^2 (the norm changed by less than 0.005%) w is already orthogonal
+// to the working precision and the second pass is skipped.
 __global__ void __launch_bounds__(kThreads) k_b_cgs_finish(const SegDev* __restrict__ segs,
-                                                           const SegState* __restrict__ ss,
+                                                           SegState* __restrict__ ss,
                                                            const int* __restrict__ tb, int n_tiles,
-                                                           const double* __restrict__ part, int pass) {
+                                                           const double* __restrict__ part, int pass,
+                                                           int* __restrict__ cnt) {
   if (ss[blockIdx.x].status != kRunning || (pass == 1 && !ss[blockIdx.x].redo)) return;
   const SegDev& S = segs[blockIdx.x];
   const int K = ss[blockIdx.x].j + 1;
@@ -367,35 +380,76 @@ __global__ void __launch_bounds__(kThreads) k_b_cgs_finish(const SegDev* __restr
       S.q[2 * k + 1] = b;
     }
   }
+  if (pass == 0 && last_cta(cnt + kCnts * blockIdx.x + kCntDecide, kCgsY)) {
+    double a = 0, b = 0;
+    for (int k = threadIdx.x; k < K; k += blockDim.x) {
+      const double qr = __ldcg(S.q + 2 * k), qi = __ldcg(S.q + 2 * k + 1);
+      a += qr * qr + qi * qi;
+    }
+    block_sum2(a, b);
+    if (threadIdx.x == 0) ss[blockIdx.x].redo = a > 1e-4 * S.aux[0] ? 1 : 0;
+  }
 }
 
+// w -= sum_k q_k V_k (the first pass; the second only when decided), and
+// after the second, beta_{j+1} = |w| (tile partials of the stored values,
+// closed per segment by the last CTA)
 __global__ void __launch_bounds__(kThreads) k_b_cgs_sub(const SegDev* __restrict__ segs,
                                                         const SegState* __restrict__ ss,
-                                                        const TileDev* __restrict__ tiles, int pass) {
+                                                        const TileDev* __restrict__ tiles, int pass,
+                                                        const int* __restrict__ tb, double* __restrict__ part,
+                                                        int* __restrict__ cnt) {
   const TileDev t = tiles[blockIdx.x];
-  if (ss[t.seg].status != kRunning || (pass == 1 && !ss[t.seg].redo)) return;
+  if (ss[t.seg].status != kRunning) return;
+  const bool sub = pass == 0 || ss[t.seg].redo;
+  if (!sub && pass == 0) return;
   const SegDev& S = segs[t.seg];
   __shared__ float sq[2 * (kMaxSteps + 1)];
   const int K = ss[t.seg].j + 1;
-  for (int k = threadIdx.x; k < 2 * K; k += blockDim.x) sq[k] = (float)S.q[k];
-  __syncthreads();
+  if (sub) {
+    for (int k = threadIdx.x; k < 2 * K; k += blockDim.x) sq[k] = (float)S.q[k];
+    __syncthreads();
+  }
   // FP32: the q_k are tiny against |w| once the vectors are nearly orthogonal
+  FFAcc sr;
   for (int r = threadIdx.x; r < t.rows; r += blockDim.x) {
     const int64_t i = t.row0 + r;
     const float2 y = S.w[i];
     float re = y.x, im = y.y;
-    for (int k = 0; k < K; ++k) {
-      const float2 x = S.V[(int64_t)k * S.n + i];
-      re = fmaf(-sq[2 * k], x.x, fmaf(sq[2 * k + 1], x.y, re));
-      im = fmaf(-sq[2 * k], x.y, fmaf(-sq[2 * k + 1], x.x, im));
+    if (sub) {
+      for (int k = 0; k < K; ++k) {
+        const float2 x = S.V[(int64_t)k * S.n + i];
+        re = fmaf(-sq[2 * k], x.x, fmaf(sq[2 * k + 1], x.y, re));
+        im = fmaf(-sq[2 * k], x.y, fmaf(-sq[2 * k + 1], x.x, im));
+      }
+      S.w[i] = make_float2(re, im);
     }
-    S.w[i] = make_float2(re, im);
+    if (pass == 1) {
+      sr.add_prod(re, re);
+      sr.add_prod(im, im);
+    }
+  }
+  if (pass == 0) return;
+  double s2 = sr.value(), z = 0;
+  block_sum2(s2, z);
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = s2;
+    part[2 * blockIdx.x + 1] = 0.0;
+  }
+  const int k0 = tb[t.seg], k1 = tb[t.seg + 1];
+  if (last_cta(cnt + kCnts * t.seg + kCntBeta, k1 - k0)) {
+    seg_sum(part, k0, k1, s2, z);
+    if (threadIdx.x == 0) S.beta[ss[t.seg].j + 1] = sqrt(s2);
   }
 }
 
-__global__ void __launch_bounds__(kThreads) k_b_scale(const SegDev* __restrict__ segs,
-                                                      const SegState* __restrict__ ss,
-                                                      const TileDev* __restrict__ tiles) {
+// V_{j+1} = w / beta_{j+1} and u_{j+1} = V_{j+1} / norm for the next H*v;
+// then the segment's last CTA advances j and, every check_every steps, tests
+// convergence: the wanted lowest Ritz pairs of T_j (bisection and inverse
+// iteration in FP64) and their residual bounds beta_j |y_k[j-1]|.
+__global__ void __launch_bounds__(kThreads) k_b_scale(const SegDev* __restrict__ segs, SegState* __restrict__ ss,
+                                                      const TileDev* __restrict__ tiles, const int* __restrict__ tb,
+                                                      int* __restrict__ cnt) {
   const TileDev t = tiles[blockIdx.x];
   if (ss[t.seg].status != kRunning) return;
   const SegDev& S = segs[t.seg];
@@ -405,60 +459,41 @@ __global__ void __launch_bounds__(kThreads) k_b_scale(const SegDev* __restrict__
   for (int r = threadIdx.x; r < t.rows; r += blockDim.x) {
     const int64_t i = t.row0 + r;
     const float2 y = S.w[i];
-    vn[i] = make_float2(fmaf(y.x, s.l, __fmul_rn(y.x, s.h)), fmaf(y.y, s.l, __fmul_rn(y.y, s.h)));
+    const float2 x = make_float2(fmaf(y.x, s.l, __fmul_rn(y.x, s.h)), fmaf(y.y, s.l, __fmul_rn(y.y, s.h)));
+    vn[i] = x;
+    const float ni = (float)S.nrm_inv[S.lid[i]];
+    S.u[i] = make_float2(x.x * ni, x.y * ni);
   }
-}
-
-// Whether the second Gram-Schmidt pass is needed (Daniel, Gragg, Kaufman and
-// Stewart's test): the first pass removed sum |q_k|^2 from |w|^2; when that
-// is below 1e-4 |w|^2 (the norm changed by less than 0.005%) w is already
-// orthogonal to the working precision and the second pass is skipped.
-__global__ void __launch_bounds__(kThreads) k_b_cgs_decide(const SegDev* __restrict__ segs,
-                                                           SegState* __restrict__ ss) {
-  if (ss[blockIdx.x].status != kRunning) return;
-  const SegDev& S = segs[blockIdx.x];
-  const int K = ss[blockIdx.x].j + 1;
-  double a = 0, b = 0;
-  for (int k = threadIdx.x; k < K; k += blockDim.x) a += S.q[2 * k] * S.q[2 * k] + S.q[2 * k + 1] * S.q[2 * k + 1];
-  block_sum2(a, b);
-  if (threadIdx.x == 0) ss[blockIdx.x].redo = a > 1e-4 * S.aux[0] ? 1 : 0;
-}
-
-__global__ void k_b_advance(const SegDev* __restrict__ segs, SegState* __restrict__ ss, int n_seg) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s < n_seg && ss[s].status == kRunning) {
-    ss[s].j += 1;
-    if (ss[s].j >= segs[s].m_max) ss[s].status = kMaxedOut;
-  }
-}
-
-// Convergence test, one CTA per segment, every check_every steps: the wanted
-// lowest Ritz pairs of T_j and their residual bounds beta_j |y_k[j-1]|.
-__global__ void __launch_bounds__(128) k_b_check(const SegDev* __restrict__ segs, SegState* __restrict__ ss) {
-  const SegDev& S = segs[blockIdx.x];
-  const int j = ss[blockIdx.x].j;
-  if (ss[blockIdx.x].status != kRunning || S.tol <= 0 || j % S.check_every != 0 || j < 2 * S.want + 2) return;
-  __shared__ double d[kMaxSteps + 1], e[kMaxSteps + 1];
+  if (!last_cta(cnt + kCnts * t.seg + kCntAdvance, tb[t.seg + 1] - tb[t.seg])) return;
   __shared__ int ok;
-  for (int i = threadIdx.x; i < j; i += blockDim.x) {
-    d[i] = S.alpha[i];
-    e[i] = i > 0 ? S.beta[i] : 0.0;
+  __shared__ double d[kMaxSteps + 1], e[kMaxSteps + 1];
+  const int jn = j + 1;
+  if (threadIdx.x == 0) {
+    ok = 1;
+    ss[t.seg].j = jn;
+    if (jn >= S.m_max) ss[t.seg].status = kMaxedOut;
   }
-  if (threadIdx.x == 0) ok = 1;
+  __syncthreads();
+  if (jn >= S.m_max || S.tol <= 0 || jn % S.check_every != 0 || jn < 2 * S.want + 2) return;
+  for (int i = threadIdx.x; i < jn; i += blockDim.x) {
+    d[i] = __ldcg(S.alpha + i);
+    e[i] = i > 0 ? __ldcg(S.beta + i) : 0.0;
+  }
   __syncthreads();
   for (int k = threadIdx.x; k < S.want; k += blockDim.x) {
-    const double th = tridiag_eigenvalue(d, e, j, k);
+    const double th = tridiag_eigenvalue(d, e, jn, k);
     double* y = S.ywork + (int64_t)k * 6 * S.m_max;
-    tridiag_eigenvector(d, e, j, th, y, y + S.m_max);
-    if (S.beta[j] * fabs(y[j - 1]) > S.tol * fmax(1.0, fabs(th))) ok = 0;
+    tridiag_eigenvector(d, e, jn, th, y, y + S.m_max);
+    if (__ldcg(S.beta + jn) * fabs(y[jn - 1]) > S.tol * fmax(1.0, fabs(th))) ok = 0;
   }
   __syncthreads();
-  if (threadIdx.x == 0 && ok) ss[blockIdx.x].status = kConverged;
+  if (threadIdx.x == 0 && ok) ss[t.seg].status = kConverged;
 }
 
-// start vector V_0 = x / |x| of one segment (one CTA)
+// start vector V_0 = x / |x| of one segment (one CTA), and u_0 = V_0 / norm
 __global__ void __launch_bounds__(kThreads) k_b_start(float2* __restrict__ V0, const float2* __restrict__ x,
-                                                      int64_t n) {
+                                                      int64_t n, const double* __restrict__ nrm_inv,
+                                                      const uint8_t* __restrict__ lid, float2* __restrict__ u) {
   FFAcc s;
   for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
     s.add_prod(x[i].x, x[i].x);
@@ -467,8 +502,13 @@ __global__ void __launch_bounds__(kThreads) k_b_start(float2* __restrict__ V0, c
   double a = s.value(), b = 0;
   block_sum2(a, b);
   const FFScalar inv(1.0 / sqrt(a));
-  for (int64_t i = threadIdx.x; i < n; i += blockDim.x)
-    V0[i] = make_float2(fmaf(x[i].x, inv.l, __fmul_rn(x[i].x, inv.h)), fmaf(x[i].y, inv.l, __fmul_rn(x[i].y, inv.h)));
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    const float2 v = make_float2(fmaf(x[i].x, inv.l, __fmul_rn(x[i].x, inv.h)),
+                                 fmaf(x[i].y, inv.l, __fmul_rn(x[i].y, inv.h)));
+    V0[i] = v;
+    const float ni = (float)nrm_inv[lid[i]];
+    u[i] = make_float2(v.x * ni, v.y * ni);
+  }
 }
 
 struct Segment {
@@ -496,6 +536,7 @@ struct Batch {
   cudaStream_t st = nullptr;
   SegDev* d_segs = nullptr;
   SegState* d_state = nullptr;
+  int* d_cnt = nullptr;  // kCnts ticket counters per segment (fused reductions)
   TileDev* d_tiles = nullptr;
   int* d_tb = nullptr;
   double* d_part = nullptr;
@@ -518,6 +559,7 @@ struct Batch {
     for (Segment& g : segs) release(g);
     cudaFree(d_segs);
     cudaFree(d_state);
+    cudaFree(d_cnt);
     cudaFree(d_tiles);
     cudaFree(d_tb);
     cudaFree(d_part);
@@ -700,10 +742,12 @@ int rebuild(Batch& B) {
   tb.push_back((int)tiles.size());
   cudaFree(B.d_segs);
   cudaFree(B.d_state);
+  cudaFree(B.d_cnt);
   cudaFree(B.d_tiles);
   cudaFree(B.d_tb);
   B.d_segs = nullptr;
   B.d_state = nullptr;
+  B.d_cnt = nullptr;
   B.d_tiles = nullptr;
   B.d_tb = nullptr;
   B.n_tiles = (int)tiles.size();
@@ -720,6 +764,7 @@ int rebuild(Batch& B) {
   }
   if (cudaMalloc(&B.d_segs, sizeof(SegDev) * sd.size()) != cudaSuccess ||
       cudaMalloc(&B.d_state, sizeof(SegState) * ss.size()) != cudaSuccess ||
+      cudaMalloc(&B.d_cnt, sizeof(int) * kCnts * sd.size()) != cudaSuccess ||
       cudaMalloc(&B.d_tiles, sizeof(TileDev) * tiles.size()) != cudaSuccess ||
       cudaMalloc(&B.d_tb, sizeof(int) * tb.size()) != cudaSuccess)
     return EDG_ERR_NOMEM;
@@ -727,31 +772,27 @@ int rebuild(Batch& B) {
   cudaMemcpyAsync(B.d_state, ss.data(), sizeof(SegState) * ss.size(), cudaMemcpyHostToDevice, B.st);
   cudaMemcpyAsync(B.d_tiles, tiles.data(), sizeof(TileDev) * tiles.size(), cudaMemcpyHostToDevice, B.st);
   cudaMemcpyAsync(B.d_tb, tb.data(), sizeof(int) * tb.size(), cudaMemcpyHostToDevice, B.st);
+  cudaMemsetAsync(B.d_cnt, 0, sizeof(int) * kCnts * sd.size(), B.st);
   if (cudaStreamSynchronize(B.st) != cudaSuccess) return EDG_ERR_CUDA;  // the host vectors go out of scope
   B.n_dev = (int)sd.size();
   const int nt = B.n_tiles, ns = B.n_dev, lpr = B.opts.lanes_per_row;
   cudaGraph_t g;
   if (cudaStreamBeginCapture(B.st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return EDG_ERR_CUDA;
-  k_b_u<<<nt, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles);
-  if (lpr == 8) k_b_hv<8><<<nt, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles);
-  else if (lpr == 32) k_b_hv<32><<<nt, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles);
-  else k_b_hv<16><<<nt, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles);
-  k_b_dot<<<nt, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles, B.d_part, 0);
-  k_b_finish<<<ns, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tb, B.d_part, 0);
-  k_b_step<<<nt, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles);
-  k_b_dot<<<nt, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles, B.d_part, 1);
-  k_b_finish<<<ns, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tb, B.d_part, 2);
+  // one step, nine kernels: H*v and alpha; the three-term update and |w|^2;
+  // two classical Gram-Schmidt passes (tile dots, per-segment sums with the
+  // second-pass decision, subtraction; the second pass ends with beta);
+  // V_{j+1}, u_{j+1}, the step counter and the convergence test
+  int* cnt = B.d_cnt;
+  if (lpr == 8) k_b_hv<8><<<nt, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles, B.d_tb, B.d_part, cnt);
+  else if (lpr == 32) k_b_hv<32><<<nt, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles, B.d_tb, B.d_part, cnt);
+  else k_b_hv<16><<<nt, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles, B.d_tb, B.d_part, cnt);
+  k_b_step<<<nt, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles, B.d_tb, B.d_part, cnt);
   for (int pass = 0; pass < 2; ++pass) {
     k_b_cgs_dot<<<dim3(nt, kCgsY), kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles, nt, B.d_part, pass);
-    k_b_cgs_finish<<<dim3(ns, kCgsY), kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tb, nt, B.d_part, pass);
-    k_b_cgs_sub<<<nt, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles, pass);
-    if (pass == 0) k_b_cgs_decide<<<ns, kThreads, 0, B.st>>>(B.d_segs, B.d_state);
+    k_b_cgs_finish<<<dim3(ns, kCgsY), kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tb, nt, B.d_part, pass, cnt);
+    k_b_cgs_sub<<<nt, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles, pass, B.d_tb, B.d_part, cnt);
   }
-  k_b_dot<<<nt, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles, B.d_part, 1);
-  k_b_finish<<<ns, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tb, B.d_part, 1);
-  k_b_scale<<<nt, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles);
-  k_b_advance<<<(ns + 127) / 128, 128, 0, B.st>>>(B.d_segs, B.d_state, ns);
-  k_b_check<<<ns, 128, 0, B.st>>>(B.d_segs, B.d_state);
+  k_b_scale<<<nt, kThreads, 0, B.st>>>(B.d_segs, B.d_state, B.d_tiles, B.d_tb, cnt);
   cudaError_t e = cudaStreamEndCapture(B.st, &g);
   if (e != cudaSuccess) return EDG_ERR_CUDA;
   e = cudaGraphInstantiate(&B.graph, g, 0);
@@ -865,7 +906,7 @@ int edg_batch_add(edg_batch* bh, edg_sector* sec, const edg_batch_request* req) 
     release(g);
     return rc;
   }
-  k_b_start<<<1, kThreads, 0, B.st>>>(d.V, d.w, n);
+  k_b_start<<<1, kThreads, 0, B.st>>>(d.V, d.w, n, d.nrm_inv, d.lid, d.u);
   cudaMemsetAsync(d.beta, 0, sizeof(double) * (m + 2), B.st);
   if ((e = cudaGetLastError()) != cudaSuccess) {
     release(g);
@@ -900,6 +941,65 @@ int edg_batch_step(edg_batch* bh, int n_steps) {
   }
   if (rc == EDG_OK) rc = settle(B);
   return rc;
+}
+
+int edg_batch_tune(edg_batch* bh, int steps, int* tile_rows, int* lanes_per_row, double* ms) {
+  if (!bh || steps < 1) return fail(EDG_ERR_INVALID, "edg_batch_tune: NULL batch or steps < 1");
+  Batch& B = bh->b;
+  if (B.segs.empty()) return fail(EDG_ERR_INVALID, "edg_batch_tune: add the segments first");
+  for (const Segment& g : B.segs)
+    if (g.st.j != 0 || g.st.status != kRunning || g.cancelled)
+      return fail(EDG_ERR_INVALID, "edg_batch_tune: tune before the first step");
+  static const int kTiles[4] = {256, 1024, 4096, 16384}, kLanes[2] = {8, 16};
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const edg_batch_opts keep = B.opts;
+  float best = 1e30f;
+  int bt = keep.tile_rows, bl = keep.lanes_per_row, rc = EDG_OK;
+  for (int ti = 0; ti < 4 && rc == EDG_OK; ++ti)
+    for (int li = 0; li < 2 && rc == EDG_OK; ++li) {
+      B.opts.tile_rows = kTiles[ti];
+      B.opts.lanes_per_row = kLanes[li];
+      if ((rc = rebuild(B)) != EDG_OK) break;
+      cudaGraphLaunch(B.graph, B.st);  // warm-up step
+      cudaEventRecord(e0, B.st);
+      for (int k = 0; k < steps; ++k) cudaGraphLaunch(B.graph, B.st);
+      cudaEventRecord(e1, B.st);
+      const cudaError_t ce = cudaEventSynchronize(e1);
+      float t = 0;
+      cudaEventElapsedTime(&t, e0, e1);
+      if (ce != cudaSuccess) rc = cuda_fail(ce, "edg_batch_tune");
+      if (ms) ms[ti * 2 + li] = t / steps;
+      if (t < best) {
+        best = t;
+        bt = kTiles[ti];
+        bl = kLanes[li];
+      }
+      // back to the segments' start: seeded start vectors, step 0
+      for (Segment& g : B.segs) {
+        if (rc == EDG_OK) rc = edg_fill_random(g.d.w, g.d.n, EDG_C64, g.req.seed, B.st);
+        k_b_start<<<1, kThreads, 0, B.st>>>(g.d.V, g.d.w, g.d.n, g.d.nrm_inv, g.d.lid, g.d.u);
+        cudaMemsetAsync(g.d.beta, 0, sizeof(double) * (g.d.m_max + 2), B.st);
+        g.st = SegState{};
+        g.st.status = kRunning;
+      }
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  B.opts = keep;
+  if (rc == EDG_OK) {
+    B.opts.tile_rows = bt;
+    B.opts.lanes_per_row = bl;
+  }
+  const cudaError_t ce = cudaStreamSynchronize(B.st);
+  if (rc == EDG_OK && ce != cudaSuccess) rc = cuda_fail(ce, "edg_batch_tune");
+  // the device tables and step counters from the reset host states
+  if (rc == EDG_OK && (rc = rebuild(B)) != EDG_OK) rc = fail(rc, "edg_batch_tune: rebuilding the step graph");
+  if (rc != EDG_OK) return rc;
+  if (tile_rows) *tile_rows = bt;
+  if (lanes_per_row) *lanes_per_row = bl;
+  return EDG_OK;
 }
 
 int edg_batch_cancel(edg_batch* bh, int64_t tag) {

@@ -139,11 +139,14 @@ class Server:
     FP64 Rayleigh quotients 1e-6 gives eigenvalues within about 1e-10
     relative of the FP64 ones for these models (checked by the tests).
     build_ahead: build admitted requests' sectors on a builder thread while
-    the batch steps (False: build them in the loop)."""
+    the batch steps (False: build them in the loop).  tune: before the first
+    step, time the batch's tile sizes and lanes per row on the requests
+    admitted first (edg_batch_tune) and keep the fastest; ``tuned`` then
+    holds the choice (otherwise tile_rows and lanes_per_row stay)."""
 
     def __init__(self, hbm_budget: Optional[int] = None, max_iterations: int = 300, res_tol: float = 1e-6,
                  tile_rows: int = 4096, lanes_per_row: int = 8, check_every: int = 10, max_active: int = 4096,
-                 build_ahead: bool = True):
+                 build_ahead: bool = True, tune: bool = True):
         if hbm_budget is None:
             import torch
 
@@ -155,6 +158,8 @@ class Server:
         self.check_every = int(check_every)
         self.max_active = int(max_active)
         self.build_ahead = bool(build_ahead)
+        self.tune = bool(tune)
+        self.tuned: Optional[dict] = None
         self.batch = BatchSolver(tile_rows=tile_rows, lanes_per_row=lanes_per_row, check_every=check_every)
         self.peak_live = 0
         self.peak_bytes = 0
@@ -297,6 +302,8 @@ class Server:
                     self.peak_live = max(self.peak_live, len(live))
                     self.peak_bytes = max(self.peak_bytes, used)
                 if live:
+                    if self.tune and self.tuned is None:
+                        self.tuned = self.batch.tune()
                     self.batch.step(self.check_every)
                     for r in self.batch.poll():
                         req, sec, need, adm = live.pop(r["tag"])

@@ -63,11 +63,13 @@ def sector_list(spec: L.TorusSpec, Sz: Optional[float] = None):
 
 def sweep(spec: L.TorusSpec, Sz: Optional[float] = None, n_ev: int = 4, max_iterations: int = 300,
           res_tol: float = 1e-6, hbm_budget: Optional[int] = None, seed: int = 1,
-          distributed: bool = False) -> List[Level]:
+          distributed: bool = False, tune: bool = True) -> List[Level]:
     """Lowest levels of every sector, sorted as the reference sorts them.
 
     distributed: with a process group up (one rank per GPU), each rank solves
-    every world-th sector and the levels are collected on every rank."""
+    every world-th sector and the levels are collected on every rank.
+    tune: pick the batch's tile size and lanes per row with the library's
+    autotuner (edg_batch_tune) on each group of sectors before it runs."""
     if hbm_budget is None:
         import torch
 
@@ -80,6 +82,8 @@ def sweep(spec: L.TorusSpec, Sz: Optional[float] = None, n_ev: int = 4, max_iter
 
     def drain():
         nonlocal used
+        if tune and live:
+            batch.tune()
         for r in batch.run():
             sec, meta, need = live.pop(r["tag"])
             N.check(r["status"])

@@ -289,6 +289,15 @@ int edg_batch_add(edg_batch* b, edg_sector* s, const edg_batch_request* req);
 /* Run up to n_steps steps of every live segment (fewer when none is left);
  * segments that stop are finished before this returns or at the next call. */
 int edg_batch_step(edg_batch* b, int n_steps);
+/* Autotuner of the batch kernels: times `steps` steps of the segments added so
+ * far (before the batch's first step) for tiles of 256, 1024, 4096 and 16384
+ * rows with 8 and 16 lanes per stored row, keeps the fastest for the rest of
+ * the batch and returns it (NULL allowed); ms (NULL allowed) receives the 8
+ * trial times per step, tiles major.  The segments are then put back at their
+ * seeded start, so the results are those of an untuned batch created with the
+ * chosen options.  A segment's arithmetic depends on the tile size and the
+ * lanes per row (the order of its sums), not on the other segments. */
+int edg_batch_tune(edg_batch* b, int steps, int* tile_rows, int* lanes_per_row, double* ms);
 /* Withdraw the live segment with this tag: its memory is released now and its
  * result (status EDG_ERR_CANCELLED, no levels) comes back through
  * edg_batch_poll.  The other segments' arithmetic is unchanged.

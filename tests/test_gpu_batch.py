@@ -152,3 +152,29 @@ def test_cancel_releases_a_segment_and_leaves_the_others(mods):
     assert res[0]["status"] == 0 and np.array_equal(res[0]["eigs"], alone["eigs"])
     with pytest.raises(Exception):
         B2.cancel(5)
+
+
+def test_tuner_keeps_results_of_an_untuned_batch(mods):
+    """edg_batch_tune times the tile and lane choices on the segments, then
+    puts them back at their start: the tuned batch returns the bits of a
+    fresh batch created with the chosen options."""
+    batch, sector = mods
+    secs = [stored_sector(sector, n, i) for n, i, _ in CASES[:6]]
+    B = batch.BatchSolver()
+    for k, sec in enumerate(secs):
+        B.add(sec, n_ev=2, max_iterations=100, tol=0.0, seed=3 + k, tag=k)
+    choice = B.tune(steps=2)
+    assert choice["tile_rows"] in (256, 1024, 4096, 16384) and choice["lanes_per_row"] in (8, 16)
+    assert len(choice["ms_per_step"]) == 8 and all(v > 0 for v in choice["ms_per_step"].values())
+    tuned = {r["tag"]: r for r in B.run()}
+    B2 = batch.BatchSolver(tile_rows=choice["tile_rows"], lanes_per_row=choice["lanes_per_row"])
+    for k, sec in enumerate(secs):
+        B2.add(sec, n_ev=2, max_iterations=100, tol=0.0, seed=3 + k, tag=k)
+    fresh = {r["tag"]: r for r in B2.run()}
+    for k in range(len(secs)):
+        assert np.array_equal(tuned[k]["eigs"], fresh[k]["eigs"]), k
+    B3 = batch.BatchSolver()
+    B3.add(secs[0], n_ev=2, max_iterations=100, tol=0.0, seed=3, tag=0)
+    B3.step(1)
+    with pytest.raises(Exception):
+        B3.tune()

@@ -23,12 +23,19 @@ def stream(mods):
 TILE = 4096  # rows per tile: a segment's sums depend on it, so alone and mixed share it
 
 
+TUNED = {}
+
+
 @pytest.fixture(scope="module")
 def served(mods, stream):
+    """The stream through the loop with the library's tuner choosing the
+    batch's tiles; the alone runs below reuse its choice."""
     serving = mods[3]
-    srv = serving.Server(max_iterations=300, res_tol=1e-6, tile_rows=TILE)
+    srv = serving.Server(max_iterations=300, res_tol=1e-6)
     out = srv.run(stream)
     srv.close()
+    assert srv.tuned and srv.tuned["tile_rows"] in (256, 1024, 4096, 16384)
+    TUNED.update(srv.tuned)
     return {s.rid: s for s in out}
 
 
@@ -47,7 +54,7 @@ def test_alone_equals_in_mix(served, stream, mods):
     for req in stream[:4]:
         sec = sector.GpuSector(lattice.make_model(req.spec, req.Sz, req.kx, req.ky))
         assert sec.build_targets()
-        B = batch.BatchSolver(tile_rows=TILE, lanes_per_row=8, check_every=10)
+        B = batch.BatchSolver(tile_rows=TUNED["tile_rows"], lanes_per_row=TUNED["lanes_per_row"], check_every=10)
         B.add(sec, n_ev=req.n_ev, max_iterations=min(300, sec.n_p), tol=1e-6, seed=1 + req.rid, tag=req.rid)
         alone = B.run()[0]
         mixed = served[req.rid]
@@ -88,7 +95,8 @@ def test_bad_requests_are_reported_and_the_rest_unchanged(served, stream, mods):
     serving = mods[3]
     bad = serving.Request(900, stream[2].arrival, serving.L.TorusSpec("square", 5, 4), 0.0, 9, 0, 1)  # kx >= Lx
     extra = serving.Request(901, stream[3].arrival, stream[3].spec, stream[3].Sz, stream[3].kx, stream[3].ky, 1)
-    srv = serving.Server(max_iterations=300, res_tol=1e-6, tile_rows=TILE)
+    srv = serving.Server(max_iterations=300, res_tol=1e-6, tile_rows=TUNED["tile_rows"],
+                         lanes_per_row=TUNED["lanes_per_row"], tune=False)
     srv.cancel(901)  # withdrawn before it arrives
     out = {s.rid: s for s in srv.run(list(stream) + [bad, extra])}
     srv.close()

@@ -102,6 +102,10 @@ def _fake_batch(clock, log):
             for k in self.left:
                 self.left[k] -= 1
 
+        def tune(self, steps=3):
+            log.append(("tune", len(self.left)))
+            return {"tile_rows": 1024, "lanes_per_row": 8, "ms_per_step": {}}
+
         def cancel(self, tag):
             self.left[tag] = 0  # reported by the next poll
             self.cancelled.add(tag)
@@ -236,3 +240,11 @@ def test_cancel_queued_and_running_requests(monkeypatch):
         if rid not in (late, holder["running"]):
             assert s.ok and np.array_equal(s.eigs, ref_by[rid].eigs)
     assert serving.summarize(out)["cancelled"] == 2
+
+
+def test_batch_is_tuned_once_before_its_first_step(monkeypatch):
+    reqs = serving.make_stream(10, rate=40.0, seed=13, sizes=(20,))
+    srv, out, log = _run(monkeypatch, reqs, budget=1 << 50)
+    tunes = [i for i, e in enumerate(log) if e[0] == "tune"]
+    assert len(tunes) == 1 and tunes[0] > 0 and log[tunes[0]][1] >= 1
+    assert srv.tuned["tile_rows"] == 1024 and len(out) == len(reqs)
