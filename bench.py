@@ -201,6 +201,62 @@ def cpu_sample_rate(model, reps, lid, budget_s: float, threads: int, seed: int =
     return len(rows) / dt / n_p, len(rows), dt
 
 
+def cpu_sector_baselines(args, threads):
+    """The reference's sHv row formula with its per-configuration tables (the
+    oracle's table-mode restatement, oracle/time_reference.py shows it against
+    the reference's own sHv) beside this library's H*v on the same sectors:
+    config 1, a 28-site serving-size sector and one of config 2's 30-site
+    sectors.  CPU on all host threads and on one; GPU in FP64 and FP32."""
+    import torch
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from time_reference import SECTORS
+
+    from ed_code_gb300 import lattice as L
+    from ed_code_gb300.sector import GpuSector, fill_random
+
+    out = []
+    for name, kw, (Sz, kx, ky) in SECTORS:
+        if args.cpu_sectors != "all" and name not in args.cpu_sectors.split(","):
+            continue
+        model = L.make_model(L.TorusSpec(**kw), Sz, kx, ky)
+        sec = GpuSector(model)
+        sec.build_targets()
+        sec.tune(0)
+        st = torch.cuda.Stream()
+        gpu = {}
+        for dt, tag in ((torch.complex128, "fp64"), (torch.complex64, "fp32")):
+            v = torch.empty(sec.n_p, dtype=dt, device="cuda")
+            w = torch.empty_like(v)
+            fill_random(v, 5, st)
+            reps = max(10, min(1000, int(5e7 // sec.n_p)))
+            with torch.cuda.stream(st):
+                for _ in range(3):
+                    sec.hv(v, w, st)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(st)
+                for _ in range(reps):
+                    sec.hv(v, w, st)
+                e1.record(st)
+            torch.cuda.synchronize()
+            gpu[tag] = e0.elapsed_time(e1) / reps
+        n_p = sec.n_p
+        sec.close()
+        t0 = time.perf_counter()
+        S = O.OracleSector(model)
+        t_tables = time.perf_counter() - t0
+        vh = O.splitmix_vector(S.n_p, 5)
+        all_s = S.time_hv(vh, threads)
+        one_s = S.time_hv(vh, 1, 0.1)
+        del S
+        out.append({"sector": name, "n_p": n_p, "cpu_ms_all_threads": round(all_s * 1e3, 4),
+                    "cpu_ms_1_thread": round(one_s * 1e3, 4), "cpu_tables_seconds": round(t_tables, 2),
+                    "gpu_ms_fp64": round(gpu["fp64"], 4), "gpu_ms_fp32": round(gpu["fp32"], 4),
+                    "gpu_fp64_over_cpu_all_threads": round(all_s * 1e3 / gpu["fp64"], 1)})
+    return out
+
+
 def run_reference(args, world, rank):
     """The reference's algorithm on the host cores: the sHv row formula with
     the orbit walk of representative_p per target (the oracle's restatement;
@@ -373,7 +429,13 @@ def run_device(args, world, rank, local_rank):
         rate, n_rows, dt = cpu_sample_rate(model, states, lid, args.cpu_seconds, threads)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{n_rows} random rows of the {sec.n_p}-row sector in {dt:.1f} s, scaled to one H*v "
-                         "(oracle row formula in FP64: orbit walk + binary search per target)"}
+                         "(oracle row formula in FP64: orbit walk + binary search per target; the reference's "
+                         "own tables need ~217 GB at 36 sites)"}
+        if args.cpu_sectors != "none":
+            cpu["per_sector"] = cpu_sector_baselines(args, threads)
+            cpu["per_sector_kind"] = ("port: the reference's table-mode sHv row formula (oracle), full H*v per "
+                                      "call; profiles/cpu_reference_shv.md times it against the reference's own "
+                                      "sHv on the same sectors")
 
     peak, peak_kind = measured_peak_hbm()
     achieved = B / (ms_step / 1e3) / 1e9
@@ -528,23 +590,13 @@ def run_batch(args):
         t_create += time.perf_counter() - tb
     torch.cuda.synchronize()
     t_build = time.perf_counter() - t0
-    # autotune the tiles on a few steps of the whole batch
-    trials = {}
-    for rows in (256, 1024, 4096):
-        for lpr in (8, 16):
-            B = BatchSolver(tile_rows=rows, lanes_per_row=lpr)
-            for k, sec in enumerate(secs):
-                B.add(sec, n_ev=3, max_iterations=150, tol=0.0, seed=2, tag=k)
-            B.step(3)
-            t1 = time.perf_counter()
-            B.step(10)
-            trials[(rows, lpr)] = (time.perf_counter() - t1) / 10
-            B.close()
-    best = min(trials, key=trials.get)
-    B = BatchSolver(tile_rows=best[0], lanes_per_row=best[1])
+    # the library's autotuner picks the tiles on a few steps of the whole batch
+    B = BatchSolver()
     t1 = time.perf_counter()
     for k, sec in enumerate(secs):
         B.add(sec, n_ev=3, max_iterations=150, tol=0.0, seed=2, tag=k)
+    choice = B.tune(steps=5)
+    t_tune = time.perf_counter() - t1
     res = {r["tag"]: r for r in B.run(chunk=10)}
     t_solve = time.perf_counter() - t1
     timers = B.timers()
@@ -561,8 +613,7 @@ def run_batch(args):
            "dims": [int(min(s.n_p for s in secs)), int(max(s.n_p for s in secs))],
            "solve_seconds": t_solve, "build_seconds": t_build, "batch_timers": timers,
            "build_split": {"term_lists": t_model, "sector_and_rows": t_create}, "e2e_solves_per_s": n / (t_solve + t_build),
-           "tiles": {"tile_rows": best[0], "lanes_per_row": best[1],
-                     "ms_per_step": {f"{r}x{l}": round(1e3 * v, 3) for (r, l), v in sorted(trials.items())}},
+           "tiles": choice, "tune_seconds": t_tune,
            "max_rel_err_vs_plain_fp64": max(errs), "checked": len(errs),
            "plain_fp64_seconds_per_sector": float(np.mean(pt)),
            "speedup_vs_sequential_plain": float(np.mean(pt)) * n / t_solve,
@@ -681,6 +732,8 @@ def main():
     ap.add_argument("--rows", default=None,
                     help="LANES,POLICY[,CTAS_PER_SM[,PIPELINED]]: fix the stored-row kernel instead of timing it")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--cpu-sectors", default="all",
+                    help="CPU-baseline sectors timed beside the GPU: all, none, or names from oracle/time_reference.py")
     ap.add_argument("--ref-step-seconds", type=float, default=4.0)
     ap.add_argument("--mode", choices=["hv", "serve", "batch", "precision", "solve36"], default="hv",
                     help="hv: the headline H*v line; the others time the solver configurations")

@@ -394,6 +394,16 @@ static double complex hv_row(const or_lookup *L, int64_t idi, double norm_i, dou
 }
 
 /* sHv, 2-D (H_v.cpp:192-357), with the reference's tables. */
+/* Threads of the OpenMP loops that take no thread count (table-mode H*v,
+ * basis build); 0 or less leaves the runtime's default. */
+void or_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
+
 void or_hv_tables(const or_basis *b, const double *v, double *w, double lambda, const or_bond *bonds, int nb,
                   double Ch, const or_tri *tris, int nt, double ChCh, const or_bowtie *bows, int nbw) {
   or_lookup L;

@@ -55,6 +55,7 @@ int64_t or_sector_dim3(int n_sites, int n_ones, const int *T1, const int *T2, co
 void or_free_basis(or_basis *b);
 
 /* w = H v with the reference's tables (sHv, H_v.cpp:192-357).  v, w interleaved re/im. */
+void or_set_threads(int n);
 void or_hv_tables(const or_basis *b, const double *v, double *w, double lambda, const or_bond *bonds, int nb,
                   double Ch, const or_tri *tris, int nt, double ChCh, const or_bowtie *bows, int nbw);
 

@@ -89,6 +89,7 @@ def lib() -> C.CDLL:
         L.or_sample_reps.restype = C.c_int64
         L.or_value_vector.argtypes = [C.c_void_p, C.c_int64, C.c_uint64, C.c_void_p]
         L.or_free.argtypes = [C.c_void_p]
+        L.or_set_threads.argtypes = [C.c_int]
         L.or_n_choose_k.argtypes = [C.c_int, C.c_int]
         L.or_n_choose_k.restype = C.c_int64
         _lib = L
@@ -158,6 +159,25 @@ class OracleSector:
         lib().or_hv_tables(self._p, v.ctypes.data, w.ctypes.data, m.Jz, t.bonds, t.nb, m.Ch, t.tris, t.nt, m.ChCh,
                            t.bows, t.nbw)
         return w
+
+    def time_hv(self, v: np.ndarray, threads: int, min_seconds: float = 0.3):
+        """Seconds per table-mode H*v (the reference's sHv row formula with its
+        rep_loc/state_ph tables) on `threads` OpenMP threads, averaged over
+        repeated calls until min_seconds have passed."""
+        import time
+
+        lib().or_set_threads(int(threads))
+        try:
+            self.hv(v)  # warm
+            n, t0 = 0, time.perf_counter()
+            while True:
+                self.hv(v)
+                n += 1
+                dt = time.perf_counter() - t0
+                if dt >= min_seconds:
+                    return dt / n
+        finally:
+            lib().or_set_threads(os.cpu_count() or 1)
 
     def dense(self) -> np.ndarray:
         """Dense H (makeH, H_v.cpp:21-190, is the same row formula applied to unit vectors)."""

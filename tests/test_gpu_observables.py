@@ -118,3 +118,40 @@ def test_spin_correlations_and_chirality(states):
         e += b.J * (c["SxSx+SySy"] + model.Jz * c["SzSz"])
     e -= model.Ch * Ob.chirality(model, tris, vecs[0])
     assert abs(e - eigs[0]) < 1e-10 * abs(eigs[0])
+
+
+def test_observables_match_the_reference_analysis_programs(cuda_device):
+    """Pinned to the reference's own analysis programs: pspincorr and
+    pchirality (analysis/src, compiled from the reference's sources) read the
+    two lowest eigenvectors ED2 wrote for the 4x3 triangular sector at k=(1,1)
+    and printed <bra|Sz_i Sz_j|ket>, <bra|SxSx+SySy|ket> and the chirality
+    (tests/golden/make_observables.py).  They print six significant digits,
+    which sets the tolerance."""
+    import os
+
+    from ed_code_gb300 import lattice as L
+    from ed_code_gb300 import observables
+    from ed_code_gb300.sector import GpuSector
+
+    fix = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "observables.npz"))
+    model = L.make_model(L.TorusSpec("triangular", 4, 3, Jz=0.8, Ch=0.2), 0, 1, 1)
+    sec = GpuSector(model)
+    states, _, _ = sec.basis()
+    assert np.array_equal(states, fix["states"])
+    sec.close()
+    vec = [fix["vec0"] / np.linalg.norm(fix["vec0"]), fix["vec1"] / np.linalg.norm(fix["vec1"])]
+
+    def close(got, want):
+        assert abs(got - want) <= 1e-5 * abs(want) + 2e-6, (got, want)
+
+    for tag, (ket, bra) in {"11": (0, 0), "12": (0, 1), "21": (1, 0)}.items():
+        zz, xy = fix[f"szsz_{tag}"], fix[f"xy_{tag}"]
+        pairs = sorted({(int(a), int(b)) for a, b, _, _ in zz})
+        res = observables.spin_correlations(model, pairs, ket=vec[ket], bra=vec[bra])
+        for a, b, re, im in zz:
+            close(res[(int(a), int(b))]["SzSz"], complex(re, im))
+        for a, b, re, im in xy:
+            close(res[(int(a), int(b))]["SxSx+SySy"], complex(re, im))
+    tris = [tuple(int(x) for x in t) for t in fix["triangles"]]
+    for tag, (ket, bra) in {"00": (0, 0), "01": (0, 1)}.items():
+        close(observables.chirality(model, tris, ket=vec[ket], bra=vec[bra]), complex(fix[f"chirality_{tag}"][0]))

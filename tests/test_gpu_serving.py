@@ -20,9 +20,8 @@ def stream(mods):
     return serving.make_stream(10, rate=400.0, seed=11, sizes=(20, 24))
 
 
-TILE = 4096  # rows per tile: a segment's sums depend on it, so alone and mixed share it
-
-
+# A segment's sums depend on the batch's tile size and lanes per row, so the
+# alone runs share the choice the loop's tuner made (TUNED).
 TUNED = {}
 
 
