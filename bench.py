@@ -401,6 +401,34 @@ def run_device(args, world, rank, local_rank):
     value = R.job_rate(world, args.steps, ms_max / 1e3)
     ms_step = ms_max / args.steps
 
+    # the block H*v: 2 and 4 vectors per pass (each row's entries read once,
+    # each gathered line serving every vector), timed the same way
+    block = None
+    if mode == "stored-rows" and not args.no_block:
+        block = {}
+        for nv in (2, 4):
+            V = torch.empty((sec.n_p, nv), dtype=ctype, device=dev)
+            W = torch.empty_like(V)
+            with torch.cuda.stream(stream):
+                fill_random(V, 7, stream)
+                for _ in range(args.warmup):
+                    sec.hv_block(V, W, stream)
+                b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                b0.record(stream)
+                for _ in range(args.steps):
+                    sec.hv_block(V, W, stream)
+                b1.record(stream)
+            torch.cuda.synchronize()
+            ms_b = b0.elapsed_time(b1) / args.steps
+            # algorithmic bytes of one block launch: the entry stream and row
+            # offsets once, every vector's own bytes nv times
+            Bb = sec.algorithmic_bytes_block(elem, nnz, nv)
+            block[f"nv{nv}"] = {"ms_per_launch": ms_b, "hv_per_s": nv * 1e3 / ms_b,
+                                "algorithmic_bytes_per_launch": Bb, "GBps": Bb / (ms_b / 1e3) / 1e9,
+                                "frac_of_measured_hbm": Bb / (ms_b / 1e3) / 1e9 / measured_peak_hbm()[0]}
+            del V, W
+        torch.cuda.empty_cache()
+
     # e2e through the C ABI host-buffer call: pinned v in, w out, every step
     e2e = None
     if not args.no_e2e:
@@ -458,6 +486,7 @@ def run_device(args, world, rank, local_rank):
                    "l2": "inputs larger than L2 (no flush needed)", "orbit_search": "torus" if sec.info["torus"] else "walk"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "traffic": traffic},
+        "block_hv": block,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "clocks": clocks,
@@ -705,7 +734,7 @@ def run_solve36(args):
     sec.tune(0)
     t_build = time.perf_counter() - t0
     t1 = time.perf_counter()
-    r = sec.solve_mixed(n_ev=6, iterations=300, reorth_every=0, seed=4)
+    r = sec.solve_mixed(n_ev=6, iterations=300, reorth_every=0, seed=4)  # 2 GB vectors: local form
     t_solve = time.perf_counter() - t1
     out = {"metric": "36-site sector solve", "mode": "solve36", "value": t_solve, "unit": "s",
            "higher_is_better": False, "n_gpus": 1, "data": "synthetic", "build_seconds": t_build,
@@ -729,6 +758,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--matrix-free", action="store_true", help="do not store the searched targets")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-block", action="store_true", help="skip the 2- and 4-vector block H*v timing")
     ap.add_argument("--rows", default=None,
                     help="LANES,POLICY[,CTAS_PER_SM[,PIPELINED]]: fix the stored-row kernel instead of timing it")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -744,7 +774,8 @@ def main():
     ap.add_argument("--hamiltonians", type=int, default=64)
     ap.add_argument("--plain-sample", type=int, default=3)
     ap.add_argument("--momenta", type=int, default=30)
-    ap.add_argument("--reorth", type=int, default=0)
+    ap.add_argument("--reorth", type=int, default=1,
+                    help="precision/solve: 1 reorthogonalise every step, 0 locally against the last two vectors")
     ap.add_argument("--serve-tile", type=int, default=4096, help="serve: rows per tile of the batch kernels")
     ap.add_argument("--ingest-ncu", metavar="CSV", default=None,
                     help="record the DRAM bytes per launch of --kernel from this ncu CSV in profiles/traffic.json "

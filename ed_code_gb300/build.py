@@ -23,7 +23,8 @@ LIB = os.path.join(HERE, "libedgpu.so")
 REF_LIB = os.path.join(HERE, "libedgpu_ref.so")
 
 CUDA_UNITS = ["capi.cu", "basis.cu", "hv.cu", "lanczos.cu", "lanczos_mixed.cu", "targets.cu", "hv_noalloc.cu",
-              "batch.cu", "tridiag_dev.cu", "dense.cu"]
+              "batch.cu", "tridiag_dev.cu", "dense.cu",
+              "hv_block.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

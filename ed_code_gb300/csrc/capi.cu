@@ -38,7 +38,7 @@ static void free_sector(Sector& S) {
   free_targets(S);
   void* ptrs[] = {S.dP,   S.reps,    S.lid,         S.recs,         S.vrecs,       S.Ia,    S.Ib,
                   S.groups, S.ch,   S.bows,    S.nk,          S.rots,         S.perms,       S.binom, S.host_in.ptr,
-                  S.host_out.ptr, S.lz_work.ptr};
+                  S.host_out.ptr, S.lz_work.ptr, S.ublk.ptr};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (S.stream) cudaStreamDestroy(S.stream);

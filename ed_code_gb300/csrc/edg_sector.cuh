@@ -96,6 +96,7 @@ struct Sector {
   float2* vtab32 = nullptr;
   int n_vals = 0;
   DeviceBuffer ubuf;            // u = v / norm scratch
+  DeviceBuffer ublk;            // the same for edg_hv_block's interleaved vectors
   size_t targets_bytes = 0;
   int csr_lpr = 16;             // lanes per CSR row (8, 16 or 32): edg_sector_tune
   int csr_pol = 1;              // cache policy of the CSR loads (1 or 2): edg_sector_tune
@@ -147,6 +148,8 @@ cudaError_t count_offdiag(const Sector& S, unsigned long long* nnz_dev, cudaStre
 int build_targets(Sector& S, int64_t max_bytes, std::string& err);
 void free_targets(Sector& S);
 cudaError_t launch_hv_stored(const Sector& S, const void* v, void* w, bool fp64, cudaStream_t st);
+// hv_block.cu: W = H V for nv = 2 or 4 vectors interleaved by row, u the n_p x nv scratch
+cudaError_t launch_hv_block(const Sector& S, const void* v, void* w, int nv, bool fp64, void* u, cudaStream_t st);
 // stored rows in row order: rows [r0, r1) of H*v, with the u = v/norm pass first when with_u
 cudaError_t launch_hv_rows(const Sector& S, const void* v, void* w, bool fp64, int64_t r0, int64_t r1, bool with_u,
                            cudaStream_t st);

@@ -187,6 +187,15 @@ class GpuSector:
                 "evecs": evecs[:n] if want_vectors else None,
                 "stats": {f: getattr(st, f) for f, _ in N.edg_mixed_stats._fields_}}
 
+    def hv_block(self, v, w, stream=None) -> None:
+        """W = H V for torch tensors of shape (n_p, 2) or (n_p, 4) (the vectors
+        interleaved by row), on the device (edg_hv_block)."""
+        nv = int(v.shape[1])
+        code = N.EDG_C128 if v.dtype == __import__("torch").complex128 else N.EDG_C64
+        st = stream.cuda_stream if stream is not None else 0
+        N.check(N.lib().edg_hv_block(self._h, C.c_void_p(v.data_ptr()), C.c_void_p(w.data_ptr()), nv, code,
+                                     C.c_void_p(st)))
+
     def count_offdiag(self) -> int:
         n = C.c_int64()
         N.check(N.lib().edg_count_offdiag(self._h, C.byref(n)))
@@ -208,6 +217,16 @@ class GpuSector:
             return (self.n_p * (2 * S + 1) + nnz * (S + entry) + 8 * (self.n_p + 1) + 8 * self.n_p
                     + self.n_p * (2 * S + 1))
         return self.n_p * (8 + 1 + 2 * S) + nnz_off * S
+
+    def algorithmic_bytes_block(self, elem_bytes: int, nnz_off: Optional[int], nv: int) -> int:
+        """Bytes one block H*v on nv vectors must move (stored rows): the
+        entries, row offsets and diagonal once; per vector v_i, w_i, one u_j
+        per nonzero and the u pass; the stabiliser byte twice (u pass, row)."""
+        S = elem_bytes
+        nnz = self.info.get("n_targets", 0)
+        entry = self.info.get("entry_bytes") or 6
+        return (nnz * entry + 8 * (self.n_p + 1) + 8 * self.n_p + 2 * self.n_p
+                + nv * (self.n_p * 2 * S + nnz * S + self.n_p * 2 * S))
 
     def close(self) -> None:
         if getattr(self, "_h", None):

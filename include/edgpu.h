@@ -171,6 +171,17 @@ int edg_hv_host(edg_sector* s, const void* v, void* w, int dtype);
  * on the GPU race and must be ordered by the caller. */
 int edg_hv_noalloc(edg_sector* s, const void* v, void* w, int dtype, void* stream);
 
+/* W = H V for n_vectors = 2 or 4 vectors at once, interleaved by row: entry i
+ * of vector q at index i * n_vectors + q of v and w (device pointers, n_p *
+ * n_vectors complex entries each, dtype EDG_C128 or EDG_C64), enqueued on
+ * `stream`.  Each row's stored entries are read once and each gathered line
+ * serves all the vectors, so the bytes per vector fall with n_vectors; every
+ * vector gets the bits edg_hv gives it alone.  Needs stored rows; keeps a
+ * scratch of n_p * n_vectors entries on the sector.  No counterpart in the
+ * reference (its sHv takes one vector, H_v.cpp:192); it serves block solvers
+ * and the FP64 Rayleigh quotients of several Ritz vectors. */
+int edg_hv_block(edg_sector* s, const void* v, void* w, int n_vectors, int dtype, void* stream);
+
 /* Number of nonzero off-diagonal bond/chirality targets summed over rows
  * (the nnz_off of the algorithmic byte count). */
 int edg_count_offdiag(edg_sector* s, int64_t* nnz_off);

@@ -334,3 +334,28 @@ def test_large_sector_6x5_generic_walk(gpu):
     perm = [int(x) for x in np.random.default_rng(4).permutation(20)]
     sec = large_sector_check(gpu, L.TorusSpec("triangular", 5, 4, Jz=0.9, Ch=0.3, relabel=perm), 0, 1, 2)
     assert sec.info["torus"] == 0
+
+
+@pytest.mark.parametrize("name,idx", [("tri6x4_k10", 0), ("sq4x4_j2", 1)])
+def test_block_hv_equals_single_vector(gpu, name, idx):
+    """edg_hv_block on 2 and 4 interleaved vectors: each vector gets the bits
+    edg_hv gives it alone (same lanes per row), in FP64 and FP32."""
+    import torch
+
+    sec = gpu.GpuSector(golden_model(name, idx))
+    assert sec.build_targets()
+    for lanes in (8, 16):
+        sec.set_rows(lanes, 2, 0, 1)
+        for dt in (np.complex128, np.complex64):
+            for nv in (2, 4):
+                vs = [O.splitmix_vector(sec.n_p, 20 + q).astype(dt) for q in range(nv)]
+                V = torch.from_numpy(np.stack(vs, axis=1).copy()).cuda()
+                W = torch.empty_like(V)
+                sec.hv_block(V, W)
+                torch.cuda.synchronize()
+                Wh = W.cpu().numpy()
+                for q in range(nv):
+                    assert np.array_equal(Wh[:, q], sec.sHv(vs[q], dtype=dt)), (lanes, dt, nv, q)
+    with pytest.raises(Exception):
+        sec.hv_block(torch.zeros((sec.n_p, 3), dtype=torch.complex64, device="cuda"),
+                     torch.zeros((sec.n_p, 3), dtype=torch.complex64, device="cuda"))

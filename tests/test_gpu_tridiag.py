@@ -61,7 +61,7 @@ def _dense(d, e):
 
 
 @pytest.mark.parametrize("name,k", list(_cases()))
-def test_eigenpairs_match_zheev(gpu, name, k):
+def test_eigenpairs_match_zheev(cuda_device, name, k):
     d, e = _t(name, k)
     ref_w, ref_v = FIX[f"{name}_k{k}_eigs"], FIX[f"{name}_k{k}_vecs"]
     nv = ref_v.shape[1]
@@ -98,7 +98,7 @@ def _cw_restatement(th, hat, scale, want):
 
 
 @pytest.mark.parametrize("name", CASES)
-def test_copy_filter_matches_zheev_spectra(gpu, name):
+def test_copy_filter_matches_zheev_spectra(cuda_device, name):
     import scipy.linalg as sl
 
     k = int(FIX[f"{name}_prefixes"][-1])
@@ -116,7 +116,7 @@ def test_copy_filter_matches_zheev_spectra(gpu, name):
         assert np.linalg.norm(T @ V[q] - got[q] * V[q]) <= 1e-10 * scale
 
 
-def test_bad_arguments_are_rejected(gpu):
+def test_bad_arguments_are_rejected(cuda_device):
     from ed_code_gb300 import _native as N
 
     d = np.zeros(4)
