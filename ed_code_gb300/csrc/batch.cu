@@ -203,8 +203,7 @@ __global__ void __launch_bounds__(kThreads) k_b_hv(const SegDev* __restrict__ se
       const int64_t i = t.row0 + r;
       const float ni = (float)S.nrm[S.lid[i]];
       const float d = (float)S.ezz[i];
-      const float2 vi = v[i];
-      S.w[i] = make_float2(ar * ni + d * vi.x, ai * ni + d * vi.y);
+      S.w[i] = row_out(ar, ai, ni, d, v[i]);
     }
     r += rows_per_pass;
     beg = beg1;

@@ -57,6 +57,25 @@ __device__ __forceinline__ double2 ld_keep(const double2* a, uint64_t pol) {
   return r;
 }
 
+// acc += c * x for complex c, x, as explicit FMAs in a fixed order, so every
+// kernel that sums rows (single vector, block, batch) rounds the same way
+// whatever the compiler would have contracted.
+__device__ __forceinline__ float fmaR(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fmaR(double a, double b, double c) { return fma(a, b, c); }
+template <typename Real, typename CT>
+__device__ __forceinline__ void cmac(Real& ar, Real& ai, const CT& c, const CT& x) {
+  ar = fmaR(c.x, x.x, fmaR(-c.y, x.y, ar));
+  ai = fmaR(c.x, x.y, fmaR(c.y, x.x, ai));
+}
+// a row's result: norm_i * sum + Ezz_i * v_i
+template <typename Real, typename CT>
+__device__ __forceinline__ CT row_out(Real ar, Real ai, Real ni, Real d, const CT& vi) {
+  CT out;
+  out.x = fmaR(ar, ni, d * vi.x);
+  out.y = fmaR(ai, ni, d * vi.y);
+  return out;
+}
+
 // Entry formats of the stored rows.  kSplit: a u32 column array and a u16
 // value-id array (6 bytes an entry).  kPacked: one u32 an entry, the column
 // in the low cb bits and the value id above them (4 bytes), used when the
@@ -142,8 +161,7 @@ __device__ __forceinline__ void csr_consume(uint64_t beg, uint64_t end, int sl, 
     if (e[q] == 0xFFFFFFFFu) continue;
     const int id = packed ? (int)(e[q] >> cb) : (int)h[q];
     const CT c = kSmemTab ? vtab[id] : __ldg(vtab + id);
-    ar += c.x * x[q].x - c.y * x[q].y;
-    ai += c.x * x[q].y + c.y * x[q].x;
+    cmac(ar, ai, c, x[q]);
   }
   for (uint64_t t = beg + sl + LPR * kU; t < end; t += LPR) {
     uint32_t jt;
@@ -151,8 +169,7 @@ __device__ __forceinline__ void csr_consume(uint64_t beg, uint64_t end, int sl, 
     ld_entry<kFmt, kPol>(col, vid, t, cb, pf, jt, idt);
     const CT c = kSmemTab ? vtab[idt] : __ldg(vtab + idt);
     const CT y = ld_keep(u + jt, pl);
-    ar += c.x * y.x - c.y * y.y;
-    ai += c.x * y.y + c.y * y.x;
+    cmac(ar, ai, c, y);
   }
 #pragma unroll
   for (int o = LPR / 2; o > 0; o >>= 1) {

@@ -133,10 +133,7 @@ __global__ void __launch_bounds__(kBlkThreads) k_hv_blk(const uint64_t* __restri
       const int id = packed ? (int)(e[q] >> cb) : (int)h[q];
       const CT c = tab[id];
 #pragma unroll
-      for (int k = 0; k < NV; ++k) {
-        ar[k] += c.x * x[q][k].x - c.y * x[q][k].y;
-        ai[k] += c.x * x[q][k].y + c.y * x[q][k].x;
-      }
+      for (int k = 0; k < NV; ++k) cmac(ar[k], ai[k], c, x[q][k]);
     }
     for (uint64_t t = beg + sl + LPR * kU; t < end; t += LPR) {
       uint32_t jt;
@@ -144,11 +141,7 @@ __global__ void __launch_bounds__(kBlkThreads) k_hv_blk(const uint64_t* __restri
       ld_entry<kFmt, kPol>(col, vid, t, cb, pf, jt, idt);
       const CT c = tab[idt];
 #pragma unroll
-      for (int k = 0; k < NV; ++k) {
-        const CT y = ld_keep(u + (int64_t)jt * NV + k, pl);
-        ar[k] += c.x * y.x - c.y * y.y;
-        ai[k] += c.x * y.y + c.y * y.x;
-      }
+      for (int k = 0; k < NV; ++k) cmac(ar[k], ai[k], c, ld_keep(u + (int64_t)jt * NV + k, pl));
     }
 #pragma unroll
     for (int o = LPR / 2; o > 0; o >>= 1)
@@ -161,13 +154,7 @@ __global__ void __launch_bounds__(kBlkThreads) k_hv_blk(const uint64_t* __restri
       const Real ni = nrm[lid[i]];
       const Real d = (Real)ezz[i];
 #pragma unroll
-      for (int k = 0; k < NV; ++k) {
-        const CT vi = v[i * NV + k];
-        CT out;
-        out.x = ar[k] * ni + d * vi.x;
-        out.y = ai[k] * ni + d * vi.y;
-        w[i * NV + k] = out;
-      }
+      for (int k = 0; k < NV; ++k) w[i * NV + k] = row_out(ar[k], ai[k], ni, d, v[i * NV + k]);
     }
     i += stride;
     beg = beg1;

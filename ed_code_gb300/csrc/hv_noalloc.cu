@@ -30,6 +30,7 @@
 #include <string>
 
 #include "../../include/edgpu.h"
+#include "csr_row.cuh"
 #include "edg_sector.cuh"
 
 struct edg_sector {
@@ -131,23 +132,14 @@ __global__ void __launch_bounds__(kThreads) k_na_rows(const uint64_t* __restrict
       const uint32_t e = __ldg(col + t);
       const CT c = __ldg(vtab + (vid ? (uint32_t)__ldg(vid + t) : e >> cb));
       const CT x = u[vid ? e : e & ((1u << cb) - 1u)];
-      ar += c.x * x.x - c.y * x.y;
-      ai += c.x * x.y + c.y * x.x;
+      edg::cmac(ar, ai, c, x);
     }
 #pragma unroll
     for (int o = LPR / 2; o > 0; o >>= 1) {
       ar += __shfl_down_sync(0xffffffffu, ar, o, LPR);
       ai += __shfl_down_sync(0xffffffffu, ai, o, LPR);
     }
-    if (sl == 0 && i < n) {
-      const CT vi = v[i];
-      const Real ni = nrm[lid[i]];
-      const Real d = (Real)ezz[i];
-      CT out;
-      out.x = ar * ni + d * vi.x;
-      out.y = ai * ni + d * vi.y;
-      w[i] = out;
-    }
+    if (sl == 0 && i < n) w[i] = edg::row_out(ar, ai, nrm[lid[i]], (Real)ezz[i], v[i]);
   }
 }
 

@@ -304,13 +304,7 @@ __global__ void __launch_bounds__(kTgtThreads) k_hv_csr(const uint64_t* __restri
   };
   auto store = [&](int64_t r, Real ar, Real ai) {
     if (sl == 0 && r < n_p) {
-      const CT vi = v[r];
-      const Real ni = nrm[lid[r]];
-      const Real d = (Real)ezz[r];
-      CT out;
-      out.x = ar * ni + d * vi.x;
-      out.y = ai * ni + d * vi.y;
-      w[r] = out;
+      w[r] = row_out(ar, ai, nrm[lid[r]], (Real)ezz[r], v[r]);
     }
   };
   int64_t i = row0 + warp * kRows + sub;
