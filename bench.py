@@ -423,9 +423,11 @@ def run_device(args, world, rank, local_rank):
             # algorithmic bytes of one block launch: the entry stream and row
             # offsets once, every vector's own bytes nv times
             Bb = sec.algorithmic_bytes_block(elem, nnz, nv)
+            tb = profile_traffic(f"hv_block_nv{nv}_{args.workload}_{args.dtype}")
             block[f"nv{nv}"] = {"ms_per_launch": ms_b, "hv_per_s": nv * 1e3 / ms_b,
                                 "algorithmic_bytes_per_launch": Bb, "GBps": Bb / (ms_b / 1e3) / 1e9,
-                                "frac_of_measured_hbm": Bb / (ms_b / 1e3) / 1e9 / measured_peak_hbm()[0]}
+                                "frac_of_measured_hbm": Bb / (ms_b / 1e3) / 1e9 / measured_peak_hbm()[0],
+                                "traffic": tb, "traffic_over_algorithmic": None if tb is None else tb / Bb}
             del V, W
         torch.cuda.empty_cache()
 
@@ -468,6 +470,9 @@ def run_device(args, world, rank, local_rank):
     peak, peak_kind = measured_peak_hbm()
     achieved = B / (ms_step / 1e3) / 1e9
     traffic = profile_traffic(f"hv_{mode}_{args.workload}_{args.dtype}")
+    # the problem's own bytes (per row the representative, stabiliser byte,
+    # v_i and w_i; per nonzero one v_j), whatever the kernel stores
+    B_base = sec.n_p * (8 + 1 + 2 * elem) + nnz * elem
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -485,7 +490,10 @@ def run_device(args, world, rank, local_rank):
                    "matrix_free_GBps": B_mf / (mf_ms / 1e3) / 1e9,
                    "l2": "inputs larger than L2 (no flush needed)", "orbit_search": "torus" if sec.info["torus"] else "walk"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_kind": peak_kind, "traffic": traffic},
+                     "peak_kind": peak_kind, "traffic": traffic,
+                     "traffic_over_algorithmic": None if traffic is None else traffic / B,
+                     "base_bytes": B_base, "base_achieved": B_base / (ms_step / 1e3) / 1e9,
+                     "base_frac": B_base / (ms_step / 1e3) / 1e9 / peak},
         "block_hv": block,
         "cpu_baseline": cpu,
         "e2e": e2e,

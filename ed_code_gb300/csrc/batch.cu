@@ -9,24 +9,33 @@
 // leave independently: a segment added while others are half way starts at
 // step 0 with the next graph.  The rows of all live segments are cut into
 // tiles of `tile_rows` rows, and each kernel below runs one CTA per tile that
-// reads its segment's descriptor:
+// reads its segment's descriptor.  One step is nine kernels:
 //
-//   u       u = V_j / norm
-//   hv      w = H V_j              (CSR rows, lanes_per_row lanes per row)
-//   dot     alpha_j = Re<V_j|w>    (tile partials; one CTA per segment sums
-//                                   its own tiles in order: deterministic, and
-//                                   independent of the other segments)
-//   step    w -= alpha_j V_j + beta_j V_{j-1}
-//   cgs     w -= sum_k <V_k|w> V_k over k <= j (FP64 coefficients); a second
-//           pass only when the first removed more than 1e-4 of |w|^2
-//   norm    beta_{j+1} = |w|
-//   scale   V_{j+1} = w / beta_{j+1};  j += 1
-//   check   every check_every steps: the wanted Ritz pairs of T_j (bisection
-//           and inverse iteration in FP64, one CTA per segment); a segment
-//           whose residual bounds beta_j |y_k[j-1]| are all below
-//           tol * max(1, |theta_k|) stops, as does one that reached its
-//           maximum number of steps.
+//   k_b_hv          u_j = V_j / norm was written by the previous step;
+//                   w = H V_j (CSR rows, lanes_per_row lanes per row) and the
+//                   tile's partial of alpha_j = Re<V_j|w>
+//   k_b_step        w -= alpha_j V_j + beta_j V_{j-1} and the tile's |w|^2
+//   k_b_cgs_dot     classical Gram-Schmidt: the tile's <V_k|w>, k <= j
+//   k_b_cgs_finish  the segment's <V_k|w> summed over its tiles (FP64); on
+//                   the first pass also whether a second pass is needed (the
+//                   first removed more than 1e-4 of |w|^2)
+//   k_b_cgs_sub     w -= sum_k <V_k|w> V_k; the second pass ends with the
+//                   tile's |w|^2 for beta_{j+1}
+//   (the three Gram-Schmidt kernels run twice; the second pass returns at
+//   once for a segment that does not need it)
+//   k_b_scale       V_{j+1} = w / beta_{j+1}, u_{j+1}; the segment's last CTA
+//                   advances j and, every check_every steps, runs the
+//                   convergence test: the wanted Ritz pairs of T_j
+//                   (bisection and inverse iteration in FP64); a segment whose
+//                   residual bounds beta_j |y_k[j-1]| are all below
+//                   tol * max(1, |theta_k|) stops, as does one that reached
+//                   its maximum number of steps.
 //
+// Each reduction over a segment's tiles (alpha, |w|^2, the Gram-Schmidt
+// decision, beta, the step counter) is closed by the segment's last CTA to
+// finish (a ticket counter, below), so no kernel exists only to reduce and
+// no CTA waits for another.
+
 // The vectors are reorthogonalised every step: with FP32 vectors the copies
 // of converged levels otherwise appear within a few steps.  A stopped segment
 // is finished with the single-sector solver's code (MixedFinish): Ritz
