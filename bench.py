@@ -431,6 +431,31 @@ def run_device(args, world, rank, local_rank):
             del V, W
         torch.cuda.empty_cache()
 
+    # the other vector precision on the same rows (FP64 when the line is FP32:
+    # the plain form's sHv), timed the same way
+    other = None
+    if mode == "stored-rows" and not args.no_other_dtype:
+        o_ct, o_elem = (torch.complex64, 8) if fp64 else (torch.complex128, 16)
+        vo = torch.empty(sec.n_p, dtype=o_ct, device=dev)
+        wo = torch.empty_like(vo)
+        with torch.cuda.stream(stream):
+            fill_random(vo, 4, stream)
+            for _ in range(args.warmup):
+                sec.hv(vo, wo, stream)
+            o0, o1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            o0.record(stream)
+            for _ in range(args.steps):
+                sec.hv(vo, wo, stream)
+            o1.record(stream)
+        torch.cuda.synchronize()
+        ms_o = o0.elapsed_time(o1) / args.steps
+        Bo = sec.algorithmic_bytes(o_elem, nnz)
+        other = {"vector": "c64" if fp64 else "c128", "ms_per_step": ms_o, "hv_per_s": 1e3 / ms_o,
+                 "algorithmic_bytes": Bo, "GBps": Bo / (ms_o / 1e3) / 1e9,
+                 "frac_of_measured_hbm": Bo / (ms_o / 1e3) / 1e9 / measured_peak_hbm()[0]}
+        del vo, wo
+        torch.cuda.empty_cache()
+
     # e2e through the C ABI host-buffer call: pinned v in, w out, every step
     e2e = None
     if not args.no_e2e:
@@ -495,6 +520,7 @@ def run_device(args, world, rank, local_rank):
                      "base_bytes": B_base, "base_achieved": B_base / (ms_step / 1e3) / 1e9,
                      "base_frac": B_base / (ms_step / 1e3) / 1e9 / peak},
         "block_hv": block,
+        "other_precision_hv": other,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "clocks": clocks,
@@ -767,6 +793,8 @@ def main():
     ap.add_argument("--matrix-free", action="store_true", help="do not store the searched targets")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-block", action="store_true", help="skip the 2- and 4-vector block H*v timing")
+    ap.add_argument("--no-other-dtype", action="store_true",
+                    help="skip timing the H*v in the other vector precision (FP64 for a c64 line)")
     ap.add_argument("--rows", default=None,
                     help="LANES,POLICY[,CTAS_PER_SM[,PIPELINED]]: fix the stored-row kernel instead of timing it")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)

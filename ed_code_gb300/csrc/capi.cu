@@ -553,10 +553,22 @@ int edg_hv_host(edg_sector* s, const void* v, void* w, int dtype) {
   cudaError_t e = ensure(S.host_in, bytes);
   if (e == cudaSuccess) e = ensure(S.host_out, bytes);
   if (e != cudaSuccess) return cuda_fail(e, "hv_host buffers");
-  e = cudaMemcpyAsync(S.host_in.ptr, v, bytes, cudaMemcpyHostToDevice, S.stream);
   const bool fp64 = dtype == EDG_C128;
   const int64_t n = S.P.n_p;
   constexpr int kChunks = 8;
+  // v in page-locked host memory that the device can address: with stored
+  // rows, one kernel reads it in place and writes both the device copy of v
+  // and u = v / norm, instead of a copy-engine copy and then the u pass
+  cudaPointerAttributes va{};
+  const void* v_dev = nullptr;
+  if (cudaPointerGetAttributes(&va, v) != cudaSuccess)
+    cudaGetLastError();
+  else if (va.type == cudaMemoryTypeHost && va.devicePointer &&
+           reinterpret_cast<uintptr_t>(va.devicePointer) % (fp64 ? 16 : 8) == 0)
+    v_dev = va.devicePointer;
+  const bool u_done = S.col && v_dev;
+  e = u_done ? launch_u_in(S, v_dev, S.host_in.ptr, fp64, S.stream)
+             : cudaMemcpyAsync(S.host_in.ptr, v, bytes, cudaMemcpyHostToDevice, S.stream);
   // w in page-locked host memory that the device can address (cudaHostAlloc,
   // cudaHostRegister): the kernel stores each w_i there itself, over the
   // host link while it runs, with no copy after it.
@@ -567,7 +579,8 @@ int edg_hv_host(edg_sector* s, const void* v, void* w, int dtype) {
   else if (wa.type == cudaMemoryTypeHost)
     w_dev = wa.devicePointer;
   if (e == cudaSuccess && w_dev) {
-    e = launch_hv(S, S.host_in.ptr, w_dev, fp64, S.stream);
+    e = u_done ? launch_hv_rows(S, S.host_in.ptr, w_dev, fp64, 0, n, false, S.stream)
+               : launch_hv(S, S.host_in.ptr, w_dev, fp64, S.stream);
   } else if (S.col && n >= (1 << 20)) {
     // rows in row order: the w rows of chunk c go back to the host while the
     // rows of chunk c + 1 are computed
@@ -577,7 +590,7 @@ int edg_hv_host(edg_sector* s, const void* v, void* w, int dtype) {
     const size_t elem = fp64 ? 16 : 8;
     for (int c = 0; c < kChunks && e == cudaSuccess; ++c) {
       const int64_t r0 = n * c / kChunks, r1 = n * (c + 1) / kChunks;
-      e = launch_hv_rows(S, S.host_in.ptr, S.host_out.ptr, fp64, r0, r1, c == 0, S.stream);
+      e = launch_hv_rows(S, S.host_in.ptr, S.host_out.ptr, fp64, r0, r1, c == 0 && !u_done, S.stream);
       if (e == cudaSuccess) e = cudaEventRecord(S.chunk_done[c], S.stream);
       if (e == cudaSuccess) e = cudaStreamWaitEvent(S.copy_stream, S.chunk_done[c], 0);
       if (e == cudaSuccess)
@@ -586,7 +599,9 @@ int edg_hv_host(edg_sector* s, const void* v, void* w, int dtype) {
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(S.copy_stream);
   } else {
-    if (e == cudaSuccess) e = launch_hv(S, S.host_in.ptr, S.host_out.ptr, fp64, S.stream);
+    if (e == cudaSuccess)
+      e = u_done ? launch_hv_rows(S, S.host_in.ptr, S.host_out.ptr, fp64, 0, n, false, S.stream)
+                 : launch_hv(S, S.host_in.ptr, S.host_out.ptr, fp64, S.stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(w, S.host_out.ptr, bytes, cudaMemcpyDeviceToHost, S.stream);
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(S.stream);

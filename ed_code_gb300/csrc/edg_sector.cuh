@@ -153,6 +153,9 @@ cudaError_t launch_hv_block(const Sector& S, const void* v, void* w, int nv, boo
 // stored rows in row order: rows [r0, r1) of H*v, with the u = v/norm pass first when with_u
 cudaError_t launch_hv_rows(const Sector& S, const void* v, void* w, bool fp64, int64_t r0, int64_t r1, bool with_u,
                            cudaStream_t st);
+// stored rows: u = v / norm and v_dst = v from a v_src the device reads in
+// place (mapped page-locked host memory)
+cudaError_t launch_u_in(const Sector& S, const void* v_src, void* v_dst, bool fp64, cudaStream_t st);
 int tune_rows(Sector& S, int lpr, int* chosen, double* ms_out);
 int hv_grid_blocks(bool fp64, bool torus, bool chch);
 

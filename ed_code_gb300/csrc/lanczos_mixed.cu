@@ -55,17 +55,18 @@ namespace {
 //   P32: FP32 complex vectors; sums of exact products in float-float, the
 //        three-term update with FP64 scalars split into FP32 heads and tails
 //        and rounded once to the FP32 storage (ff.cuh);
-//   P64: FP64 complex vectors and plain FP64 arithmetic (compensated sums),
-//        the same algorithm with nothing reduced -- the FP64 arm that the
-//        FP32 form is compared with.
+//   P64: FP64 complex vectors and plain FP64 arithmetic (products summed with
+//        FMAs, as an FP64 zdotc does), the same algorithm with nothing
+//        reduced -- the FP64 arm that the FP32 form is compared with.
 __device__ __forceinline__ float fmr(float a, float b, float c) { return fmaf(a, b, c); }
 __device__ __forceinline__ double fmr(double a, double b, double c) { return fma(a, b, c); }
 
-struct DAcc {  // FP64 products into a compensated FP64 sum
-  Acc a;
-  __device__ __forceinline__ void add_prod(double x, double y) { a.add(x * y); }
-  __device__ __forceinline__ void sub_prod(double x, double y) { a.add(-(x * y)); }
-  __device__ __forceinline__ double value() const { return a.value(); }
+struct DAcc {  // FP64 products summed in FP64, one FMA each
+  double s = 0.0;
+  __device__ __forceinline__ void add(double x) { s += x; }
+  __device__ __forceinline__ void add_prod(double x, double y) { s = fma(x, y, s); }
+  __device__ __forceinline__ void sub_prod(double x, double y) { s = fma(-x, y, s); }
+  __device__ __forceinline__ double value() const { return s; }
 };
 struct DScalar {
   double v;
@@ -105,7 +106,8 @@ __device__ __forceinline__ typename P::V mk(typename P::Real x, typename P::Real
 template <class P>
 __global__ void __launch_bounds__(kRedThreads) k_dot(const typename P::V* __restrict__ V, int64_t ld,
                                                      const typename P::V* __restrict__ x, int64_t n,
-                                                     double* __restrict__ part) {
+                                                     double* __restrict__ part, const double* run = nullptr) {
+  if (run && *run == 0.0) return;
   const typename P::V* a = V + (int64_t)blockIdx.y * ld;
   typename P::A sr, si;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -136,7 +138,8 @@ __global__ void __launch_bounds__(kRedThreads) k_dot(const typename P::V* __rest
 // Sum the partials of vector k (one CTA per k); mode 0: complex result to
 // out[2k], mode 1: real part to out[0], mode 2: sqrt of the real part to out[0].
 __global__ void __launch_bounds__(kRedThreads) k_finish(const double* __restrict__ part, int nb, double* out,
-                                                        int mode) {
+                                                        int mode, const double* run = nullptr) {
+  if (run && *run == 0.0) return;
   const double* p = part + (int64_t)blockIdx.x * nb * 2;
   __shared__ double rr[kRedThreads], ri[kRedThreads];
   double a = 0, b = 0;
@@ -296,7 +299,8 @@ __global__ void k_scale_inv(typename P::V* dst, const typename P::V* src, const 
 // rounding of y itself.
 template <class P>
 __global__ void k_sub(typename P::V* __restrict__ y, const typename P::V* __restrict__ V, int64_t ld,
-                      const double* __restrict__ q, int K, int64_t n) {
+                      const double* __restrict__ q, int K, int64_t n, const double* run = nullptr) {
+  if (run && *run == 0.0) return;
   using R = typename P::Real;
   extern __shared__ __align__(16) unsigned char sraw[];
   R* sq = reinterpret_cast<R*>(sraw);
@@ -313,6 +317,25 @@ __global__ void k_sub(typename P::V* __restrict__ y, const typename P::V* __rest
     }
     y[i] = mk<P>(re, im);
   }
+}
+
+// Whether a classical Gram-Schmidt pass needs a second one (Daniel, Gragg,
+// Kaufman and Stewart's criterion): the first removed sum_k |q_k|^2 of
+// x's |x|^2; more than 1e-4 of it means x had a component along the V_k large
+// enough that the pass's own rounding matters, and the pass is repeated.
+// *run = 1.0 or 0.0 for the second pass's kernels.
+__global__ void __launch_bounds__(kRedThreads) k_cgs_decide(const double* __restrict__ q, int K,
+                                                            const double* __restrict__ xn2, double* run) {
+  __shared__ double sm[kRedThreads];
+  double a = 0;
+  for (int k = threadIdx.x; k < K; k += blockDim.x) a += q[2 * k] * q[2 * k] + q[2 * k + 1] * q[2 * k + 1];
+  sm[threadIdx.x] = a;
+  __syncthreads();
+  for (int h = kRedThreads / 2; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) sm[threadIdx.x] += sm[threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *run = sm[0] > 1e-4 * *xn2 ? 1.0 : 0.0;
 }
 
 // Second pass of the resident-vector mode: X_e += sum_t y[e*m + j0 + t] V_{j0+t}
@@ -341,13 +364,13 @@ __global__ void __launch_bounds__(256) k_ritz_window(double2* __restrict__ X, in
     for (int e = 0; e < E; ++e) {
       double sr, si;
       if (P::kFp64) {
-        Acc ar, ai;
+        DAcc ar, ai;
 #pragma unroll
         for (int t = 0; t < kRing; ++t)
           if (t < cnt) {
             const double c = sc[e * kRing + t];
-            ar.add(c * (double)v[t].x);
-            ai.add(c * (double)v[t].y);
+            ar.add_prod(c, (double)v[t].x);
+            ai.add_prod(c, (double)v[t].y);
           }
         sr = ar.value();
         si = ai.value();
@@ -422,15 +445,15 @@ __global__ void __launch_bounds__(256) k_ritz_vectors(double2* __restrict__ X, i
     for (int k = threadIdx.x; k < qn * cnt; k += blockDim.x) sy[k] = y[(int64_t)(q0 + k / cnt) * m + k % cnt];
     __syncthreads();
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-      Acc ar[kRitzChunk], ai[kRitzChunk];
+      DAcc ar[kRitzChunk], ai[kRitzChunk];
       for (int j = 0; j < cnt; ++j) {
         const typename P::V v = V[(int64_t)j * ldv + i];
 #pragma unroll
         for (int q = 0; q < kRitzChunk; ++q)
           if (q < qn) {
             const double c = sy[q * cnt + j];
-            ar[q].add(c * (double)v.x);
-            ai[q].add(c * (double)v.y);
+            ar[q].add_prod(c, (double)v.x);
+            ai[q].add_prod(c, (double)v.y);
           }
       }
 #pragma unroll
@@ -741,25 +764,33 @@ static int solve_mixed_t(Sector& S, const edg_mixed_opts& o, double* eigs, doubl
         if (!second && (j + 1) % o.reorth_every == 0) {
           // Periodic reorthogonalisation in its two-vector form: between two
           // reorthogonalisations v_j has drifted too, so it is cleaned against
-          // v_0..v_{j-1} first, then w against v_0..v_j; each classical
-          // Gram-Schmidt pass runs twice.  (Cleaning w alone lets the
-          // recurrence carry v_j's error into every later vector.)
-          auto cgs2 = [&](Vt* x, int K) {
-            for (int pass = 0; pass < 2; ++pass)
+          // v_0..v_{j-1} first, then w against v_0..v_j.  (Cleaning w alone
+          // lets the recurrence carry v_j's error into every later vector.)
+          // Classical Gram-Schmidt; the coefficients of all K vectors stay in
+          // scal[0, 2K).  v_j's cleaning always takes a second pass; w's takes
+          // one only when the first removed more than 1e-4 of |w|^2 (decided
+          // on the device, lq[1]), as every step's reorthogonalisation needs
+          // it only now and then.
+          auto cgs2 = [&](Vt* x, int K, const double* xn2) {
+            for (int pass = 0; pass < 2; ++pass) {
+              const double* run = pass == 1 && xn2 ? lq + 1 : nullptr;
               for (int k0 = 0; k0 < K; k0 += 512) {
                 const int kk = std::min(512, K - k0);
-                k_dot<P><<<dim3(kRedBlocks, kk), kRedThreads, 0, st>>>(V + (int64_t)k0 * n, n, x, n, part);
-                k_finish<<<kk, kRedThreads, 0, st>>>(part, kRedBlocks, scal, 0);
-                k_sub<P><<<grid_n(n), 256, sizeof(typename P::Real) * 2 * kk, st>>>(x, V + (int64_t)k0 * n, n, scal,
-                                                                                    kk, n);
+                k_dot<P><<<dim3(kRedBlocks, kk), kRedThreads, 0, st>>>(V + (int64_t)k0 * n, n, x, n, part, run);
+                k_finish<<<kk, kRedThreads, 0, st>>>(part, kRedBlocks, scal + 2 * k0, 0, run);
+                k_sub<P><<<grid_n(n), 256, sizeof(typename P::Real) * 2 * kk, st>>>(x, V + (int64_t)k0 * n, n,
+                                                                                    scal + 2 * k0, kk, n, run);
               }
+              if (pass == 0 && xn2) k_cgs_decide<<<1, kRedThreads, 0, st>>>(scal, K, xn2, lq + 1);
+            }
           };
           if (o.reorth_every > 1 && j > 0) {
-            cgs2(vec(j), j);
+            cgs2(vec(j), j, nullptr);
             norm_into(vec(j), scal + 2 * (m + 1));
             k_scale_inv<P><<<grid_n(n), 256, 0, st>>>(vec(j), vec(j), scal + 2 * (m + 1), n);
           }
-          cgs2(w, j + 1);
+          k_finish<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, lq, 1);  // |w|^2 after the step (k_step)
+          cgs2(w, j + 1, lq);
           norm_into(w, beta + j + 1);
         } else if (!second) {
           k_finish<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, beta + j + 1, 2);

@@ -253,6 +253,45 @@ __global__ void k_u_scale(const typename CT2<Real>::T* __restrict__ v, const uin
   }
 }
 
+// The same u, for a v that the device reads in place (page-locked host memory
+// mapped into its address space), plus a device copy vd of v for the rows'
+// diagonal term: one pass over the host link, four loads in flight per
+// thread, instead of a copy-engine copy followed by the u pass.  u gets the
+// bits k_u_scale gives it.
+template <typename Real>
+__global__ void k_u_scale_in(const typename CT2<Real>::T* __restrict__ v, const uint8_t* __restrict__ lid,
+                             const double* __restrict__ nrm_inv_tab, int64_t n, typename CT2<Real>::T* __restrict__ vd,
+                             typename CT2<Real>::T* __restrict__ u) {
+  using CT = typename CT2<Real>::T;
+  __shared__ Real tab[65];
+  for (int k = threadIdx.x; k < 65; k += blockDim.x) tab[k] = (Real)nrm_inv_tab[k];
+  __syncthreads();
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + 3 * stride < n; i += 4 * stride) {
+    CT x[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) x[k] = v[i + k * stride];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int64_t r = i + k * stride;
+      vd[r] = x[k];
+      const Real s = tab[lid[r]];
+      x[k].x *= s;
+      x[k].y *= s;
+      u[r] = x[k];
+    }
+  }
+  for (; i < n; i += stride) {
+    CT x = v[i];
+    vd[i] = x;
+    const Real s = tab[lid[i]];
+    x.x *= s;
+    x.y *= s;
+    u[i] = x;
+  }
+}
+
 // CSR SpMV with a value dictionary: 32/LPR rows per warp, a warp's row
 // groups a grid stride apart.  kFmt: kSplit or kPacked entries (csr_row.cuh),
 // cb the column bits of a packed entry.  kPipe sets how far a warp loads
@@ -745,6 +784,19 @@ int tune_rows(Sector& S, int lpr, int* chosen, double* ms_out) {
 cudaError_t launch_hv_rows(const Sector& S, const void* v, void* w, bool fp64, int64_t r0, int64_t r1, bool with_u,
                            cudaStream_t st) {
   return fp64 ? launch_csr_t<double>(S, v, w, st, r0, r1, with_u) : launch_csr_t<float>(S, v, w, st, r0, r1, with_u);
+}
+
+cudaError_t launch_u_in(const Sector& S, const void* v_src, void* v_dst, bool fp64, cudaStream_t st) {
+  const int64_t n = S.P.n_p;
+  const int grid = (int)std::min<int64_t>((n + 255) / 256, 152 * 16);
+  const double* nrm_inv = params_field(S, offsetof(SectorParams, nrm_inv));
+  if (fp64)
+    k_u_scale_in<double><<<grid, 256, 0, st>>>(static_cast<const double2*>(v_src), S.lid, nrm_inv, n,
+                                               static_cast<double2*>(v_dst), static_cast<double2*>(S.ubuf.ptr));
+  else
+    k_u_scale_in<float><<<grid, 256, 0, st>>>(static_cast<const float2*>(v_src), S.lid, nrm_inv, n,
+                                              static_cast<float2*>(v_dst), static_cast<float2*>(S.ubuf.ptr));
+  return cudaGetLastError();
 }
 
 cudaError_t launch_hv_stored(const Sector& S, const void* v, void* w, bool fp64, cudaStream_t st) {

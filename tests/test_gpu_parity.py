@@ -208,8 +208,10 @@ def test_host_call_in_row_chunks_equals_device_call(gpu, dtype):
 @pytest.mark.parametrize("stored", [True, False])
 def test_host_call_into_pinned_w_equals_device_call(gpu, dtype, stored):
     """With w in page-locked host memory edg_hv_host has the kernel store w
-    there directly: the same bits as one device call, on stored rows and on
-    the matrix-free kernel; pageable w (the copy path) agrees too."""
+    there directly, and with v there (stored rows) one kernel reads it in
+    place for u = v/norm: the same bits as one device call for every mix of
+    page-locked and pageable v and w, on stored rows and on the matrix-free
+    kernel."""
     import ctypes as C
 
     import torch
@@ -226,12 +228,12 @@ def test_host_call_into_pinned_w_equals_device_call(gpu, dtype, stored):
     sec.hv(vd, wd)
     torch.cuda.synchronize()
     code = N.EDG_C128 if dtype == np.complex128 else N.EDG_C64
-    for pinned in (True, False):
-        vh = v.pin_memory() if pinned else v.clone()
-        wh = torch.full((sec.n_p,), float("nan"), dtype=tdt, pin_memory=pinned)
+    for pin_v, pin_w in ((True, True), (True, False), (False, True), (False, False)):
+        vh = v.pin_memory() if pin_v else v.clone()
+        wh = torch.full((sec.n_p,), float("nan"), dtype=tdt, pin_memory=pin_w)
         for _ in range(2):
             N.check(N.lib().edg_hv_host(sec._h, C.c_void_p(vh.data_ptr()), C.c_void_p(wh.data_ptr()), code))
-            assert torch.equal(wh, wd.cpu()), pinned
+            assert torch.equal(wh, wd.cpu()), (pin_v, pin_w)
 
 
 def test_hv_device_equals_host(gpu):
