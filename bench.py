@@ -572,7 +572,8 @@ def run_serve(args):
 
     torch.cuda.init()
     warm = serving.make_stream(4, rate=1e6, seed=99, sizes=(20,))
-    srv = serving.Server(max_iterations=300, res_tol=args.res_tol, tile_rows=args.serve_tile)
+    srv = serving.Server(max_iterations=300, res_tol=args.res_tol, tile_rows=args.serve_tile,
+                         reorth=args.batch_reorth, tune=bool(args.serve_tune))
     srv.run(warm)
     stream = serving.make_stream(args.requests, rate=args.rate, seed=3)
     t0 = time.perf_counter()
@@ -609,9 +610,9 @@ def run_serve(args):
            "plain_fp64_seconds_per_request": {str(k): float(np.mean(v)) for k, v in sorted(plain_t.items())},
            "sequential_plain_solves_per_s": len(stream) / seq_plain if seq_plain else None,
            "speedup_vs_sequential_plain": (summ["solves_per_s"] * seq_plain / len(stream)) if seq_plain else None,
-           "peak_active": srv.peak_live, "create_seconds": t_create, "batch_timers": timers,
+           "peak_active": srv.peak_live, "create_seconds": t_create, "batch_timers": timers, "tuned": srv.tuned,
            "config": {"workload": f"poisson {args.rate}/s, {args.requests} requests, N in 20/24/28/32, seed 3",
-                      "tile_rows": args.serve_tile,
+                      "tile_rows": args.serve_tile, "reorth": "partial" if args.batch_reorth else "every step",
                       "res_tol": args.res_tol, "max_iterations": 300, "vectors": "c64 Krylov, f64 alpha/beta/RQ"}}
     print(json.dumps(out), flush=True)
     return 0
@@ -654,7 +655,7 @@ def run_batch(args):
     torch.cuda.synchronize()
     t_build = time.perf_counter() - t0
     # the library's autotuner picks the tiles on a few steps of the whole batch
-    B = BatchSolver()
+    B = BatchSolver(reorth=args.batch_reorth)
     t1 = time.perf_counter()
     for k, sec in enumerate(secs):
         B.add(sec, n_ev=3, max_iterations=150, tol=0.0, seed=2, tag=k)
@@ -681,7 +682,8 @@ def run_batch(args):
            "plain_fp64_seconds_per_sector": float(np.mean(pt)),
            "speedup_vs_sequential_plain": float(np.mean(pt)) * n / t_solve,
            "config": {"workload": f"{args.hamiltonians} Hamiltonians (4x4 square / 5x4 triangular), all momenta, "
-                                  "Sz=0, seed 2", "iterations": 150, "n_ev": 3}}
+                                  "Sz=0, seed 2", "iterations": 150, "n_ev": 3,
+                      "reorth": "partial" if args.batch_reorth else "every step"}}
     print(json.dumps(out), flush=True)
     return 0
 
@@ -813,6 +815,10 @@ def main():
     ap.add_argument("--reorth", type=int, default=1,
                     help="precision/solve: 1 reorthogonalise every step, 0 locally against the last two vectors")
     ap.add_argument("--serve-tile", type=int, default=4096, help="serve: rows per tile of the batch kernels")
+    ap.add_argument("--serve-tune", type=int, default=1, choices=[0, 1],
+                    help="serve: time the batch tiles on the first requests (1) or keep --serve-tile (0)")
+    ap.add_argument("--batch-reorth", type=int, default=0, choices=[0, 1],
+                    help="serve/batch: reorthogonalise every step (0) or partially (1)")
     ap.add_argument("--ingest-ncu", metavar="CSV", default=None,
                     help="record the DRAM bytes per launch of --kernel from this ncu CSV in profiles/traffic.json "
                          "under --tag, and exit")

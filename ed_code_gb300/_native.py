@@ -60,7 +60,7 @@ class edg_sector_info(C.Structure):
 
 
 class edg_batch_opts(C.Structure):
-    _fields_ = [("tile_rows", C.c_int), ("lanes_per_row", C.c_int), ("check_every", C.c_int)]
+    _fields_ = [("tile_rows", C.c_int), ("lanes_per_row", C.c_int), ("check_every", C.c_int), ("reorth", C.c_int)]
 
 
 class edg_batch_request(C.Structure):
@@ -70,7 +70,8 @@ class edg_batch_request(C.Structure):
 
 class edg_batch_result(C.Structure):
     _fields_ = [("tag", C.c_int64), ("status", C.c_int), ("n_found", C.c_int), ("iterations", C.c_int),
-                ("converged", C.c_int), ("eigs", C.c_double * 32), ("ritz", C.c_double * 32),
+                ("converged", C.c_int), ("reorth_steps", C.c_int), ("reserved", C.c_int),
+                ("eigs", C.c_double * 32), ("ritz", C.c_double * 32),
                 ("residuals", C.c_double * 32)]
 
 

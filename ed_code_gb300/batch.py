@@ -17,9 +17,11 @@ from . import _native as N
 
 
 class BatchSolver:
-    def __init__(self, tile_rows: int = 1024, lanes_per_row: int = 8, check_every: int = 10):
+    def __init__(self, tile_rows: int = 1024, lanes_per_row: int = 8, check_every: int = 10, reorth: int = 0):
+        """reorth: 0 reorthogonalises every step; 1 only where Simon's
+        estimates of the lost orthogonality call for it (partial)."""
         h = C.c_void_p()
-        opts = N.edg_batch_opts(int(tile_rows), int(lanes_per_row), int(check_every))
+        opts = N.edg_batch_opts(int(tile_rows), int(lanes_per_row), int(check_every), int(reorth))
         N.check(N.lib().edg_batch_create(C.byref(opts), C.byref(h)))
         self._h = h
         self._sectors: Dict[int, object] = {}  # tag -> sector, kept alive until polled
@@ -76,6 +78,7 @@ class BatchSolver:
                 k = r.n_found
                 out.append({"tag": int(r.tag), "status": int(r.status), "n_found": k,
                             "iterations": int(r.iterations), "converged": bool(r.converged),
+                            "reorth_steps": int(r.reorth_steps),
                             "eigs": np.array(r.eigs[:k]), "ritz": np.array(r.ritz[:k]),
                             "residuals": np.array(r.residuals[:k])})
                 self._sectors.pop(int(r.tag), None)

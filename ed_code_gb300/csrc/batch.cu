@@ -94,6 +94,7 @@ struct SegDev {
   double* q;              // 2 (m_max + 1): reorthogonalisation coefficients
   double* ywork;          // want x 6 m_max: Ritz coefficients + inverse-iteration work
   double* aux;            // [0]: |w|^2 before reorthogonalisation
+  double* omega;          // partial reorthogonalisation: 2 x (m_max + 2) estimates (nullptr: every step)
   int64_t n;
   int m_max, want, check_every;
   int pack_cb;            // column bits of packed entries (vid == nullptr)
@@ -104,7 +105,9 @@ struct SegState {
   int j;       // steps taken
   int status;  // kRunning, kConverged, kMaxedOut, kCancelled (set on the host)
   int redo;    // this step's second Gram-Schmidt pass is needed
-  int pad;
+  int orth;    // this step's first Gram-Schmidt pass runs (always without omega)
+  int force;   // partial reorthogonalisation: the next step reorthogonalises too
+  int n_orth;  // steps that reorthogonalised
 };
 
 struct TileDev {
@@ -248,9 +251,68 @@ __global__ void __launch_bounds__(kThreads) k_b_hv(const SegDev* __restrict__ se
   }
 }
 
+// Partial reorthogonalisation (Simon, "The Lanczos algorithm with partial
+// reorthogonalization", Math. Comp. 42 (1984) 115): omega_{j,k} estimates
+// v_j^H v_k from T alone,
+//   beta_{j+1} omega_{j+1,k} = beta_{k+1} omega_{j,k+1} + (alpha_k - alpha_j) omega_{j,k}
+//                              + beta_k omega_{j,k-1} - beta_j omega_{j-1,k} + theta_{j,k},
+// with omega_{k,k} = 1, omega_{k+1,k} = psi (the local level) and a rounding
+// term theta = eps (beta_{k+1} + beta_{j+1}) taken with the sign that makes
+// |omega| grow.  eps is the unit roundoff of the FP32 Krylov vectors.  When
+// an estimate passes sqrt(eps), w is reorthogonalised against all stored
+// vectors at this step and the next (the vector before it carries the same
+// loss), and the estimates of the new vector fall back to eps.  Between
+// such steps the first Gram-Schmidt pass is skipped.  beta_{j+1} here is |w|
+// before the reorthogonalisation.  One CTA (the segment's last of k_b_step)
+// updates the estimates; they live in two rows of S.omega by the parity of j.
+__device__ void pro_update(const SegDev& S, SegState& st, int j, double w2) {
+  constexpr double kEps = 5.9604644775390625e-08;  // 2^-24
+  const double delta = sqrt(kEps);
+  const int ld = S.m_max + 2;
+  double* cur = S.omega + (int64_t)(j & 1) * ld;        // omega_{j, .}
+  double* nxt = S.omega + (int64_t)((j + 1) & 1) * ld;  // omega_{j-1, .} in, omega_{j+1, .} out
+  const double bt = fmax(sqrt(w2), 1e-300);
+  const double aj = __ldcg(S.alpha + j), bj = j > 0 ? __ldcg(S.beta + j) : 0.0;
+  __shared__ double smax[kThreads];
+  __shared__ int s_orth;
+  if (j == 0 && threadIdx.x == 0) cur[0] = 1.0;
+  __syncthreads();
+  double mx = 0.0;
+  for (int k = threadIdx.x; k < j; k += blockDim.x) {
+    const double bk1 = __ldcg(S.beta + k + 1);
+    double x = bk1 * __ldcg(cur + k + 1) + (__ldcg(S.alpha + k) - aj) * __ldcg(cur + k) - bj * __ldcg(nxt + k);
+    if (k > 0) x += __ldcg(S.beta + k) * __ldcg(cur + k - 1);
+    x = (x + copysign(kEps * (bk1 + bt), x)) / bt;
+    nxt[k] = x;
+    mx = fmax(mx, fabs(x));
+  }
+  smax[threadIdx.x] = mx;
+  __syncthreads();
+  for (int h = kThreads / 2; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) smax[threadIdx.x] = fmax(smax[threadIdx.x], smax[threadIdx.x + h]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const bool cross = smax[0] > delta;
+    const bool orth = cross || st.force;
+    st.orth = orth ? 1 : 0;
+    st.force = cross ? 1 : 0;
+    if (orth) ++st.n_orth;
+    else st.redo = 0;
+    nxt[j] = kEps * (fabs(aj) + bj + bt) / bt;
+    nxt[j + 1] = 1.0;
+    s_orth = orth;
+  }
+  __syncthreads();
+  if (s_orth)
+    for (int k = threadIdx.x; k < j; k += blockDim.x) nxt[k] = kEps;
+}
+
 // w -= alpha_j V_j + beta_j V_{j-1}, and |w|^2 (tile partials of the stored
-// values, closed per segment by the last CTA into aux[0])
-__global__ void __launch_bounds__(kThreads) k_b_step(const SegDev* __restrict__ segs, const SegState* __restrict__ ss,
+// values, closed per segment by the last CTA into aux[0]); then whether this
+// step reorthogonalises (every step, or by the partial-reorthogonalisation
+// estimates)
+__global__ void __launch_bounds__(kThreads) k_b_step(const SegDev* __restrict__ segs, SegState* __restrict__ ss,
                                                      const TileDev* __restrict__ tiles, const int* __restrict__ tb,
                                                      double* __restrict__ part, int* __restrict__ cnt) {
   const TileDev t = tiles[blockIdx.x];
@@ -280,6 +342,12 @@ __global__ void __launch_bounds__(kThreads) k_b_step(const SegDev* __restrict__ 
   if (last_cta(cnt + kCnts * t.seg + kCntNorm, k1 - k0)) {
     seg_sum(part, k0, k1, s2, z);
     if (threadIdx.x == 0) S.aux[0] = s2;
+    if (S.omega) {
+      pro_update(S, ss[t.seg], j, s2);
+    } else if (threadIdx.x == 0) {
+      ss[t.seg].orth = 1;
+      ++ss[t.seg].n_orth;
+    }
   }
 }
 
@@ -318,7 +386,7 @@ __global__ void __launch_bounds__(kThreads) k_b_cgs_dot(const SegDev* __restrict
   constexpr int kWarps = kThreads / 32;
   const TileDev t = tiles[blockIdx.x];
   const SegDev& S = segs[t.seg];
-  const bool run = ss[t.seg].status == kRunning && (pass == 0 || ss[t.seg].redo);
+  const bool run = ss[t.seg].status == kRunning && (pass == 0 ? ss[t.seg].orth : ss[t.seg].redo);
   const int K = run ? ss[t.seg].j + 1 : 0;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const float2* __restrict__ w = S.w + t.row0;
@@ -373,7 +441,7 @@ __global__ void __launch_bounds__(kThreads) k_b_cgs_finish(const SegDev* __restr
                                                            const int* __restrict__ tb, int n_tiles,
                                                            const double* __restrict__ part, int pass,
                                                            int* __restrict__ cnt) {
-  if (ss[blockIdx.x].status != kRunning || (pass == 1 && !ss[blockIdx.x].redo)) return;
+  if (ss[blockIdx.x].status != kRunning || !(pass == 0 ? ss[blockIdx.x].orth : ss[blockIdx.x].redo)) return;
   const SegDev& S = segs[blockIdx.x];
   const int K = ss[blockIdx.x].j + 1;
   for (int k = blockIdx.y; k < K; k += kCgsY) {
@@ -409,7 +477,7 @@ __global__ void __launch_bounds__(kThreads) k_b_cgs_sub(const SegDev* __restrict
                                                         int* __restrict__ cnt) {
   const TileDev t = tiles[blockIdx.x];
   if (ss[t.seg].status != kRunning) return;
-  const bool sub = pass == 0 || ss[t.seg].redo;
+  const bool sub = pass == 0 ? ss[t.seg].orth : ss[t.seg].redo;
   if (!sub && pass == 0) return;
   const SegDev& S = segs[t.seg];
   __shared__ float sq[2 * (kMaxSteps + 1)];
@@ -529,7 +597,7 @@ struct Segment {
 };
 
 void release(Segment& g) {
-  void* p[] = {g.d.V, g.d.w, g.d.u, g.d.alpha, g.d.beta, g.d.q, g.d.ywork, g.d.aux};
+  void* p[] = {g.d.V, g.d.w, g.d.u, g.d.alpha, g.d.beta, g.d.q, g.d.ywork, g.d.aux, g.d.omega};
   for (void* x : p)
     if (x) cudaFree(x);
   g.d = SegDev{};
@@ -578,8 +646,19 @@ struct Batch {
 
 namespace {
 
+// Rows per tile of a segment: the batch's tile_rows, raised for a segment
+// that would otherwise be cut into more than kMaxSegTiles tiles (a tuner
+// that chose small tiles on small sectors must not cut a large one into tens
+// of thousands).  It depends on the segment alone, so a segment's arithmetic
+// is the same in any mix.
+constexpr int64_t kMaxSegTiles = 4096;
+int64_t seg_tile_rows(int tile_rows, int64_t n) {
+  const int64_t need = (n + kMaxSegTiles - 1) / kMaxSegTiles;
+  return std::max<int64_t>(tile_rows, (need + 31) / 32 * 32);
+}
+
 int64_t segment_bytes(int64_t n, int m, int want) {
-  return (int64_t)sizeof(float2) * n * (m + 3) + (int64_t)sizeof(double) * (4 * (m + 2) + 6 * (int64_t)want * m);
+  return (int64_t)sizeof(float2) * n * (m + 3) + (int64_t)sizeof(double) * (6 * (m + 2) + 6 * (int64_t)want * m);
 }
 
 // copy the device step counters and statuses into the host mirror
@@ -699,6 +778,7 @@ void finish_stopped(Batch& B) {
     r.tag = g.req.tag;
     r.iterations = g.st.j;
     r.converged = g.st.status == kConverged;
+    r.reorth_steps = g.st.n_orth;
     r.status = status[i];
     if (status[i] == EDG_OK) {
       const int na = sel[i].na;
@@ -737,13 +817,13 @@ int rebuild(Batch& B) {
   std::vector<SegState> ss;
   std::vector<TileDev> tiles;
   std::vector<int> tb;
-  const int rows = B.opts.tile_rows;
   int m_cap = 1;
   for (size_t k = 0; k < B.segs.size(); ++k) {
     sd.push_back(B.segs[k].d);
     ss.push_back(B.segs[k].st);
     m_cap = std::max(m_cap, B.segs[k].d.m_max);
     tb.push_back((int)tiles.size());
+    const int64_t rows = seg_tile_rows(B.opts.tile_rows, B.segs[k].d.n);
     for (int64_t r0 = 0; r0 < B.segs[k].d.n; r0 += rows)
       tiles.push_back(TileDev{(int)k, (int)std::min<int64_t>(rows, B.segs[k].d.n - r0), r0});
   }
@@ -843,6 +923,10 @@ int edg_batch_create(const edg_batch_opts* opts, edg_batch** out) {
   o.tile_rows = std::max(32, std::min(o.tile_rows, 1 << 20));
   if (o.lanes_per_row != 8 && o.lanes_per_row != 16 && o.lanes_per_row != 32) o.lanes_per_row = 8;
   if (o.check_every <= 0) o.check_every = 10;
+  if (o.reorth != 0 && o.reorth != 1) {
+    delete h;
+    return fail(EDG_ERR_INVALID, "batch: reorth must be 0 (every step) or 1 (partial)");
+  }
   if (cudaStreamCreateWithFlags(&h->b.st, cudaStreamNonBlocking) != cudaSuccess) {
     delete h;
     return fail(EDG_ERR_CUDA, "batch stream");
@@ -902,6 +986,7 @@ int edg_batch_add(edg_batch* bh, edg_sector* sec, const edg_batch_request* req) 
   if (e == cudaSuccess) e = cudaMalloc(&d.q, sizeof(double) * 2 * (m + 1));
   if (e == cudaSuccess) e = cudaMalloc(&d.ywork, sizeof(double) * 6 * (size_t)d.want * m);
   if (e == cudaSuccess) e = cudaMalloc(&d.aux, sizeof(double) * 2);
+  if (e == cudaSuccess && B.opts.reorth == 1) e = cudaMalloc(&d.omega, sizeof(double) * 2 * (m + 2));
   if (e != cudaSuccess) {
     cudaGetLastError();
     release(g);

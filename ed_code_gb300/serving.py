@@ -140,13 +140,14 @@ class Server:
     relative of the FP64 ones for these models (checked by the tests).
     build_ahead: build admitted requests' sectors on a builder thread while
     the batch steps (False: build them in the loop).  tune: before the first
-    step, time the batch's tile sizes and lanes per row on the requests
-    admitted first (edg_batch_tune) and keep the fastest; ``tuned`` then
-    holds the choice (otherwise tile_rows and lanes_per_row stay)."""
+    step of each run(), time the batch's tile sizes and lanes per row on the
+    requests admitted first (edg_batch_tune) and keep the fastest; ``tuned`` then
+    holds the choice (otherwise tile_rows and lanes_per_row stay).  reorth:
+    the batch's reorthogonalisation (0: every step, 1: partial)."""
 
     def __init__(self, hbm_budget: Optional[int] = None, max_iterations: int = 300, res_tol: float = 1e-6,
                  tile_rows: int = 4096, lanes_per_row: int = 8, check_every: int = 10, max_active: int = 4096,
-                 build_ahead: bool = True, tune: bool = True):
+                 build_ahead: bool = True, tune: bool = True, reorth: int = 0):
         if hbm_budget is None:
             import torch
 
@@ -160,7 +161,8 @@ class Server:
         self.build_ahead = bool(build_ahead)
         self.tune = bool(tune)
         self.tuned: Optional[dict] = None
-        self.batch = BatchSolver(tile_rows=tile_rows, lanes_per_row=lanes_per_row, check_every=check_every)
+        self.batch = BatchSolver(tile_rows=tile_rows, lanes_per_row=lanes_per_row, check_every=check_every,
+                                 reorth=reorth)
         self.peak_live = 0
         self.peak_bytes = 0
         self.create_seconds = 0.0   # sector construction (basis and stored rows)
@@ -195,6 +197,8 @@ class Server:
     def run(self, requests: Sequence[Request], clock: Callable[[], float] = time.perf_counter,
             on_result: Optional[Callable[[Served], None]] = None) -> List[Served]:
         pending = sorted(requests, key=lambda r: r.arrival)
+        if self.tune:
+            self.tuned = None  # each stream is tuned on its own first requests
         queue: List[Request] = []
         live: Dict[int, tuple] = {}       # rid -> (request, sector, bytes, admitted)
         building: Dict[int, tuple] = {}   # rid -> (request, bytes, admitted)

@@ -17,7 +17,7 @@
 extern "C" {
 #endif
 
-#define EDGPU_ABI_VERSION 7
+#define EDGPU_ABI_VERSION 8
 
 enum {
   EDG_OK = 0,
@@ -256,7 +256,7 @@ int edg_solve_mixed(edg_sector* s, const edg_mixed_opts* opts, double* eigs, dou
  * (sector_lanczos in a loop over momenta, ED.cpp:120-131).  Each segment is a
  * sector with stored rows and a request; every Lanczos step of all live
  * segments is one replay of a captured CUDA graph.  FP32 Krylov vectors
- * (reorthogonalised every step), FP64 alpha/beta, FP64 Rayleigh quotients and
+ * (reorthogonalised every step, or partially: opts.reorth), FP64 alpha/beta, FP64 Rayleigh quotients and
  * residuals as in edg_solve_mixed.  A segment stops when the residual bounds
  * of its wanted Ritz pairs are below tol * max(1, |theta|) (tested every
  * check_every steps) or after max_iterations steps, and is then finished and
@@ -266,6 +266,9 @@ typedef struct {
   int tile_rows;      /* rows per CTA tile (0: 1024) */
   int lanes_per_row;  /* lanes per stored row: 8, 16 or 32 (0: 8) */
   int check_every;    /* steps between convergence tests (0: 10) */
+  int reorth;         /* 0: reorthogonalise every step; 1: partial reorthogonalisation
+                         (only the steps where estimates of the lost orthogonality,
+                         from alpha/beta alone, pass sqrt(eps_FP32), and the step after) */
 } edg_batch_opts;
 
 typedef struct {
@@ -282,6 +285,8 @@ typedef struct {
   int n_found;         /* distinct levels returned (<= n_ev) */
   int iterations;      /* Lanczos steps taken */
   int converged;       /* 1: stopped by the tolerance, 0: by max_iterations */
+  int reorth_steps;    /* steps that reorthogonalised against the stored vectors */
+  int reserved;
   double eigs[32];     /* FP64 Rayleigh quotients, ascending */
   double ritz[32];     /* the Ritz values of T they came from */
   double residuals[32];/* |Hx - eig x| / |x| in FP64 */

@@ -42,7 +42,7 @@ def test_python_binding_covers_every_symbol():
 
 def test_abi_version_and_error_string(libedgpu):
     libedgpu.edg_abi_version.restype = ctypes.c_int
-    assert libedgpu.edg_abi_version() == 7
+    assert libedgpu.edg_abi_version() == 8
     libedgpu.edg_last_error.restype = ctypes.c_char_p
     assert isinstance(libedgpu.edg_last_error(), bytes)
 

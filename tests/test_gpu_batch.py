@@ -39,9 +39,12 @@ CASES = [("sq4x4", 0, 3), ("sq4x4_j2", 0, 3), ("sq4x4_j2", 1, 3), ("sq4x4_phase_
          ("tri4x3", 4, 3), ("tri4x3_relabel", 1, 2), ("sq6x4_k00", 0, 3), ("tri6x4_k10", 0, 2)]
 
 
-def test_batch_matches_reference(mods):
+@pytest.mark.parametrize("reorth", [0, 1])
+def test_batch_matches_reference(mods, reorth):
+    """Every step reorthogonalised (0) or partially (1): the same eigenvalues
+    to 1e-9; the partial form reorthogonalises on fewer steps."""
     batch, sector = mods
-    B = batch.BatchSolver(tile_rows=512)
+    B = batch.BatchSolver(tile_rows=512, reorth=reorth)
     secs = {}
     for k, (name, idx, n_ev) in enumerate(CASES):
         secs[k] = stored_sector(sector, name, idx)
@@ -57,17 +60,22 @@ def test_batch_matches_reference(mods):
         rel = np.abs(r["eigs"][:n] - ref[:n]) / np.abs(ref[:n])
         assert rel.max() <= REL_TOL, (name, r["eigs"], ref[:n])
         assert r["iterations"] == min(200, secs[k].n_p)
+        if reorth == 0:
+            assert r["reorth_steps"] == r["iterations"], r
+        elif r["iterations"] >= 150:
+            assert 0 < r["reorth_steps"] < r["iterations"], (name, r["reorth_steps"])
 
 
-def test_alone_equals_in_mix(mods):
+@pytest.mark.parametrize("reorth", [0, 1])
+def test_alone_equals_in_mix(mods, reorth):
     """A segment's arithmetic reads only its own tiles: joining a batch whose
     composition changes before, during and after it gives the same bits."""
     batch, sector = mods
     a = stored_sector(sector, "sq6x4_k00", 0)
-    B1 = batch.BatchSolver(tile_rows=512)
+    B1 = batch.BatchSolver(tile_rows=512, reorth=reorth)
     B1.add(a, n_ev=2, max_iterations=120, tol=0.0, seed=7, tag=0)
     alone = B1.run()[0]
-    B2 = batch.BatchSolver(tile_rows=512)
+    B2 = batch.BatchSolver(tile_rows=512, reorth=reorth)
     others = [stored_sector(sector, "sq4x4", 0), stored_sector(sector, "tri6x4_k10", 0),
               stored_sector(sector, "sq4x4_j2", 1)]
     B2.add(others[0], n_ev=3, max_iterations=60, tol=0.0, seed=3, tag=10)
@@ -81,12 +89,14 @@ def test_alone_equals_in_mix(mods):
     assert mixed[0]["iterations"] == alone["iterations"] == 120
     assert np.array_equal(mixed[0]["eigs"], alone["eigs"])
     assert np.array_equal(mixed[0]["residuals"], alone["residuals"])
+    assert mixed[0]["reorth_steps"] == alone["reorth_steps"]
 
 
-def test_tolerance_stops_early(mods):
+@pytest.mark.parametrize("reorth", [0, 1])
+def test_tolerance_stops_early(mods, reorth):
     batch, sector = mods
     sec = stored_sector(sector, "sq6x4_k00", 0)
-    B = batch.BatchSolver(tile_rows=1024, check_every=5)
+    B = batch.BatchSolver(tile_rows=1024, check_every=5, reorth=reorth)
     B.add(sec, n_ev=2, max_iterations=400, tol=1e-6, seed=1)
     r = B.run()[0]
     assert r["converged"] and r["iterations"] < 400, r
@@ -109,9 +119,12 @@ def test_batch_rejects_bad_requests(mods):
         B.add(plain, n_ev=1, max_iterations=1000)
     assert B.info()["active"] == 0
     assert B.footprint(plain, 2, 50) > 0
+    with pytest.raises(EdgError, match="reorth"):
+        batch.BatchSolver(reorth=2)
 
 
-def test_large_segment_matches_single_sector_solver(mods):
+@pytest.mark.parametrize("reorth", [0, 1])
+def test_large_segment_matches_single_sector_solver(mods, reorth):
     """A segment of 5.2e6 rows (tiles of 4096, the Gram-Schmidt dots summed
     per tile by one warp per Krylov vector): its levels agree with the
     single-sector FP32 solver with full reorthogonalisation (itself within
@@ -122,12 +135,12 @@ def test_large_segment_matches_single_sector_solver(mods):
     sec = sector.GpuSector(L.make_model(L.TorusSpec("triangular", 6, 5, Jz=0.8, Ch=0.2), 0, 2, 3, bowties=False))
     assert sec.n_p >= 1 << 20 and sec.build_targets()
     ref = sec.solve_mixed(n_ev=3, iterations=150, reorth_every=1, seed=2)["eigs"]
-    B = batch.BatchSolver(tile_rows=4096)
+    B = batch.BatchSolver(tile_rows=4096, reorth=reorth)
     B.add(sec, n_ev=3, max_iterations=150, tol=0.0, seed=2, tag=0)
     r = B.run()[0]
     assert r["status"] == 0 and r["n_found"] >= 3, r
     rel = np.abs(r["eigs"][:3] - ref[:3]) / np.abs(ref[:3])
-    assert rel.max() <= REL_TOL, (r["eigs"], ref)
+    assert rel.max() <= REL_TOL, (r["eigs"], ref, r["reorth_steps"])
 
 
 def test_cancel_releases_a_segment_and_leaves_the_others(mods):
