@@ -817,8 +817,8 @@ def main():
     ap.add_argument("--serve-tile", type=int, default=4096, help="serve: rows per tile of the batch kernels")
     ap.add_argument("--serve-tune", type=int, default=1, choices=[0, 1],
                     help="serve: time the batch tiles on the first requests (1) or keep --serve-tile (0)")
-    ap.add_argument("--batch-reorth", type=int, default=0, choices=[0, 1],
-                    help="serve/batch: reorthogonalise every step (0) or partially (1)")
+    ap.add_argument("--batch-reorth", type=int, default=1, choices=[0, 1],
+                    help="serve/batch: reorthogonalise partially (1, the serving loop's default) or every step (0)")
     ap.add_argument("--ingest-ncu", metavar="CSV", default=None,
                     help="record the DRAM bytes per launch of --kernel from this ncu CSV in profiles/traffic.json "
                          "under --tag, and exit")

@@ -36,8 +36,11 @@
 // finish (a ticket counter, below), so no kernel exists only to reduce and
 // no CTA waits for another.
 
-// The vectors are reorthogonalised every step: with FP32 vectors the copies
-// of converged levels otherwise appear within a few steps.  A stopped segment
+// The vectors are reorthogonalised every step against all stored vectors
+// (with FP32 vectors the copies of converged levels otherwise appear within a
+// few steps), or, with opts.reorth = 1, against v_{j-1} and v_j every step and
+// against all of them only on the steps where Simon's estimates of the lost
+// orthogonality call for it (pro_update below).  A stopped segment
 // is finished with the single-sector solver's code (MixedFinish): Ritz
 // vectors in FP64, one FP64 H*v each for the Rayleigh quotient (the returned
 // eigenvalue) and its residual.
@@ -105,9 +108,9 @@ struct SegState {
   int j;       // steps taken
   int status;  // kRunning, kConverged, kMaxedOut, kCancelled (set on the host)
   int redo;    // this step's second Gram-Schmidt pass is needed
-  int orth;    // this step's first Gram-Schmidt pass runs (always without omega)
-  int force;   // partial reorthogonalisation: the next step reorthogonalises too
-  int n_orth;  // steps that reorthogonalised
+  int kf;      // this step's Gram-Schmidt runs over V_kf..V_j: 0 (full) or j-1 (local)
+  int force;   // partial reorthogonalisation: the next step reorthogonalises fully too
+  int n_orth;  // steps that reorthogonalised fully
 };
 
 struct TileDev {
@@ -256,15 +259,16 @@ __global__ void __launch_bounds__(kThreads) k_b_hv(const SegDev* __restrict__ se
 // v_j^H v_k from T alone,
 //   beta_{j+1} omega_{j+1,k} = beta_{k+1} omega_{j,k+1} + (alpha_k - alpha_j) omega_{j,k}
 //                              + beta_k omega_{j,k-1} - beta_j omega_{j-1,k} + theta_{j,k},
-// with omega_{k,k} = 1, omega_{k+1,k} = psi (the local level) and a rounding
-// term theta = eps (beta_{k+1} + beta_{j+1}) taken with the sign that makes
-// |omega| grow.  eps is the unit roundoff of the FP32 Krylov vectors.  When
-// an estimate passes sqrt(eps), w is reorthogonalised against all stored
+// with omega_{k,k} = 1 and a rounding term theta = eps (|alpha_k| + beta_{k+1}
+// + |alpha_j| + beta_{j+1}) taken with the sign that makes |omega| grow; eps
+// is the unit roundoff of the FP32 Krylov vectors.  Every step w is
+// reorthogonalised locally, against v_{j-1} and v_j (two vectors), so the
+// estimates against those two restart at eps.  When an estimate against an
+// older vector passes sqrt(eps), w is reorthogonalised against all stored
 // vectors at this step and the next (the vector before it carries the same
-// loss), and the estimates of the new vector fall back to eps.  Between
-// such steps the first Gram-Schmidt pass is skipped.  beta_{j+1} here is |w|
-// before the reorthogonalisation.  One CTA (the segment's last of k_b_step)
-// updates the estimates; they live in two rows of S.omega by the parity of j.
+// loss), and its estimates fall back to eps.  beta_{j+1} here is |w| before
+// the reorthogonalisation.  One CTA (the segment's last of k_b_step) updates
+// the estimates; they live in two rows of S.omega by the parity of j.
 __device__ void pro_update(const SegDev& S, SegState& st, int j, double w2) {
   constexpr double kEps = 5.9604644775390625e-08;  // 2^-24
   const double delta = sqrt(kEps);
@@ -274,15 +278,15 @@ __device__ void pro_update(const SegDev& S, SegState& st, int j, double w2) {
   const double bt = fmax(sqrt(w2), 1e-300);
   const double aj = __ldcg(S.alpha + j), bj = j > 0 ? __ldcg(S.beta + j) : 0.0;
   __shared__ double smax[kThreads];
-  __shared__ int s_orth;
+  __shared__ int s_full;
   if (j == 0 && threadIdx.x == 0) cur[0] = 1.0;
   __syncthreads();
   double mx = 0.0;
-  for (int k = threadIdx.x; k < j; k += blockDim.x) {
-    const double bk1 = __ldcg(S.beta + k + 1);
-    double x = bk1 * __ldcg(cur + k + 1) + (__ldcg(S.alpha + k) - aj) * __ldcg(cur + k) - bj * __ldcg(nxt + k);
+  for (int k = threadIdx.x; k + 1 < j; k += blockDim.x) {  // k <= j - 2: older than the local pair
+    const double bk1 = __ldcg(S.beta + k + 1), ak = __ldcg(S.alpha + k);
+    double x = bk1 * __ldcg(cur + k + 1) + (ak - aj) * __ldcg(cur + k) - bj * __ldcg(nxt + k);
     if (k > 0) x += __ldcg(S.beta + k) * __ldcg(cur + k - 1);
-    x = (x + copysign(kEps * (bk1 + bt), x)) / bt;
+    x = (x + copysign(kEps * (fabs(ak) + bk1 + fabs(aj) + bt), x)) / bt;
     nxt[k] = x;
     mx = fmax(mx, fabs(x));
   }
@@ -294,18 +298,18 @@ __device__ void pro_update(const SegDev& S, SegState& st, int j, double w2) {
   }
   if (threadIdx.x == 0) {
     const bool cross = smax[0] > delta;
-    const bool orth = cross || st.force;
-    st.orth = orth ? 1 : 0;
+    const bool full = cross || st.force;
+    st.kf = full ? 0 : (j > 0 ? j - 1 : 0);
     st.force = cross ? 1 : 0;
-    if (orth) ++st.n_orth;
-    else st.redo = 0;
-    nxt[j] = kEps * (fabs(aj) + bj + bt) / bt;
+    if (full) ++st.n_orth;
+    if (j > 0) nxt[j - 1] = kEps;  // the local reorthogonalisation
+    nxt[j] = kEps;
     nxt[j + 1] = 1.0;
-    s_orth = orth;
+    s_full = full;
   }
   __syncthreads();
-  if (s_orth)
-    for (int k = threadIdx.x; k < j; k += blockDim.x) nxt[k] = kEps;
+  if (s_full)
+    for (int k = threadIdx.x; k + 1 < j; k += blockDim.x) nxt[k] = kEps;
 }
 
 // w -= alpha_j V_j + beta_j V_{j-1}, and |w|^2 (tile partials of the stored
@@ -345,7 +349,7 @@ __global__ void __launch_bounds__(kThreads) k_b_step(const SegDev* __restrict__ 
     if (S.omega) {
       pro_update(S, ss[t.seg], j, s2);
     } else if (threadIdx.x == 0) {
-      ss[t.seg].orth = 1;
+      ss[t.seg].kf = 0;
       ++ss[t.seg].n_orth;
     }
   }
@@ -386,11 +390,11 @@ __global__ void __launch_bounds__(kThreads) k_b_cgs_dot(const SegDev* __restrict
   constexpr int kWarps = kThreads / 32;
   const TileDev t = tiles[blockIdx.x];
   const SegDev& S = segs[t.seg];
-  const bool run = ss[t.seg].status == kRunning && (pass == 0 ? ss[t.seg].orth : ss[t.seg].redo);
-  const int K = run ? ss[t.seg].j + 1 : 0;
+  const bool run = ss[t.seg].status == kRunning && (pass == 0 || ss[t.seg].redo);
+  const int K = run ? ss[t.seg].j + 1 : 0, kf = ss[t.seg].kf;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const float2* __restrict__ w = S.w + t.row0;
-  for (int k = blockIdx.y * kWarps + wid; k < K; k += kCgsY * kWarps) {
+  for (int k = kf + blockIdx.y * kWarps + wid; k < K; k += kCgsY * kWarps) {
     const float2* __restrict__ x = S.V + (int64_t)k * S.n + t.row0;
     KahanAcc sr, si;
     int r = lane;
@@ -441,10 +445,10 @@ __global__ void __launch_bounds__(kThreads) k_b_cgs_finish(const SegDev* __restr
                                                            const int* __restrict__ tb, int n_tiles,
                                                            const double* __restrict__ part, int pass,
                                                            int* __restrict__ cnt) {
-  if (ss[blockIdx.x].status != kRunning || !(pass == 0 ? ss[blockIdx.x].orth : ss[blockIdx.x].redo)) return;
+  if (ss[blockIdx.x].status != kRunning || (pass == 1 && !ss[blockIdx.x].redo)) return;
   const SegDev& S = segs[blockIdx.x];
-  const int K = ss[blockIdx.x].j + 1;
-  for (int k = blockIdx.y; k < K; k += kCgsY) {
+  const int K = ss[blockIdx.x].j + 1, kf = ss[blockIdx.x].kf;
+  for (int k = kf + blockIdx.y; k < K; k += kCgsY) {
     double a = 0, b = 0;
     for (int t = tb[blockIdx.x] + threadIdx.x; t < tb[blockIdx.x + 1]; t += blockDim.x) {
       a += part[((int64_t)k * n_tiles + t) * 2];
@@ -458,7 +462,7 @@ __global__ void __launch_bounds__(kThreads) k_b_cgs_finish(const SegDev* __restr
   }
   if (pass == 0 && last_cta(cnt + kCnts * blockIdx.x + kCntDecide, kCgsY)) {
     double a = 0, b = 0;
-    for (int k = threadIdx.x; k < K; k += blockDim.x) {
+    for (int k = kf + threadIdx.x; k < K; k += blockDim.x) {
       const double qr = __ldcg(S.q + 2 * k), qi = __ldcg(S.q + 2 * k + 1);
       a += qr * qr + qi * qi;
     }
@@ -477,13 +481,12 @@ __global__ void __launch_bounds__(kThreads) k_b_cgs_sub(const SegDev* __restrict
                                                         int* __restrict__ cnt) {
   const TileDev t = tiles[blockIdx.x];
   if (ss[t.seg].status != kRunning) return;
-  const bool sub = pass == 0 ? ss[t.seg].orth : ss[t.seg].redo;
-  if (!sub && pass == 0) return;
+  const bool sub = pass == 0 || ss[t.seg].redo;
   const SegDev& S = segs[t.seg];
   __shared__ float sq[2 * (kMaxSteps + 1)];
-  const int K = ss[t.seg].j + 1;
+  const int K = ss[t.seg].j + 1, kf = ss[t.seg].kf;
   if (sub) {
-    for (int k = threadIdx.x; k < 2 * K; k += blockDim.x) sq[k] = (float)S.q[k];
+    for (int k = 2 * kf + threadIdx.x; k < 2 * K; k += blockDim.x) sq[k] = (float)S.q[k];
     __syncthreads();
   }
   // FP32: the q_k are tiny against |w| once the vectors are nearly orthogonal
@@ -493,7 +496,7 @@ __global__ void __launch_bounds__(kThreads) k_b_cgs_sub(const SegDev* __restrict
     const float2 y = S.w[i];
     float re = y.x, im = y.y;
     if (sub) {
-      for (int k = 0; k < K; ++k) {
+      for (int k = kf; k < K; ++k) {
         const float2 x = S.V[(int64_t)k * S.n + i];
         re = fmaf(-sq[2 * k], x.x, fmaf(sq[2 * k + 1], x.y, re));
         im = fmaf(-sq[2 * k], x.y, fmaf(-sq[2 * k + 1], x.x, im));

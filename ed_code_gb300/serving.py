@@ -143,11 +143,12 @@ class Server:
     step of each run(), time the batch's tile sizes and lanes per row on the
     requests admitted first (edg_batch_tune) and keep the fastest; ``tuned`` then
     holds the choice (otherwise tile_rows and lanes_per_row stay).  reorth:
-    the batch's reorthogonalisation (0: every step, 1: partial)."""
+    the batch's reorthogonalisation (1, the default: partial; 0: every
+    step)."""
 
     def __init__(self, hbm_budget: Optional[int] = None, max_iterations: int = 300, res_tol: float = 1e-6,
                  tile_rows: int = 4096, lanes_per_row: int = 8, check_every: int = 10, max_active: int = 4096,
-                 build_ahead: bool = True, tune: bool = True, reorth: int = 0):
+                 build_ahead: bool = True, tune: bool = True, reorth: int = 1):
         if hbm_budget is None:
             import torch
 

@@ -53,7 +53,9 @@ def test_alone_equals_in_mix(served, stream, mods):
     for req in stream[:4]:
         sec = sector.GpuSector(lattice.make_model(req.spec, req.Sz, req.kx, req.ky))
         assert sec.build_targets()
-        B = batch.BatchSolver(tile_rows=TUNED["tile_rows"], lanes_per_row=TUNED["lanes_per_row"], check_every=10)
+        # the loop's batch: the tuner's tiles, partial reorthogonalisation (its default)
+        B = batch.BatchSolver(tile_rows=TUNED["tile_rows"], lanes_per_row=TUNED["lanes_per_row"], check_every=10,
+                              reorth=1)
         B.add(sec, n_ev=req.n_ev, max_iterations=min(300, sec.n_p), tol=1e-6, seed=1 + req.rid, tag=req.rid)
         alone = B.run()[0]
         mixed = served[req.rid]
