@@ -585,6 +585,9 @@ def run_serve(args):
     srv.close()
     summ = serving.summarize(served)
     by = {s.rid: s for s in served}
+    unconverged = [[s.rid, stream[s.rid].n_sites, stream[s.rid].n_ev, s.iterations,
+                    float(max(s.residuals)) if len(s.residuals) else None]
+                   for s in served if not s.converged]
     # plain FP64, one request after another, on a seeded sample (two per size)
     rng = np.random.default_rng(5)
     sample = []
@@ -606,6 +609,7 @@ def run_serve(args):
            "unit": "solves/s", "higher_is_better": True, "n_gpus": 1, "data": "synthetic",
            "p50_s": summ["p50_s"], "p99_s": summ["p99_s"], "makespan_s": summ["makespan_s"], "wall_s": wall,
            "requests": len(served), "converged": summ["converged"],
+           "unconverged_rid_sites_nev_steps_resid": unconverged,
            "max_rel_err_vs_plain_fp64": max(errs) if errs else None, "checked": len(errs),
            "plain_fp64_seconds_per_request": {str(k): float(np.mean(v)) for k, v in sorted(plain_t.items())},
            "sequential_plain_solves_per_s": len(stream) / seq_plain if seq_plain else None,
@@ -631,15 +635,18 @@ def run_batch(args):
     rng = np.random.default_rng(2)
     specs = []
     for h in range(args.hamiltonians):
-        if rng.random() < 0.5:
+        if args.batch_shape == "tri7x4":  # 28-site sectors (1.43e6 states), the first --momenta momenta
+            spec = L.TorusSpec("triangular", 7, 4, Jz=float(rng.uniform(0.5, 1.5)), Ch=float(rng.uniform(0, 0.4)))
+        elif rng.random() < 0.5:
             spec = L.TorusSpec("square", 4, 4, Jz=float(rng.uniform(0.5, 1.5)), J2=float(rng.uniform(0, 0.5)),
                                Ch=float(rng.uniform(0, 0.4)))
         else:
             spec = L.TorusSpec("triangular", 5, 4, Jz=float(rng.uniform(0.5, 1.5)), J2=float(rng.uniform(0, 0.5)),
                                Ch=float(rng.uniform(0, 0.4)))
-        for kx in range(spec.Lx):
-            for ky in range(spec.Ly):
-                specs.append((spec, kx, ky))
+        moms = [(kx, ky) for kx in range(spec.Lx) for ky in range(spec.Ly)]
+        if args.batch_shape == "tri7x4":
+            moms = moms[: args.momenta]
+        specs += [(spec, kx, ky) for kx, ky in moms]
     t0 = time.perf_counter()
     secs = []
     t_model = t_create = 0.0
@@ -678,11 +685,13 @@ def run_batch(args):
            "solve_seconds": t_solve, "build_seconds": t_build, "batch_timers": timers,
            "build_split": {"term_lists": t_model, "sector_and_rows": t_create}, "e2e_solves_per_s": n / (t_solve + t_build),
            "tiles": choice, "tune_seconds": t_tune,
-           "max_rel_err_vs_plain_fp64": max(errs), "checked": len(errs),
-           "plain_fp64_seconds_per_sector": float(np.mean(pt)),
-           "speedup_vs_sequential_plain": float(np.mean(pt)) * n / t_solve,
-           "config": {"workload": f"{args.hamiltonians} Hamiltonians (4x4 square / 5x4 triangular), all momenta, "
-                                  "Sz=0, seed 2", "iterations": 150, "n_ev": 3,
+           "max_rel_err_vs_plain_fp64": max(errs) if errs else None, "checked": len(errs),
+           "plain_fp64_seconds_per_sector": float(np.mean(pt)) if pt else None,
+           "speedup_vs_sequential_plain": float(np.mean(pt)) * n / t_solve if pt else None,
+           "config": {"workload": (f"{args.hamiltonians} Hamiltonians (4x4 square / 5x4 triangular), all momenta, "
+                                   "Sz=0, seed 2") if args.batch_shape == "small" else
+                      f"{args.hamiltonians} 7x4 triangular Hamiltonians, {args.momenta} momenta each, Sz=0, seed 2",
+                      "iterations": 150, "n_ev": 3,
                       "reorth": "partial" if args.batch_reorth else "every step"}}
     print(json.dumps(out), flush=True)
     return 0
@@ -812,6 +821,8 @@ def main():
     ap.add_argument("--hamiltonians", type=int, default=64)
     ap.add_argument("--plain-sample", type=int, default=3)
     ap.add_argument("--momenta", type=int, default=30)
+    ap.add_argument("--batch-shape", choices=["small", "tri7x4"], default="small",
+                    help="batch: 4x4/5x4 Hamiltonians with all momenta, or 7x4 ones with --momenta momenta")
     ap.add_argument("--reorth", type=int, default=1,
                     help="precision/solve: 1 reorthogonalise every step, 0 locally against the last two vectors")
     ap.add_argument("--serve-tile", type=int, default=4096, help="serve: rows per tile of the batch kernels")

@@ -50,6 +50,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstddef>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -98,6 +99,7 @@ struct SegDev {
   double* ywork;          // want x 6 m_max: Ritz coefficients + inverse-iteration work
   double* aux;            // [0]: |w|^2 before reorthogonalisation
   double* omega;          // partial reorthogonalisation: 2 x (m_max + 2) estimates (nullptr: every step)
+  double pro_delta;       // its threshold on the estimates
   int64_t n;
   int m_max, want, check_every;
   int pack_cb;            // column bits of packed entries (vid == nullptr)
@@ -264,14 +266,18 @@ __global__ void __launch_bounds__(kThreads) k_b_hv(const SegDev* __restrict__ se
 // is the unit roundoff of the FP32 Krylov vectors.  Every step w is
 // reorthogonalised locally, against v_{j-1} and v_j (two vectors), so the
 // estimates against those two restart at eps.  When an estimate against an
-// older vector passes sqrt(eps), w is reorthogonalised against all stored
+// older vector passes eps^(3/4), w is reorthogonalised against all stored
 // vectors at this step and the next (the vector before it carries the same
-// loss), and its estimates fall back to eps.  beta_{j+1} here is |w| before
+// loss), and its estimates fall back to eps.  (Simon's sqrt(eps) keeps the
+// eigenvalues of T accurate, but with FP32 vectors it let 12 of 1,000
+// serving requests with 4 levels stop unconverged after 300 steps; eps^(3/4)
+// converged all of them at the same speed.)  beta_{j+1} here is |w| before
 // the reorthogonalisation.  One CTA (the segment's last of k_b_step) updates
 // the estimates; they live in two rows of S.omega by the parity of j.
+constexpr double kProDelta = 3.814697265625e-06;  // eps^(3/4) = 2^-18
 __device__ void pro_update(const SegDev& S, SegState& st, int j, double w2) {
   constexpr double kEps = 5.9604644775390625e-08;  // 2^-24
-  const double delta = sqrt(kEps);
+  const double delta = S.pro_delta;
   const int ld = S.m_max + 2;
   double* cur = S.omega + (int64_t)(j & 1) * ld;        // omega_{j, .}
   double* nxt = S.omega + (int64_t)((j + 1) & 1) * ld;  // omega_{j-1, .} in, omega_{j+1, .} out
@@ -524,8 +530,8 @@ __global__ void __launch_bounds__(kThreads) k_b_cgs_sub(const SegDev* __restrict
 
 // V_{j+1} = w / beta_{j+1} and u_{j+1} = V_{j+1} / norm for the next H*v;
 // then the segment's last CTA advances j and, every check_every steps, tests
-// convergence: the wanted lowest Ritz pairs of T_j (bisection and inverse
-// iteration in FP64) and their residual bounds beta_j |y_k[j-1]|.
+// convergence: the wanted lowest Ritz pairs of T_j (multisection by a warp
+// each and inverse iteration, FP64) and their residual bounds beta_j |y_k[j-1]|.
 __global__ void __launch_bounds__(kThreads) k_b_scale(const SegDev* __restrict__ segs, SegState* __restrict__ ss,
                                                       const TileDev* __restrict__ tiles, const int* __restrict__ tb,
                                                       int* __restrict__ cnt) {
@@ -559,29 +565,49 @@ __global__ void __launch_bounds__(kThreads) k_b_scale(const SegDev* __restrict__
     e[i] = i > 0 ? __ldcg(S.beta + i) : 0.0;
   }
   __syncthreads();
-  for (int k = threadIdx.x; k < S.want; k += blockDim.x) {
-    const double th = tridiag_eigenvalue(d, e, jn, k);
-    double* y = S.ywork + (int64_t)k * 6 * S.m_max;
-    tridiag_eigenvector(d, e, jn, th, y, y + S.m_max);
-    if (__ldcg(S.beta + jn) * fabs(y[jn - 1]) > S.tol * fmax(1.0, fabs(th))) ok = 0;
+  // one warp per wanted eigenvalue (multisection), then its lane 0 runs the
+  // inverse iteration
+  for (int k = threadIdx.x >> 5; k < S.want; k += blockDim.x >> 5) {
+    const double th = warp_eigenvalue(d, e, jn, k);
+    if ((threadIdx.x & 31) == 0) {
+      double* y = S.ywork + (int64_t)k * 6 * S.m_max;
+      tridiag_eigenvector(d, e, jn, th, y, y + S.m_max);
+      if (__ldcg(S.beta + jn) * fabs(y[jn - 1]) > S.tol * fmax(1.0, fabs(th))) ok = 0;
+    }
   }
   __syncthreads();
   if (threadIdx.x == 0 && ok) ss[t.seg].status = kConverged;
 }
 
-// start vector V_0 = x / |x| of one segment (one CTA), and u_0 = V_0 / norm
-__global__ void __launch_bounds__(kThreads) k_b_start(float2* __restrict__ V0, const float2* __restrict__ x,
-                                                      int64_t n, const double* __restrict__ nrm_inv,
-                                                      const uint8_t* __restrict__ lid, float2* __restrict__ u) {
+// start vector V_0 = x / |x| of one segment, and u_0 = V_0 / norm: the CTAs'
+// partials of |x|^2 (exact products in float-float), closed by the last CTA
+// in CTA order into *nrm2 (deterministic), then the scaling
+constexpr int kStartCtas = 608;
+__global__ void __launch_bounds__(kThreads) k_b_start_norm(const float2* __restrict__ x, int64_t n,
+                                                           double* __restrict__ part, int* __restrict__ cnt,
+                                                           double* __restrict__ nrm2) {
   FFAcc s;
-  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     s.add_prod(x[i].x, x[i].x);
     s.add_prod(x[i].y, x[i].y);
   }
   double a = s.value(), b = 0;
   block_sum2(a, b);
-  const FFScalar inv(1.0 / sqrt(a));
-  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+  if (threadIdx.x == 0) part[blockIdx.x] = a;
+  if (last_cta(cnt, gridDim.x)) {
+    a = 0;
+    b = 0;
+    for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) a += __ldcg(part + k);
+    block_sum2(a, b);
+    if (threadIdx.x == 0) *nrm2 = a;
+  }
+}
+__global__ void __launch_bounds__(kThreads) k_b_start(float2* __restrict__ V0, const float2* __restrict__ x,
+                                                      int64_t n, const double* __restrict__ nrm_inv,
+                                                      const uint8_t* __restrict__ lid, float2* __restrict__ u,
+                                                      const double* __restrict__ nrm2) {
+  const FFScalar inv(1.0 / sqrt(*nrm2));
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const float2 v = make_float2(fmaf(x[i].x, inv.l, __fmul_rn(x[i].x, inv.h)),
                                  fmaf(x[i].y, inv.l, __fmul_rn(x[i].y, inv.h)));
     V0[i] = v;
@@ -608,6 +634,9 @@ void release(Segment& g) {
 
 }  // namespace
 
+struct Batch;
+static cudaError_t start_vector(Batch& B, const SegDev& d);
+
 struct Batch {
   edg_batch_opts opts{};
   std::vector<Segment> segs;  // the first n_dev are in the device tables, in order
@@ -628,6 +657,8 @@ struct Batch {
   TdScratch td;                // device Ritz selection of the stopped segments
   double* ybuf = nullptr;      // their Ritz coefficients
   size_t ybuf_n = 0;
+  double* d_start = nullptr;   // start vectors: kStartCtas partials, |x|^2
+  int* d_start_cnt = nullptr;  // their ticket counter
   // host seconds: add, step (graph replays and waits), finish (T, Ritz
   // vectors, Rayleigh quotients), release, rebuild (tables and graph capture)
   double timers[5] = {0, 0, 0, 0, 0};
@@ -643,21 +674,43 @@ struct Batch {
     cudaFree(d_tb);
     cudaFree(d_part);
     cudaFree(ybuf);
+    cudaFree(d_start);
+    cudaFree(d_start_cnt);
     if (st) cudaStreamDestroy(st);
   }
 };
 
+// V_0, u_0 of a segment from the random vector in its w, on the batch's stream
+static cudaError_t start_vector(Batch& B, const SegDev& d) {
+  cudaError_t e = cudaSuccess;
+  if (!B.d_start) {
+    if ((e = cudaMalloc(&B.d_start, sizeof(double) * (kStartCtas + 1))) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&B.d_start_cnt, sizeof(int))) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(B.d_start_cnt, 0, sizeof(int), B.st)) != cudaSuccess) return e;
+  }
+  const int grid = (int)std::min<int64_t>(kStartCtas, (d.n + kThreads - 1) / kThreads);
+  k_b_start_norm<<<grid, kThreads, 0, B.st>>>(d.w, d.n, B.d_start, B.d_start_cnt, B.d_start + kStartCtas);
+  k_b_start<<<grid, kThreads, 0, B.st>>>(d.V, d.w, d.n, d.nrm_inv, d.lid, d.u, B.d_start + kStartCtas);
+  return cudaGetLastError();
+}
+
 namespace {
 
-// Rows per tile of a segment: the batch's tile_rows, raised for a segment
-// that would otherwise be cut into more than kMaxSegTiles tiles (a tuner
-// that chose small tiles on small sectors must not cut a large one into tens
-// of thousands).  It depends on the segment alone, so a segment's arithmetic
+// Rows per tile of a segment: the batch's tile_rows, raised for a larger
+// segment -- to n/64 rows up to 4096, and beyond that so that no segment has
+// more than kMaxSegTiles tiles.  A tuner that chose small tiles on the first
+// small sectors must not cut a large one into tens of thousands: the
+// Gram-Schmidt dots sum each Krylov vector over a tile with one warp, and on
+// 256-row tiles that loop is two iterations long (on a 64-request serving
+// stream the dots then took 2.3x the subtraction pass that reads the same
+// vectors).  The rule depends on the segment alone, so a segment's arithmetic
 // is the same in any mix.
 constexpr int64_t kMaxSegTiles = 4096;
 int64_t seg_tile_rows(int tile_rows, int64_t n) {
-  const int64_t need = (n + kMaxSegTiles - 1) / kMaxSegTiles;
-  return std::max<int64_t>(tile_rows, (need + 31) / 32 * 32);
+  const int64_t by_size = std::min<int64_t>(4096, (n + 63) / 64);
+  const int64_t by_count = (n + kMaxSegTiles - 1) / kMaxSegTiles;
+  const int64_t rows = std::max<int64_t>(tile_rows, std::max(by_size, by_count));
+  return (rows + 31) / 32 * 32;
 }
 
 int64_t segment_bytes(int64_t n, int m, int want) {
@@ -990,6 +1043,7 @@ int edg_batch_add(edg_batch* bh, edg_sector* sec, const edg_batch_request* req) 
   if (e == cudaSuccess) e = cudaMalloc(&d.ywork, sizeof(double) * 6 * (size_t)d.want * m);
   if (e == cudaSuccess) e = cudaMalloc(&d.aux, sizeof(double) * 2);
   if (e == cudaSuccess && B.opts.reorth == 1) e = cudaMalloc(&d.omega, sizeof(double) * 2 * (m + 2));
+  d.pro_delta = kProDelta;
   if (e != cudaSuccess) {
     cudaGetLastError();
     release(g);
@@ -1002,9 +1056,9 @@ int edg_batch_add(edg_batch* bh, edg_sector* sec, const edg_batch_request* req) 
     release(g);
     return rc;
   }
-  k_b_start<<<1, kThreads, 0, B.st>>>(d.V, d.w, n, d.nrm_inv, d.lid, d.u);
-  cudaMemsetAsync(d.beta, 0, sizeof(double) * (m + 2), B.st);
-  if ((e = cudaGetLastError()) != cudaSuccess) {
+  e = start_vector(B, d);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d.beta, 0, sizeof(double) * (m + 2), B.st);
+  if (e != cudaSuccess || (e = cudaGetLastError()) != cudaSuccess) {
     release(g);
     return cuda_fail(e, "batch: start vector");
   }
@@ -1075,7 +1129,7 @@ int edg_batch_tune(edg_batch* bh, int steps, int* tile_rows, int* lanes_per_row,
       // back to the segments' start: seeded start vectors, step 0
       for (Segment& g : B.segs) {
         if (rc == EDG_OK) rc = edg_fill_random(g.d.w, g.d.n, EDG_C64, g.req.seed, B.st);
-        k_b_start<<<1, kThreads, 0, B.st>>>(g.d.V, g.d.w, g.d.n, g.d.nrm_inv, g.d.lid, g.d.u);
+        if (rc == EDG_OK && start_vector(B, g.d) != cudaSuccess) rc = cuda_fail(cudaGetLastError(), "batch: start vector");
         cudaMemsetAsync(g.d.beta, 0, sizeof(double) * (g.d.m_max + 2), B.st);
         g.st = SegState{};
         g.st.status = kRunning;

@@ -617,12 +617,14 @@ cudaError_t MixedFinish::rayleigh_async(Sector& S, cudaStream_t st, int64_t n, i
 }
 
 // A Rayleigh quotient within 1e-8 relative of an earlier one is the same level
-// again (a copy that slipped through the test on T) and is dropped.
+// again (a copy that slipped through the test on T) and is dropped, as is a
+// Ritz vector of zero or non-finite norm (no level to report).
 void pick_levels(const std::vector<double>& rr, const std::vector<double>& th, const std::vector<int>& acc_h, int na,
                  int want, double* eigs, double* ritz, double* resid, std::vector<int>& keep) {
   keep.clear();
   for (int q = 0; q < na; ++q) {
     const double rq = rr[4 * q + 2];
+    if (!(rr[4 * q] > 0.0) || !std::isfinite(rq) || !std::isfinite(rr[4 * q + 3])) continue;
     bool dup = false;
     for (int k : keep)
       if (std::fabs(rr[4 * k + 2] - rq) <= 1e-8 * std::fabs(rq)) dup = true;

@@ -60,6 +60,42 @@ TD_HD double tridiag_eigenvalue(const double* d, const double* e, int m, int k) 
   return 0.5 * (lo + hi);
 }
 
+#if defined(__CUDACC__)
+// Multisection on the same Sturm counts by the 32 lanes of one warp: each
+// round evaluates the count at 32 interior points of the bracket and keeps
+// the sub-interval where it passes k, 33x narrower.  Same bracket, pivot
+// threshold and stopping rule as tridiag_eigenvalue; all lanes return it.
+__device__ inline double warp_eigenvalue(const double* d, const double* e, int m, int k) {
+  const int lane = threadIdx.x & 31;
+  double lo = d[0], hi = d[0], emax = 0.0;
+  for (int i = 0; i < m; ++i) {
+    const double r = (i > 0 ? fabs(e[i]) : 0.0) + (i + 1 < m ? fabs(e[i + 1]) : 0.0);
+    lo = fmin(lo, d[i] - r);
+    hi = fmax(hi, d[i] + r);
+    if (i > 0) emax = fmax(emax, fabs(e[i]));
+  }
+  const double scale = fmax(fabs(lo), fabs(hi));
+  const double pivmin = fmax(1e-300, 2.2250738585072014e-308 * fmax(1.0, emax * emax));
+  lo -= 2.2e-16 * scale + pivmin;
+  hi += 2.2e-16 * scale + pivmin;
+  for (int round = 0; round < 64; ++round) {
+    if (hi - lo <= 2.0 * 2.2204460492503131e-16 * fmax(fabs(lo), fabs(hi))) break;
+    const double x = lo + (hi - lo) * ((double)(lane + 1) / 33.0);
+    const bool inside = x > lo && x < hi;
+    const bool above = inside && sturm_count(d, e, m, x, pivmin) > k;
+    const unsigned a = __ballot_sync(0xffffffffu, above);
+    const unsigned in = __ballot_sync(0xffffffffu, inside);
+    if (in == 0u) break;  // the bracket has no interior point left
+    const int first = a ? __ffs(a) - 1 : 32;  // counts are monotone in x
+    const double xlo = __shfl_sync(0xffffffffu, x, first > 0 ? first - 1 : 0);
+    const double xhi = __shfl_sync(0xffffffffu, x, first < 32 ? first : 31);
+    if (first > 0 && ((in >> (first - 1)) & 1u)) lo = xlo;
+    if (first < 32) hi = xhi;
+  }
+  return 0.5 * (lo + hi);
+}
+#endif
+
 // Eigenvector of eigenvalue lam, normalised, written to x[0..m-1].  Work
 // arrays: 5*m doubles in `wk`.  The sign is fixed so that the largest
 // component is positive.  For a level of a cluster of (nearly) equal

@@ -268,7 +268,7 @@ typedef struct {
   int check_every;    /* steps between convergence tests (0: 10) */
   int reorth;         /* 0: reorthogonalise every step; 1: partial reorthogonalisation
                          (only the steps where estimates of the lost orthogonality,
-                         from alpha/beta alone, pass sqrt(eps_FP32), and the step after) */
+                         from alpha/beta alone, pass eps_FP32^(3/4), and the step after) */
 } edg_batch_opts;
 
 typedef struct {
