@@ -265,7 +265,13 @@ typedef struct {
   int64_t n_p;
   /* list-free mode (reps == NULL): v_j is value_vector(rep, vseed) */
   uint64_t vseed;
+  /* list-free mode's stand-in for the rank lookup: a binary search of the
+   * representative in a sorted array of the list's size (the index found is
+   * stored to a volatile sink, so the search is not optimised away) */
+  const int64_t *probe;
+  int64_t n_probe;
 } or_lookup;
+static volatile int64_t or_probe_sink;
 
 /* Deterministic vector entry as a function of a representative's value (used
  * where the representative list is not built): splitmix64, uniform in [-1,1)^2. */
@@ -314,6 +320,7 @@ static inline int64_t lookup_target(const or_lookup *L, int64_t tmp, const doubl
     if (!pid) return -1;
     *ninv = 1 / sqrt((double)((int64_t)(L->L1 * L->L2) / lid));
     *vj = value_vector(rep, L->vseed);
+    if (L->probe) or_probe_sink = find_state(rep, L->probe, L->n_probe);
     return 0;
   }
   int64_t j = find_state(rep, L->reps, L->n_p);
@@ -447,14 +454,18 @@ void or_hv_rows(int n_sites, const int *T1, const int *T2, int kx, int ky, const
 /* Rows of H v without the representative list, for sectors whose list is too
  * large to build on the host: `rows` are representatives (or_sample_reps) and
  * v is value_vector(representative, vseed), so a target costs its orbit walk
- * (representative_p, Momentum_Basis.cpp:472-543) but no rank lookup. */
+ * (representative_p, Momentum_Basis.cpp:472-543).  With `probe` (a sorted
+ * array of n_probe values, the list's size) each target also costs the
+ * binary search that finds its rank in the list (find_state); without it, no
+ * rank lookup. */
 void or_hv_rows_listless(int n_sites, const int *T1, const int *T2, int kx, int ky, const int64_t *rows,
                          const int32_t *row_lid, int64_t n_rows, uint64_t vseed, double *w_rows, double lambda,
                          const or_bond *bonds, int nb, double Ch, const or_tri *tris, int nt, double ChCh,
-                         const or_bowtie *bows, int nbw, int n_threads) {
+                         const or_bowtie *bows, int nbw, int n_threads, const int64_t *probe, int64_t n_probe) {
   or_lookup L;
   memset(&L, 0, sizeof L);
   L.n_sites = n_sites; L.T1 = T1; L.T2 = T2; L.vseed = vseed;
+  L.probe = probe; L.n_probe = n_probe;
   or_LxLy(T1, T2, n_sites, &L.L1, &L.L2);
   L.px = 2 * kx * OR_PI / L.L1;
   L.py = 2 * ky * OR_PI / L.L2;

@@ -78,7 +78,7 @@ void or_value_vector(const int64_t *reps, int64_t n, uint64_t seed, double *v);
 void or_hv_rows_listless(int n_sites, const int *T1, const int *T2, int kx, int ky, const int64_t *rows,
                          const int32_t *row_lid, int64_t n_rows, uint64_t vseed, double *w_rows, double lambda,
                          const or_bond *bonds, int nb, double Ch, const or_tri *tris, int nt, double ChCh,
-                         const or_bowtie *bows, int nbw, int n_threads);
+                         const or_bowtie *bows, int nbw, int n_threads, const int64_t *probe, int64_t n_probe);
 int64_t or_sample_reps(int n_sites, int n_ones, const int *T1, const int *T2, int kx, int ky, uint64_t seed,
                        int64_t n, int64_t *states, int32_t *lid);
 int64_t or_build_reps(int n_sites, int n_ones, const int *T1, const int *T2, int kx, int ky, int64_t **reps,

@@ -83,7 +83,7 @@ def lib() -> C.CDLL:
         L.or_hv_rows_listless.argtypes = [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int, C.c_int,
                                           C.c_void_p, C.c_void_p, C.c_int64, C.c_uint64, C.c_void_p, C.c_double,
                                           C.POINTER(Bond), C.c_int, C.c_double, C.POINTER(Tri), C.c_int,
-                                          C.c_double, C.POINTER(Bowtie), C.c_int, C.c_int]
+                                          C.c_double, C.POINTER(Bowtie), C.c_int, C.c_int, C.c_void_p, C.c_int64]
         L.or_sample_reps.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int, C.c_int,
                                      C.c_uint64, C.c_int64, C.c_void_p, C.c_void_p]
         L.or_sample_reps.restype = C.c_int64
@@ -243,16 +243,31 @@ def value_vector(reps: np.ndarray, seed: int) -> np.ndarray:
     return v
 
 
-def hv_rows_listless(model, rows: np.ndarray, row_lid: np.ndarray, vseed: int, n_threads: int = 0):
+def hv_rows_listless(model, rows: np.ndarray, row_lid: np.ndarray, vseed: int, n_threads: int = 0,
+                     probe: np.ndarray = None):
     """Rows of H v for representatives `rows`, with v = value_vector(., vseed),
-    without the sector's representative list (no rank lookups)."""
+    without the sector's representative list.  `probe`: a sorted int64 array
+    of the list's size; each target then also pays the binary search of the
+    rank lookup (its result unused)."""
     t = TermLists(model)
     rows = np.ascontiguousarray(rows, dtype=np.int64)
     row_lid = np.ascontiguousarray(row_lid, dtype=np.int32)
     out = np.zeros(len(rows), dtype=np.complex128)
+    pp, pn = (None, 0) if probe is None else (probe.ctypes.data, len(probe))
     lib().or_hv_rows_listless(model.n_sites, t.T1, t.T2, model.kx, model.ky, rows.ctypes.data, row_lid.ctypes.data,
                               len(rows), int(vseed), out.ctypes.data, model.Jz, t.bonds, t.nb, model.Ch, t.tris, t.nt,
-                              model.ChCh, t.bows, t.nbw, int(n_threads))
+                              model.ChCh, t.bows, t.nbw, int(n_threads), pp, pn)
+    return out
+
+
+def sorted_probe(n: int, lo: int, hi: int, seed: int = 9) -> np.ndarray:
+    """n sorted int64 values spread over [lo, hi) (cumulative random gaps): the
+    size and value range of a representative list, for hv_rows_listless's
+    rank-lookup stand-in."""
+    rng = np.random.default_rng(seed)
+    gap = max(1, (hi - lo) // max(n, 1))
+    out = np.cumsum(rng.integers(1, 2 * gap, size=n, dtype=np.int64))
+    out += lo
     return out
 
 
