@@ -616,6 +616,117 @@ __global__ void __launch_bounds__(kThreads) k_b_start(float2* __restrict__ V0, c
   }
 }
 
+// The end of many small segments at once.  Each stopped segment's FP64 Ritz
+// vectors need H x, the Rayleigh quotient <x|Hx>/|x|^2 and the residual
+// |Hx - theta x| / |x| (MixedFinish::rayleigh_async: six launches a vector).
+// Segments of up to kFinMaxN rows are finished together instead: all their
+// vectors are cut into tiles of kFinRows rows, and three launches (one CTA
+// per tile) cover them all -- u = x / norm; Hx from the stored rows in FP64
+// with the partials of |x|^2 and <x|Hx>; the residual's partials.  Each
+// vector's partials are summed in tile order by its last CTA (a ticket), so
+// the results do not depend on the other vectors.
+struct FinVec {
+  const uint64_t* row_ptr;
+  const uint32_t* col;
+  const uint16_t* vid;
+  const double2* vtab;  // FP64 value table
+  const double* ezz;
+  const uint8_t* lid;
+  const double* nrm;
+  const double* nrm_inv;
+  const double2* x;
+  double2* u;
+  double2* hx;
+  double* res;  // |x|^2, <x|Hx>, theta, residual
+  int64_t n;
+  int pack_cb;
+  int t0, t1;  // its tiles
+};
+struct FinTile {
+  int v;
+  int rows;
+  int64_t row0;
+};
+constexpr int kFinRows = 1024;
+constexpr int64_t kFinMaxN = 1 << 16;
+constexpr int64_t kFinCap = 1 << 23;  // vector entries per group of finishing segments
+
+__global__ void __launch_bounds__(kThreads) k_f_u(const FinVec* __restrict__ vs, const FinTile* __restrict__ ts) {
+  const FinTile t = ts[blockIdx.x];
+  const FinVec& V = vs[t.v];
+  for (int r = threadIdx.x; r < t.rows; r += blockDim.x) {
+    const int64_t i = t.row0 + r;
+    const double s = V.nrm_inv[V.lid[i]];
+    const double2 x = V.x[i];
+    V.u[i] = make_double2(x.x * s, x.y * s);
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_f_hv(const FinVec* __restrict__ vs, const FinTile* __restrict__ ts,
+                                                   double* __restrict__ part, int* __restrict__ cnt) {
+  constexpr int LPR = 8, kRows = 32 / LPR, kPass = (kThreads / 32) * kRows;
+  const FinTile t = ts[blockIdx.x];
+  const FinVec& V = vs[t.v];
+  const int lane = threadIdx.x & 31, sl = lane % LPR, sub = lane / LPR, wid = threadIdx.x >> 5;
+  Acc s0, s1;
+  for (int base = wid * kRows; base < t.rows; base += kPass) {  // uniform within the warp
+    const int r = base + sub;
+    uint64_t beg = 0, end = 0;
+    if (r < t.rows) {
+      beg = V.row_ptr[t.row0 + r];
+      end = V.row_ptr[t.row0 + r + 1];
+    }
+    double ar, ai;
+    csr_row<double, LPR, false, 1, kByVid>(beg, end, sl, V.col, V.vid, V.pack_cb, V.vtab, V.u, ar, ai);
+    if (r < t.rows && sl == 0) {
+      const int64_t i = t.row0 + r;
+      const double2 xi = V.x[i];
+      const double2 h = row_out(ar, ai, V.nrm[V.lid[i]], V.ezz[i], xi);
+      V.hx[i] = h;
+      s0.add(xi.x * xi.x + xi.y * xi.y);
+      s1.add(xi.x * h.x + xi.y * h.y);
+    }
+  }
+  double a = s0.value(), b = s1.value();
+  block_sum2(a, b);
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = a;
+    part[2 * blockIdx.x + 1] = b;
+  }
+  if (last_cta(cnt + t.v, V.t1 - V.t0)) {
+    seg_sum(part, V.t0, V.t1, a, b);
+    if (threadIdx.x == 0) {
+      V.res[0] = a;
+      V.res[1] = b;
+      V.res[2] = b / a;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_f_res(const FinVec* __restrict__ vs, const FinTile* __restrict__ ts,
+                                                    double* __restrict__ part, int* __restrict__ cnt) {
+  const FinTile t = ts[blockIdx.x];
+  const FinVec& V = vs[t.v];
+  const double th = __ldcg(V.res + 2);
+  Acc r2;
+  for (int r = threadIdx.x; r < t.rows; r += blockDim.x) {
+    const int64_t i = t.row0 + r;
+    const double2 a = V.x[i], h = V.hx[i];
+    const double dr = h.x - th * a.x, di = h.y - th * a.y;
+    r2.add(dr * dr + di * di);
+  }
+  double a = r2.value(), b = 0;
+  block_sum2(a, b);
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = a;
+    part[2 * blockIdx.x + 1] = 0.0;
+  }
+  if (last_cta(cnt + t.v, V.t1 - V.t0)) {
+    seg_sum(part, V.t0, V.t1, a, b);
+    if (threadIdx.x == 0) V.res[3] = sqrt(a / __ldcg(V.res));
+  }
+}
+
 struct Segment {
   edg_sector* sec = nullptr;
   edg_batch_request req{};
@@ -659,6 +770,13 @@ struct Batch {
   size_t ybuf_n = 0;
   double* d_start = nullptr;   // start vectors: kStartCtas partials, |x|^2
   int* d_start_cnt = nullptr;  // their ticket counter
+  // finishing small segments together (k_f_*): Ritz vectors, u, Hx; tables
+  double2 *fx = nullptr, *fu = nullptr, *fhx = nullptr;
+  FinVec* d_fv = nullptr;
+  FinTile* d_ft = nullptr;
+  double* d_fpart = nullptr;
+  int* d_fcnt = nullptr;
+  size_t fv_cap = 0, ft_cap = 0;
   // host seconds: add, step (graph replays and waits), finish (T, Ritz
   // vectors, Rayleigh quotients), release, rebuild (tables and graph capture)
   double timers[5] = {0, 0, 0, 0, 0};
@@ -676,9 +794,51 @@ struct Batch {
     cudaFree(ybuf);
     cudaFree(d_start);
     cudaFree(d_start_cnt);
+    void* f[] = {fx, fu, fhx, d_fv, d_ft, d_fpart, d_fcnt};
+    for (void* q : f) cudaFree(q);
     if (st) cudaStreamDestroy(st);
   }
 };
+
+// the queued small-segment vectors: tables up, then the three k_f_* launches
+static cudaError_t finish_group(Batch& B, std::vector<FinVec>& fv, std::vector<FinTile>& ft) {
+  if (fv.empty()) return cudaSuccess;
+  cudaError_t e = cudaSuccess;
+  if (fv.size() > B.fv_cap) {
+    cudaFree(B.d_fv);
+    cudaFree(B.d_fcnt);
+    B.d_fv = nullptr;
+    B.d_fcnt = nullptr;
+    B.fv_cap = 0;
+    if ((e = cudaMalloc(&B.d_fv, sizeof(FinVec) * fv.size())) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&B.d_fcnt, sizeof(int) * fv.size())) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(B.d_fcnt, 0, sizeof(int) * fv.size(), B.st)) != cudaSuccess) return e;
+    B.fv_cap = fv.size();
+  }
+  if (ft.size() > B.ft_cap) {
+    cudaFree(B.d_ft);
+    cudaFree(B.d_fpart);
+    B.d_ft = nullptr;
+    B.d_fpart = nullptr;
+    B.ft_cap = 0;
+    if ((e = cudaMalloc(&B.d_ft, sizeof(FinTile) * ft.size())) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&B.d_fpart, sizeof(double) * 2 * ft.size())) != cudaSuccess) return e;
+    B.ft_cap = ft.size();
+  }
+  if ((e = cudaMemcpyAsync(B.d_fv, fv.data(), sizeof(FinVec) * fv.size(), cudaMemcpyHostToDevice, B.st)) != cudaSuccess)
+    return e;
+  if ((e = cudaMemcpyAsync(B.d_ft, ft.data(), sizeof(FinTile) * ft.size(), cudaMemcpyHostToDevice, B.st)) != cudaSuccess)
+    return e;
+  const int nt = (int)ft.size();
+  k_f_u<<<nt, kThreads, 0, B.st>>>(B.d_fv, B.d_ft);
+  k_f_hv<<<nt, kThreads, 0, B.st>>>(B.d_fv, B.d_ft, B.d_fpart, B.d_fcnt);
+  k_f_res<<<nt, kThreads, 0, B.st>>>(B.d_fv, B.d_ft, B.d_fpart, B.d_fcnt);
+  // the host tables are reused by the next group
+  if ((e = cudaStreamSynchronize(B.st)) != cudaSuccess) return e;
+  fv.clear();
+  ft.clear();
+  return cudaGetLastError();
+}
 
 // V_0, u_0 of a segment from the random vector in its w, on the batch's stream
 static cudaError_t start_vector(Batch& B, const SegDev& d) {
@@ -814,14 +974,69 @@ void finish_stopped(Batch& B) {
     for (int& s : status)
       if (s == EDG_OK) s = fail(EDG_ERR_NOMEM, "batch: finishing scratch");
   }
+  // small segments together (k_f_*), larger ones a vector at a time
+  std::vector<FinVec> fv;
+  std::vector<FinTile> ft;
+  std::vector<int> group;  // the segments (indices into status) in fv
+  int64_t fel = 0;
+  auto flush = [&]() {
+    const cudaError_t fe = finish_group(B, fv, ft);
+    if (fe != cudaSuccess)
+      for (int k : group)
+        if (status[k] == EDG_OK) status[k] = cuda_fail(fe, "batch: FP64 H*v of the small segments");
+    group.clear();
+    fel = 0;
+  };
   for (int i = 0; i < ns; ++i) {
     if (status[i] != EDG_OK) continue;
     Segment& g = B.segs[idx[i]];
     const int m = g.st.j, na = sel[i].na;
+    const Sector& S = g.sec->s;
+    if (g.d.n <= kFinMaxN && S.vtab64) {
+      const int64_t need = g.d.n * na;
+      if (fel + need > kFinCap) flush();
+      if (!B.fx) {
+        if (cudaMalloc(&B.fx, sizeof(double2) * kFinCap) != cudaSuccess ||
+            cudaMalloc(&B.fu, sizeof(double2) * kFinCap) != cudaSuccess ||
+            cudaMalloc(&B.fhx, sizeof(double2) * kFinCap) != cudaSuccess) {
+          cudaGetLastError();
+          status[i] = fail(EDG_ERR_NOMEM, "batch: finishing scratch");
+          continue;
+        }
+      }
+      status[i] = B.fin.ritz_stored_to(B.st, g.d.V, g.d.n, m, na, m, B.ybuf + y_at[i], B.fx + fel);
+      if (status[i] != EDG_OK) continue;
+      group.push_back(i);
+      for (int q = 0; q < na; ++q) {
+        FinVec v{};
+        v.row_ptr = S.row_ptr;
+        v.col = S.col;
+        v.vid = S.vid;
+        v.vtab = reinterpret_cast<const double2*>(S.vtab64);
+        v.ezz = S.ezz;
+        v.lid = S.lid;
+        v.nrm = g.d.nrm;
+        v.nrm_inv = g.d.nrm_inv;
+        v.x = B.fx + fel + (int64_t)q * g.d.n;
+        v.u = B.fu + fel + (int64_t)q * g.d.n;
+        v.hx = B.fhx + fel + (int64_t)q * g.d.n;
+        v.res = B.fin.res + 4 * (off[i] + q);
+        v.n = g.d.n;
+        v.pack_cb = S.pack_cb;
+        v.t0 = (int)ft.size();
+        for (int64_t r0 = 0; r0 < g.d.n; r0 += kFinRows)
+          ft.push_back(FinTile{(int)fv.size(), (int)std::min<int64_t>(kFinRows, g.d.n - r0), r0});
+        v.t1 = (int)ft.size();
+        fv.push_back(v);
+      }
+      fel += need;
+      continue;
+    }
     status[i] = B.fin.ritz_stored(B.st, g.d.V, g.d.n, m, na, m, B.ybuf + y_at[i]);
     if (status[i] == EDG_OK && (e = B.fin.rayleigh_async(g.sec->s, B.st, g.d.n, na, B.fin.res + 4 * off[i])) != cudaSuccess)
       status[i] = cuda_fail(e, "batch: FP64 H*v");
   }
+  flush();
   std::vector<double> rr(4 * (size_t)std::max(total, 1));
   cudaMemcpyAsync(rr.data(), B.fin.res, sizeof(double) * 4 * total, cudaMemcpyDeviceToHost, B.st);
   if ((e = cudaStreamSynchronize(B.st)) != cudaSuccess) {

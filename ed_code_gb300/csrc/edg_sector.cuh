@@ -138,6 +138,9 @@ struct MixedFinish {
                   const double* ycoef = nullptr);
   int ritz_stored(cudaStream_t st, const double2* V, int64_t n, int m, int na, int cnt,
                   const double* ycoef = nullptr);
+  // the same, written to dst (na x n) instead of X
+  int ritz_stored_to(cudaStream_t st, const float2* V, int64_t n, int m, int na, int cnt, const double* ycoef,
+                     double2* dst);
   // res[4q..4q+3] = |x_q|^2, <x_q|H x_q>, Rayleigh quotient, residual, queued
   // on st (no wait)
   cudaError_t rayleigh_async(Sector& S, cudaStream_t st, int64_t n, int na, double* res_dev);

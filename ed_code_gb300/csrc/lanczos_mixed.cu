@@ -569,8 +569,9 @@ cudaError_t MixedFinish::reserve_x(int64_t n, int na) {
 
 template <class P>
 static int ritz_stored_t(MixedFinish& F, cudaStream_t st, const typename P::V* V, int64_t n, int m, int na, int cnt,
-                         const double* ycoef) {
+                         const double* ycoef, double2* dst = nullptr) {
   const double* yc = ycoef ? ycoef : F.y;
+  double2* X = dst ? dst : F.X;
   // the coefficients of up to kRitzChunk Ritz vectors sit in shared memory:
   // 64 bytes a Krylov vector, past the default 48 KB above 768 vectors
   // (the solvers cap the steps at 2000, i.e. 128 KB, within the opt-in limit)
@@ -587,7 +588,7 @@ static int ritz_stored_t(MixedFinish& F, cudaStream_t st, const typename P::V* V
   }
   for (int q0 = 0; q0 < na; q0 += kRitzChunk) {
     const int qn = std::min(kRitzChunk, na - q0);
-    k_ritz_vectors<P><<<grid_n(n), 256, 8 * (size_t)qn * cnt, st>>>(F.X, n, V, n, yc, m, cnt, q0, qn);
+    k_ritz_vectors<P><<<grid_n(n), 256, 8 * (size_t)qn * cnt, st>>>(X, n, V, n, yc, m, cnt, q0, qn);
   }
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? EDG_OK : cuda_fail(e, "mixed Lanczos: Ritz vectors");
@@ -601,6 +602,11 @@ int MixedFinish::ritz_stored(cudaStream_t st, const float2* V, int64_t n, int m,
 int MixedFinish::ritz_stored(cudaStream_t st, const double2* V, int64_t n, int m, int na, int cnt,
                              const double* ycoef) {
   return ritz_stored_t<P64>(*this, st, V, n, m, na, cnt, ycoef);
+}
+
+int MixedFinish::ritz_stored_to(cudaStream_t st, const float2* V, int64_t n, int m, int na, int cnt,
+                                const double* ycoef, double2* dst) {
+  return ritz_stored_t<P32>(*this, st, V, n, m, na, cnt, ycoef, dst);
 }
 
 cudaError_t MixedFinish::rayleigh_async(Sector& S, cudaStream_t st, int64_t n, int na, double* res_dev) {
