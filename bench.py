@@ -736,7 +736,8 @@ def run_precision(args):
         k = min(len(e32), len(e64))
         rel = (np.abs(e32[:k] - e64[:k]) / np.abs(e64[:k])).tolist()
         rows.append({"k": [kx, ky], "n_p": sec.n_p, "fp64": e64.tolist(), "fp32": e32.tolist(), "rel_err": rel,
-                     "fp32_residual_max": float(max(r32["residuals"])), "fp32_s": t1 - t0, "fp64_s": t2 - t1})
+                     "fp32_residual_max": float(max(r32["residuals"])), "fp32_s": t1 - t0, "fp64_s": t2 - t1,
+                     "reorth_steps_fp32_fp64": [r32["stats"]["reorth_steps"], r64["stats"]["reorth_steps"]]})
         sec.close()
     rng = np.random.default_rng(1)
     pick = [moms[int(i)] for i in rng.choice(len(moms), size=min(args.plain_sample, len(moms)), replace=False)]
@@ -826,7 +827,8 @@ def main():
     ap.add_argument("--batch-shape", choices=["small", "tri7x4"], default="small",
                     help="batch: 4x4/5x4 Hamiltonians with all momenta, or 7x4 ones with --momenta momenta")
     ap.add_argument("--reorth", type=int, default=1,
-                    help="precision/solve: 1 reorthogonalise every step, 0 locally against the last two vectors")
+                    help="precision: k > 0 reorthogonalise every k steps, -1 partially (Simon's estimates), "
+                         "0 locally against the last two vectors")
     ap.add_argument("--serve-tile", type=int, default=4096, help="serve: rows per tile of the batch kernels")
     ap.add_argument("--serve-tune", type=int, default=1, choices=[0, 1],
                     help="serve: time the batch tiles on the first requests (1) or keep --serve-tile (0)")

@@ -99,7 +99,7 @@ class edg_mixed_opts(C.Structure):
 
 class edg_mixed_stats(C.Structure):
     _fields_ = [("hv_calls", C.c_int64), ("hv_seconds", C.c_double), ("total_seconds", C.c_double),
-                ("passes", C.c_int), ("stored_vectors", C.c_int)]
+                ("passes", C.c_int), ("stored_vectors", C.c_int), ("reorth_steps", C.c_int)]
 
 
 # name -> (restype, argtypes); every exported symbol of include/edgpu.h

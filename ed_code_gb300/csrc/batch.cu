@@ -75,6 +75,7 @@ int cuda_fail(cudaError_t e, const char* what);
 namespace {
 
 constexpr int kThreads = 256;
+static_assert(kThreads == kProThreads, "pro_step runs on one CTA of the batch's kernels");
 constexpr int kMaxSteps = 511;  // Krylov vectors per segment: kMaxSteps + 1
 constexpr int kCgsY = 8;        // CTAs per tile over the Krylov index k
 constexpr int kBatchMaxEv = 32;
@@ -99,7 +100,6 @@ struct SegDev {
   double* ywork;          // want x 6 m_max: Ritz coefficients + inverse-iteration work
   double* aux;            // [0]: |w|^2 before reorthogonalisation
   double* omega;          // partial reorthogonalisation: 2 x (m_max + 2) estimates (nullptr: every step)
-  double pro_delta;       // its threshold on the estimates
   int64_t n;
   int m_max, want, check_every;
   int pack_cb;            // column bits of packed entries (vid == nullptr)
@@ -256,66 +256,10 @@ __global__ void __launch_bounds__(kThreads) k_b_hv(const SegDev* __restrict__ se
   }
 }
 
-// Partial reorthogonalisation (Simon, "The Lanczos algorithm with partial
-// reorthogonalization", Math. Comp. 42 (1984) 115): omega_{j,k} estimates
-// v_j^H v_k from T alone,
-//   beta_{j+1} omega_{j+1,k} = beta_{k+1} omega_{j,k+1} + (alpha_k - alpha_j) omega_{j,k}
-//                              + beta_k omega_{j,k-1} - beta_j omega_{j-1,k} + theta_{j,k},
-// with omega_{k,k} = 1 and a rounding term theta = eps (|alpha_k| + beta_{k+1}
-// + |alpha_j| + beta_{j+1}) taken with the sign that makes |omega| grow; eps
-// is the unit roundoff of the FP32 Krylov vectors.  Every step w is
-// reorthogonalised locally, against v_{j-1} and v_j (two vectors), so the
-// estimates against those two restart at eps.  When an estimate against an
-// older vector passes eps^(3/4), w is reorthogonalised against all stored
-// vectors at this step and the next (the vector before it carries the same
-// loss), and its estimates fall back to eps.  (Simon's sqrt(eps) keeps the
-// eigenvalues of T accurate, but with FP32 vectors it let 12 of 1,000
-// serving requests with 4 levels stop unconverged after 300 steps; eps^(3/4)
-// converged all of them at the same speed.)  beta_{j+1} here is |w| before
-// the reorthogonalisation.  One CTA (the segment's last of k_b_step) updates
-// the estimates; they live in two rows of S.omega by the parity of j.
-constexpr double kProDelta = 3.814697265625e-06;  // eps^(3/4) = 2^-18
+// Partial reorthogonalisation: the segment's last CTA of k_b_step updates
+// its estimates (pro_step, lanczos_common.cuh) and sets this step's range.
 __device__ void pro_update(const SegDev& S, SegState& st, int j, double w2) {
-  constexpr double kEps = 5.9604644775390625e-08;  // 2^-24
-  const double delta = S.pro_delta;
-  const int ld = S.m_max + 2;
-  double* cur = S.omega + (int64_t)(j & 1) * ld;        // omega_{j, .}
-  double* nxt = S.omega + (int64_t)((j + 1) & 1) * ld;  // omega_{j-1, .} in, omega_{j+1, .} out
-  const double bt = fmax(sqrt(w2), 1e-300);
-  const double aj = __ldcg(S.alpha + j), bj = j > 0 ? __ldcg(S.beta + j) : 0.0;
-  __shared__ double smax[kThreads];
-  __shared__ int s_full;
-  if (j == 0 && threadIdx.x == 0) cur[0] = 1.0;
-  __syncthreads();
-  double mx = 0.0;
-  for (int k = threadIdx.x; k + 1 < j; k += blockDim.x) {  // k <= j - 2: older than the local pair
-    const double bk1 = __ldcg(S.beta + k + 1), ak = __ldcg(S.alpha + k);
-    double x = bk1 * __ldcg(cur + k + 1) + (ak - aj) * __ldcg(cur + k) - bj * __ldcg(nxt + k);
-    if (k > 0) x += __ldcg(S.beta + k) * __ldcg(cur + k - 1);
-    x = (x + copysign(kEps * (fabs(ak) + bk1 + fabs(aj) + bt), x)) / bt;
-    nxt[k] = x;
-    mx = fmax(mx, fabs(x));
-  }
-  smax[threadIdx.x] = mx;
-  __syncthreads();
-  for (int h = kThreads / 2; h > 0; h >>= 1) {
-    if ((int)threadIdx.x < h) smax[threadIdx.x] = fmax(smax[threadIdx.x], smax[threadIdx.x + h]);
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    const bool cross = smax[0] > delta;
-    const bool full = cross || st.force;
-    st.kf = full ? 0 : (j > 0 ? j - 1 : 0);
-    st.force = cross ? 1 : 0;
-    if (full) ++st.n_orth;
-    if (j > 0) nxt[j - 1] = kEps;  // the local reorthogonalisation
-    nxt[j] = kEps;
-    nxt[j + 1] = 1.0;
-    s_full = full;
-  }
-  __syncthreads();
-  if (s_full)
-    for (int k = threadIdx.x; k + 1 < j; k += blockDim.x) nxt[k] = kEps;
+  pro_step(S.alpha, S.beta, j, w2, S.omega, S.m_max + 2, &st.force, &st.kf, &st.n_orth);
 }
 
 // w -= alpha_j V_j + beta_j V_{j-1}, and |w|^2 (tile partials of the stored
@@ -922,7 +866,10 @@ void finish_stopped(Batch& B) {
       continue;
     }
     const int n_try = std::min(kMaxEv, std::min(g.req.n_ev + 4, m));
-    const int nc = std::min(m, std::max(2 * n_try + 8, n_try)), nh = std::max(0, std::min(m - 1, nc + 2));
+    // the batch reorthogonalises (every step or partially), so copies of
+    // converged levels are rare and n_try + 4 eigenvalues of T (and two more
+    // of T-hat for the copy test) suffice
+    const int nc = std::min(m, n_try + 4), nh = std::max(0, std::min(m - 1, nc + 2));
     probs[i] = TdProb{g.d.alpha, 1, g.d.beta, m, nc, nh, n_try, 1, nullptr, nullptr, nullptr};
     y_at[i] = y_total;
     y_total += (size_t)n_try * m;
@@ -1258,7 +1205,6 @@ int edg_batch_add(edg_batch* bh, edg_sector* sec, const edg_batch_request* req) 
   if (e == cudaSuccess) e = cudaMalloc(&d.ywork, sizeof(double) * 6 * (size_t)d.want * m);
   if (e == cudaSuccess) e = cudaMalloc(&d.aux, sizeof(double) * 2);
   if (e == cudaSuccess && B.opts.reorth == 1) e = cudaMalloc(&d.omega, sizeof(double) * 2 * (m + 2));
-  d.pro_delta = kProDelta;
   if (e != cudaSuccess) {
     cudaGetLastError();
     release(g);

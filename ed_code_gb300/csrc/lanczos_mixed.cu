@@ -10,6 +10,10 @@
 //    them, twice (classical Gram-Schmidt with FP64 coefficients).  With FP32
 //    vectors orthogonality decays within a few steps once a level converges:
 //    every step (1) or every few steps keeps T exact; every 20 steps does not;
+//    reorth_every = -1 keeps every vector and reorthogonalises w against
+//    v_{j-1}, v_j every step and against all of them only where Simon's
+//    estimates of the lost orthogonality call for it (pro_step,
+//    lanczos_common.cuh);
 //    reorth_every = 0 reorthogonalises w locally against the two latest
 //    vectors each step and removes the copies of converged levels
 //    afterwards; it keeps every vector when they fit with room to spare,
@@ -106,8 +110,10 @@ __device__ __forceinline__ typename P::V mk(typename P::Real x, typename P::Real
 template <class P>
 __global__ void __launch_bounds__(kRedThreads) k_dot(const typename P::V* __restrict__ V, int64_t ld,
                                                      const typename P::V* __restrict__ x, int64_t n,
-                                                     double* __restrict__ part, const double* run = nullptr) {
+                                                     double* __restrict__ part, const double* run = nullptr,
+                                                     const int* kf = nullptr, int k0 = 0) {
   if (run && *run == 0.0) return;
+  if (kf && k0 + (int)blockIdx.y < *kf) return;  // before this step's Gram-Schmidt range
   const typename P::V* a = V + (int64_t)blockIdx.y * ld;
   typename P::A sr, si;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -138,8 +144,10 @@ __global__ void __launch_bounds__(kRedThreads) k_dot(const typename P::V* __rest
 // Sum the partials of vector k (one CTA per k); mode 0: complex result to
 // out[2k], mode 1: real part to out[0], mode 2: sqrt of the real part to out[0].
 __global__ void __launch_bounds__(kRedThreads) k_finish(const double* __restrict__ part, int nb, double* out,
-                                                        int mode, const double* run = nullptr) {
+                                                        int mode, const double* run = nullptr,
+                                                        const int* kf = nullptr, int k0 = 0) {
   if (run && *run == 0.0) return;
+  if (kf && k0 + (int)blockIdx.x < *kf) return;
   const double* p = part + (int64_t)blockIdx.x * nb * 2;
   __shared__ double rr[kRedThreads], ri[kRedThreads];
   double a = 0, b = 0;
@@ -299,8 +307,10 @@ __global__ void k_scale_inv(typename P::V* dst, const typename P::V* src, const 
 // rounding of y itself.
 template <class P>
 __global__ void k_sub(typename P::V* __restrict__ y, const typename P::V* __restrict__ V, int64_t ld,
-                      const double* __restrict__ q, int K, int64_t n, const double* run = nullptr) {
+                      const double* __restrict__ q, int K, int64_t n, const double* run = nullptr,
+                      const int* kf = nullptr, int k0 = 0) {
   if (run && *run == 0.0) return;
+  const int kb = kf ? max(0, *kf - k0) : 0;  // this step's range starts at V_kf
   using R = typename P::Real;
   extern __shared__ __align__(16) unsigned char sraw[];
   R* sq = reinterpret_cast<R*>(sraw);
@@ -309,7 +319,7 @@ __global__ void k_sub(typename P::V* __restrict__ y, const typename P::V* __rest
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const typename P::V y0 = y[i];
     R re = y0.x, im = y0.y;
-    for (int k = 0; k < K; ++k) {
+    for (int k = kb; k < K; ++k) {
       const typename P::V vv = V[(int64_t)k * ld + i];
       const R qr = sq[2 * k], qi = sq[2 * k + 1];
       re = fmr(-qr, vv.x, fmr(qi, vv.y, re));
@@ -325,10 +335,12 @@ __global__ void k_sub(typename P::V* __restrict__ y, const typename P::V* __rest
 // enough that the pass's own rounding matters, and the pass is repeated.
 // *run = 1.0 or 0.0 for the second pass's kernels.
 __global__ void __launch_bounds__(kRedThreads) k_cgs_decide(const double* __restrict__ q, int K,
-                                                            const double* __restrict__ xn2, double* run) {
+                                                            const double* __restrict__ xn2, double* run,
+                                                            const int* kf) {
   __shared__ double sm[kRedThreads];
   double a = 0;
-  for (int k = threadIdx.x; k < K; k += blockDim.x) a += q[2 * k] * q[2 * k] + q[2 * k + 1] * q[2 * k + 1];
+  for (int k = (kf ? *kf : 0) + threadIdx.x; k < K; k += blockDim.x)
+    a += q[2 * k] * q[2 * k] + q[2 * k + 1] * q[2 * k + 1];
   sm[threadIdx.x] = a;
   __syncthreads();
   for (int h = kRedThreads / 2; h > 0; h >>= 1) {
@@ -336,6 +348,14 @@ __global__ void __launch_bounds__(kRedThreads) k_cgs_decide(const double* __rest
     __syncthreads();
   }
   if (threadIdx.x == 0) *run = sm[0] > 1e-4 * *xn2 ? 1.0 : 0.0;
+}
+
+// Partial reorthogonalisation's estimates for this step (pro_step); state =
+// {force, kf, full steps}.
+__global__ void __launch_bounds__(kProThreads) k_pro(const double* __restrict__ alpha, const double* __restrict__ beta,
+                                                     int j, const double* __restrict__ w2, double* omega, int ld,
+                                                     int* state) {
+  pro_step(alpha, beta, j, *w2, omega, ld, state, state + 1, state + 2);
 }
 
 // Second pass of the resident-vector mode: X_e += sum_t y[e*m + j0 + t] V_{j0+t}
@@ -652,7 +672,8 @@ static int solve_mixed_t(Sector& S, const edg_mixed_opts& o, double* eigs, doubl
   const int m = (int)std::min<int64_t>(o.iterations, n);
   const int want = std::min(std::min(o.n_ev, kMaxEv), m);
   if (want <= 0 || m < 2) return fail(EDG_ERR_INVALID, "need n_ev >= 1 and at least 2 iterations");
-  const bool reorth = o.reorth_every > 0;
+  const bool partial = o.reorth_every < 0;  // partial reorthogonalisation (pro_step)
+  const bool reorth = o.reorth_every > 0 || partial;
   bool store = reorth;  // every Krylov vector kept in HBM
   cudaStream_t st = S.stream;
   using clk = std::chrono::steady_clock;
@@ -713,6 +734,13 @@ static int solve_mixed_t(Sector& S, const edg_mixed_opts& o, double* eigs, doubl
       (e = D.alloc(&lq, 4)) != cudaSuccess)
     return fail(EDG_ERR_NOMEM, "mixed Lanczos: scratch");
   cudaMemsetAsync(beta, 0, sizeof(double) * (m + 2), st);
+  double* omega = nullptr;
+  int* pstate = nullptr;  // {force, kf, full steps}
+  if (partial) {
+    if ((e = D.alloc(&omega, 2 * (size_t)(m + 2))) != cudaSuccess || (e = D.alloc(&pstate, 3)) != cudaSuccess)
+      return fail(EDG_ERR_NOMEM, "mixed Lanczos: scratch");
+    cudaMemsetAsync(pstate, 0, sizeof(int) * 3, st);
+  }
 
   auto vec = [&](int j) -> Vt* { return j < kept ? V + (int64_t)j * n : buf[(j - kept) % ring]; };
   auto norm_into = [&](const Vt* x, double* dst) {  // dst = |x| in FP64
@@ -769,7 +797,7 @@ static int solve_mixed_t(Sector& S, const edg_mixed_opts& o, double* eigs, doubl
       } else {
         k_step<P><<<kRedBlocks, kRedThreads, 0, st>>>(w, vec(j), j > 0 ? vec(j - 1) : nullptr, alpha + j, beta + j,
                                                       n, part);
-        if (!second && (j + 1) % o.reorth_every == 0) {
+        if (!second && (partial || (j + 1) % o.reorth_every == 0)) {
           // Periodic reorthogonalisation in its two-vector form: between two
           // reorthogonalisations v_j has drifted too, so it is cleaned against
           // v_0..v_{j-1} first, then w against v_0..v_j.  (Cleaning w alone
@@ -778,27 +806,31 @@ static int solve_mixed_t(Sector& S, const edg_mixed_opts& o, double* eigs, doubl
           // scal[0, 2K).  v_j's cleaning always takes a second pass; w's takes
           // one only when the first removed more than 1e-4 of |w|^2 (decided
           // on the device, lq[1]), as every step's reorthogonalisation needs
-          // it only now and then.
-          auto cgs2 = [&](Vt* x, int K, const double* xn2) {
+          // it only now and then.  With partial reorthogonalisation the range
+          // is v_kf..v_j, kf set on the device each step (pro_step): j - 1
+          // (local) or 0 (full, when the estimates call for it).
+          auto cgs2 = [&](Vt* x, int K, const double* xn2, const int* kf) {
             for (int pass = 0; pass < 2; ++pass) {
               const double* run = pass == 1 && xn2 ? lq + 1 : nullptr;
               for (int k0 = 0; k0 < K; k0 += 512) {
                 const int kk = std::min(512, K - k0);
-                k_dot<P><<<dim3(kRedBlocks, kk), kRedThreads, 0, st>>>(V + (int64_t)k0 * n, n, x, n, part, run);
-                k_finish<<<kk, kRedThreads, 0, st>>>(part, kRedBlocks, scal + 2 * k0, 0, run);
+                k_dot<P><<<dim3(kRedBlocks, kk), kRedThreads, 0, st>>>(V + (int64_t)k0 * n, n, x, n, part, run,
+                                                                       kf, k0);
+                k_finish<<<kk, kRedThreads, 0, st>>>(part, kRedBlocks, scal + 2 * k0, 0, run, kf, k0);
                 k_sub<P><<<grid_n(n), 256, sizeof(typename P::Real) * 2 * kk, st>>>(x, V + (int64_t)k0 * n, n,
-                                                                                    scal + 2 * k0, kk, n, run);
+                                                                                    scal + 2 * k0, kk, n, run, kf, k0);
               }
-              if (pass == 0 && xn2) k_cgs_decide<<<1, kRedThreads, 0, st>>>(scal, K, xn2, lq + 1);
+              if (pass == 0 && xn2) k_cgs_decide<<<1, kRedThreads, 0, st>>>(scal, K, xn2, lq + 1, kf);
             }
           };
-          if (o.reorth_every > 1 && j > 0) {
-            cgs2(vec(j), j, nullptr);
+          if (!partial && o.reorth_every > 1 && j > 0) {
+            cgs2(vec(j), j, nullptr, nullptr);
             norm_into(vec(j), scal + 2 * (m + 1));
             k_scale_inv<P><<<grid_n(n), 256, 0, st>>>(vec(j), vec(j), scal + 2 * (m + 1), n);
           }
           k_finish<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, lq, 1);  // |w|^2 after the step (k_step)
-          cgs2(w, j + 1, lq);
+          if (partial) k_pro<<<1, kProThreads, 0, st>>>(alpha, beta, j, lq, omega, m + 2, pstate);
+          cgs2(w, j + 1, lq, partial ? pstate + 1 : nullptr);
           norm_into(w, beta + j + 1);
         } else if (!second) {
           k_finish<<<1, kRedThreads, 0, st>>>(part, kRedBlocks, beta + j + 1, 2);
@@ -862,6 +894,10 @@ static int solve_mixed_t(Sector& S, const edg_mixed_opts& o, double* eigs, doubl
   }
   *n_out = (int64_t)keep.size();
   if (stats) {
+    stats->reorth_steps = reorth ? m : 0;
+    if (partial && cudaMemcpy(&stats->reorth_steps, pstate + 2, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+      stats->reorth_steps = -1;
+    if (o.reorth_every > 1) stats->reorth_steps = m / o.reorth_every;
     stats->hv_calls = hv_calls + na;
     stats->hv_seconds = t_hv;
     stats->passes = passes;

@@ -169,7 +169,9 @@ class GpuSector:
     def solve_mixed(self, n_ev: int = 6, iterations: int = 300, reorth_every: int = 1, seed: int = 1,
                     want_vectors: bool = False, fp64_vectors: bool = False):
         """Lowest eigenvalues with FP32 Krylov vectors (edg_solve_mixed); with
-        fp64_vectors the same algorithm in FP64 throughout.
+        fp64_vectors the same algorithm in FP64 throughout.  reorth_every: k > 0
+        full reorthogonalisation every k steps, -1 partial (where Simon's
+        estimates call for it), 0 local only.
         Returns dict(eigs, ritz, residuals, evecs, stats)."""
         k = min(n_ev, 32)
         eigs = np.empty(k, np.float64)

@@ -222,6 +222,11 @@ typedef struct {
   int reorth_every;         /* > 0: keep every FP32 Krylov vector and reorthogonalise the
                                last two against all of them every reorth_every steps
                                (1 or a few: FP32 vectors lose orthogonality fast);
+                               -1: keep every vector, reorthogonalise w against the two
+                               latest every step and against all of them only on the
+                               steps where Simon's estimates of the lost orthogonality
+                               (from alpha/beta alone) pass eps_FP32^(3/4), and the step
+                               after (partial reorthogonalisation);
                                0: w reorthogonalised against the two latest vectors only;
                                every vector kept when they fit with room to spare, else
                                as many as fit and the Ritz vectors finished by a second
@@ -237,6 +242,7 @@ typedef struct {
   double hv_seconds, total_seconds;
   int passes;
   int stored_vectors;       /* Krylov vectors kept in HBM (the rest lived in a ring) */
+  int reorth_steps;         /* steps reorthogonalised against all stored vectors */
 } edg_mixed_stats;
 
 /* Lowest eigenvalues with FP32 Krylov vectors and FP32 H*v; FP64 for alpha/beta

@@ -22,7 +22,7 @@ def gpu(cuda_device):
 # takes the Ritz vectors from storage in one pass; with storage capped it
 # stores the first k vectors (none for k = 0), keeps the later ones in a ring
 # and finishes the Ritz vectors with a second pass from v_{k-1}
-FORMS = [(1, None), (4, None), (0, None), (0, "100"), (0, "0")]
+FORMS = [(1, None), (4, None), (-1, None), (0, None), (0, "100"), (0, "0")]
 
 
 def _passes(reorth, keep):
@@ -43,6 +43,8 @@ def test_mixed_matches_reference(gpu, monkeypatch, name, n_ev, reorth, keep):
     assert rel.max() <= 1e-9, (eigs, ref, out["residuals"])
     assert np.all(out["residuals"][:n_ev] < 1e-3)
     assert out["stats"]["passes"] == _passes(reorth, keep)
+    if reorth == -1:  # partial: full passes only where the estimates call for them
+        assert 0 < out["stats"]["reorth_steps"] < 300, out["stats"]
 
 
 def test_stored_partial_and_resident_forms_agree(gpu, monkeypatch):
