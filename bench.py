@@ -826,9 +826,9 @@ def main():
     ap.add_argument("--momenta", type=int, default=30)
     ap.add_argument("--batch-shape", choices=["small", "tri7x4"], default="small",
                     help="batch: 4x4/5x4 Hamiltonians with all momenta, or 7x4 ones with --momenta momenta")
-    ap.add_argument("--reorth", type=int, default=1,
-                    help="precision: k > 0 reorthogonalise every k steps, -1 partially (Simon's estimates), "
-                         "0 locally against the last two vectors")
+    ap.add_argument("--reorth", type=int, default=-1,
+                    help="precision: -1 reorthogonalise partially (Simon's estimates; the default), k > 0 every k "
+                         "steps, 0 locally against the last two vectors")
     ap.add_argument("--serve-tile", type=int, default=4096, help="serve: rows per tile of the batch kernels")
     ap.add_argument("--serve-tune", type=int, default=1, choices=[0, 1],
                     help="serve: time the batch tiles on the first requests (1) or keep --serve-tile (0)")
