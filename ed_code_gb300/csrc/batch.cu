@@ -591,8 +591,53 @@ struct FinTile {
   int rows;
   int64_t row0;
 };
+// Their Ritz vectors X_q = sum_k y_q[k] V_k, also one launch for all: a CTA
+// per tile of a segment, the same per-row arithmetic as k_ritz_vectors (FP32
+// vectors, float-float sums, up to 8 vectors per sweep of V).
+struct RitzSeg {
+  const float2* V;
+  const double* y;  // na x m coefficients
+  double2* X;       // na x n
+  int64_t n;
+  int m, na;
+};
+constexpr int kFinRitzChunk = 8;
 constexpr int kFinRows = 1024;
 constexpr int64_t kFinMaxN = 1 << 16;
+
+__global__ void __launch_bounds__(kThreads) k_f_ritz(const RitzSeg* __restrict__ rs, const FinTile* __restrict__ ts) {
+  extern __shared__ __align__(16) float2 sy2[];  // kFinRitzChunk x m (head, tail)
+  const FinTile t = ts[blockIdx.x];
+  const RitzSeg& R = rs[t.v];
+  for (int q0 = 0; q0 < R.na; q0 += kFinRitzChunk) {
+    const int qn = min(kFinRitzChunk, R.na - q0);
+    __syncthreads();
+    for (int k = threadIdx.x; k < qn * R.m; k += blockDim.x) {
+      const FFScalar c(R.y[(int64_t)(q0 + k / R.m) * R.m + k % R.m]);
+      sy2[k] = make_float2(c.h, c.l);
+    }
+    __syncthreads();
+    for (int r = threadIdx.x; r < t.rows; r += blockDim.x) {
+      const int64_t i = t.row0 + r;
+      FFAcc ar[kFinRitzChunk], ai[kFinRitzChunk];
+      for (int j = 0; j < R.m; ++j) {
+        const float2 v = R.V[(int64_t)j * R.n + i];
+#pragma unroll
+        for (int q = 0; q < kFinRitzChunk; ++q)
+          if (q < qn) {
+            const float2 c = sy2[q * R.m + j];
+            ar[q].add_prod(c.x, v.x);
+            ar[q].lo = fmaf(c.y, v.x, ar[q].lo);
+            ai[q].add_prod(c.x, v.y);
+            ai[q].lo = fmaf(c.y, v.y, ai[q].lo);
+          }
+      }
+#pragma unroll
+      for (int q = 0; q < kFinRitzChunk; ++q)
+        if (q < qn) R.X[(int64_t)(q0 + q) * R.n + i] = make_double2(ar[q].value(), ai[q].value());
+    }
+  }
+}
 constexpr int64_t kFinCap = 1 << 23;  // vector entries per group of finishing segments
 
 __global__ void __launch_bounds__(kThreads) k_f_u(const FinVec* __restrict__ vs, const FinTile* __restrict__ ts) {
@@ -718,6 +763,9 @@ struct Batch {
   double2 *fx = nullptr, *fu = nullptr, *fhx = nullptr;
   FinVec* d_fv = nullptr;
   FinTile* d_ft = nullptr;
+  RitzSeg* d_rs = nullptr;
+  FinTile* d_rt = nullptr;
+  size_t rs_cap = 0, rt_cap = 0;
   double* d_fpart = nullptr;
   int* d_fcnt = nullptr;
   size_t fv_cap = 0, ft_cap = 0;
@@ -738,16 +786,39 @@ struct Batch {
     cudaFree(ybuf);
     cudaFree(d_start);
     cudaFree(d_start_cnt);
-    void* f[] = {fx, fu, fhx, d_fv, d_ft, d_fpart, d_fcnt};
+    void* f[] = {fx, fu, fhx, d_fv, d_ft, d_fpart, d_fcnt, d_rs, d_rt};
     for (void* q : f) cudaFree(q);
     if (st) cudaStreamDestroy(st);
   }
 };
 
 // the queued small-segment vectors: tables up, then the three k_f_* launches
-static cudaError_t finish_group(Batch& B, std::vector<FinVec>& fv, std::vector<FinTile>& ft) {
+static cudaError_t finish_group(Batch& B, std::vector<RitzSeg>& rs, std::vector<FinTile>& rt,
+                                std::vector<FinVec>& fv, std::vector<FinTile>& ft) {
   if (fv.empty()) return cudaSuccess;
   cudaError_t e = cudaSuccess;
+  // the Ritz vectors first
+  if (rs.size() > B.rs_cap) {
+    cudaFree(B.d_rs);
+    B.d_rs = nullptr;
+    B.rs_cap = 0;
+    if ((e = cudaMalloc(&B.d_rs, sizeof(RitzSeg) * rs.size())) != cudaSuccess) return e;
+    B.rs_cap = rs.size();
+  }
+  if (rt.size() > B.rt_cap) {
+    cudaFree(B.d_rt);
+    B.d_rt = nullptr;
+    B.rt_cap = 0;
+    if ((e = cudaMalloc(&B.d_rt, sizeof(FinTile) * rt.size())) != cudaSuccess) return e;
+    B.rt_cap = rt.size();
+  }
+  int m_max = 1;
+  for (const RitzSeg& r : rs) m_max = std::max(m_max, r.m);
+  if ((e = cudaMemcpyAsync(B.d_rs, rs.data(), sizeof(RitzSeg) * rs.size(), cudaMemcpyHostToDevice, B.st)) != cudaSuccess)
+    return e;
+  if ((e = cudaMemcpyAsync(B.d_rt, rt.data(), sizeof(FinTile) * rt.size(), cudaMemcpyHostToDevice, B.st)) != cudaSuccess)
+    return e;
+  k_f_ritz<<<(int)rt.size(), kThreads, sizeof(float2) * kFinRitzChunk * m_max, B.st>>>(B.d_rs, B.d_rt);
   if (fv.size() > B.fv_cap) {
     cudaFree(B.d_fv);
     cudaFree(B.d_fcnt);
@@ -779,6 +850,8 @@ static cudaError_t finish_group(Batch& B, std::vector<FinVec>& fv, std::vector<F
   k_f_res<<<nt, kThreads, 0, B.st>>>(B.d_fv, B.d_ft, B.d_fpart, B.d_fcnt);
   // the host tables are reused by the next group
   if ((e = cudaStreamSynchronize(B.st)) != cudaSuccess) return e;
+  rs.clear();
+  rt.clear();
   fv.clear();
   ft.clear();
   return cudaGetLastError();
@@ -922,12 +995,14 @@ void finish_stopped(Batch& B) {
       if (s == EDG_OK) s = fail(EDG_ERR_NOMEM, "batch: finishing scratch");
   }
   // small segments together (k_f_*), larger ones a vector at a time
+  std::vector<RitzSeg> rs;
+  std::vector<FinTile> rt;
   std::vector<FinVec> fv;
   std::vector<FinTile> ft;
   std::vector<int> group;  // the segments (indices into status) in fv
   int64_t fel = 0;
   auto flush = [&]() {
-    const cudaError_t fe = finish_group(B, fv, ft);
+    const cudaError_t fe = finish_group(B, rs, rt, fv, ft);
     if (fe != cudaSuccess)
       for (int k : group)
         if (status[k] == EDG_OK) status[k] = cuda_fail(fe, "batch: FP64 H*v of the small segments");
@@ -951,8 +1026,13 @@ void finish_stopped(Batch& B) {
           continue;
         }
       }
-      status[i] = B.fin.ritz_stored_to(B.st, g.d.V, g.d.n, m, na, m, B.ybuf + y_at[i], B.fx + fel);
-      if (status[i] != EDG_OK) continue;
+      if (m > kMaxSteps) {
+        status[i] = fail(EDG_ERR_INVALID, "batch: more steps than the finish holds");
+        continue;
+      }
+      for (int64_t r0 = 0; r0 < g.d.n; r0 += kFinRows)
+        rt.push_back(FinTile{(int)rs.size(), (int)std::min<int64_t>(kFinRows, g.d.n - r0), r0});
+      rs.push_back(RitzSeg{g.d.V, B.ybuf + y_at[i], B.fx + fel, g.d.n, m, na});
       group.push_back(i);
       for (int q = 0; q < na; ++q) {
         FinVec v{};
