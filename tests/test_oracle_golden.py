@@ -120,6 +120,12 @@ def test_listless_rows_equal_list_rows():
         a = O.hv_rows(model, reps, lid, v, rows)
         b = O.hv_rows_listless(model, reps[rows], lid[rows], 99)
         assert np.array_equal(a, b)
+        # the rank-lookup stand-in of the reference arm (a binary search in a
+        # sorted array of the list's size) costs time but changes no value
+        probe = O.sorted_probe(len(reps), int(reps.min()), int(reps.max()) + 1)
+        assert len(probe) == len(reps) and np.all(np.diff(probe) > 0) and probe[0] >= reps.min()
+        c = O.hv_rows_listless(model, reps[rows], lid[rows], 99, probe=probe)
+        assert np.array_equal(a, c)
         s, sl = O.sample_reps(model, 50, seed=5)
         assert len(s) == 50 and np.all(np.isin(s, reps))
         assert np.array_equal(sl, lid[np.searchsorted(reps, s)])
