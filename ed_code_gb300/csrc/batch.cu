@@ -938,7 +938,9 @@ void finish_stopped(Batch& B) {
       status[i] = fail(EDG_ERR_INVALID, "batch: a segment stopped before its first step");
       continue;
     }
-    const int n_try = std::min(kMaxEv, std::min(g.req.n_ev + 4, m));
+    // Ritz vectors finished: the wanted levels and two spares (a copy that
+    // passes the test on T is dropped by its Rayleigh quotient)
+    const int n_try = std::min(kMaxEv, std::min(g.req.n_ev + 2, m));
     // the batch reorthogonalises (every step or partially), so copies of
     // converged levels are rare and n_try + 4 eigenvalues of T (and two more
     // of T-hat for the copy test) suffice
