@@ -1020,13 +1020,20 @@ void finish_stopped(Batch& B) {
       const int64_t need = g.d.n * na;
       if (fel + need > kFinCap) flush();
       if (!B.fx) {
-        if (cudaMalloc(&B.fx, sizeof(double2) * kFinCap) != cudaSuccess ||
-            cudaMalloc(&B.fu, sizeof(double2) * kFinCap) != cudaSuccess ||
-            cudaMalloc(&B.fhx, sizeof(double2) * kFinCap) != cudaSuccess) {
+        double2 *a = nullptr, *b = nullptr, *c = nullptr;
+        if (cudaMalloc(&a, sizeof(double2) * kFinCap) != cudaSuccess ||
+            cudaMalloc(&b, sizeof(double2) * kFinCap) != cudaSuccess ||
+            cudaMalloc(&c, sizeof(double2) * kFinCap) != cudaSuccess) {
           cudaGetLastError();
+          cudaFree(a);
+          cudaFree(b);
+          cudaFree(c);
           status[i] = fail(EDG_ERR_NOMEM, "batch: finishing scratch");
           continue;
         }
+        B.fx = a;
+        B.fu = b;
+        B.fhx = c;
       }
       if (m > kMaxSteps) {
         status[i] = fail(EDG_ERR_INVALID, "batch: more steps than the finish holds");
