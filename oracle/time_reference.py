@@ -9,7 +9,12 @@ table-mode port (oracle.OracleSector.time_hv) is timed on the same host.  The
 ratio reference / port shows how well the port, which is what the GPU machine can
 run, stands in for the reference's CPU path.  Prints a markdown table.
 
-usage: python oracle/time_reference.py
+With --solves it times the reference's whole sector solve instead: ED2 (the
+reference's driver, sector_lanczos) on config 1's 4x4 sector and on one
+5x4 triangular sector of config 3's kind, both through the reference's dense
+path (n_p <= 10000), on all host threads and on one.
+
+usage: python oracle/time_reference.py [--solves]
 """
 from __future__ import annotations
 
@@ -45,7 +50,47 @@ def run_ref(inp: str, d: str, threads: int, reps: int) -> float:
     return float(open(os.path.join(d, "hv_time.txt")).read().split()[0])
 
 
+ED2 = os.path.join(HERE, "_ref", "ED2")
+SOLVES = [
+    ("cfg1_sq4x4_k00", dict(lattice="square", Lx=4, Ly=4), (0, 0, 0), 4),
+    ("cfg3_tri5x4_k00", dict(lattice="triangular", Lx=5, Ly=4, Jz=0.9, J2=0.3, Ch=0.25), (0, 0, 0), 3),
+]
+
+
+def solves(threads_list):
+    """Wall time of ED2 on each SOLVES sector (input file from lattice.py)."""
+    import time
+
+    if not os.path.exists(ED2):
+        raise SystemExit("build the reference first: make -C oracle ref REF_SRC=<reference src/>")
+    print("| sector | n_p | threads | ED2 wall time (s) | lowest level |")
+    print("|---|---|---|---|---|")
+    for name, kw, (Sz, kx, ky), nev in SOLVES:
+        spec = L.TorusSpec(**kw)
+        n_p = O.sector_dim(L.make_model(spec, Sz, kx, ky))
+        for thr in threads_list:
+            with tempfile.TemporaryDirectory() as d:
+                inp = os.path.join(d, "in.txt")
+                with open(inp, "w") as f:
+                    f.write(L.input_file_text(spec, Sz, kx, ky, num_eigenvalues=nev))
+                env = dict(os.environ, OMP_NUM_THREADS=str(thr), OPENBLAS_NUM_THREADS=str(thr))
+                t = time.perf_counter()
+                subprocess.run([ED2, inp, os.path.join(d, "out.txt")], check=True, stdout=subprocess.DEVNULL, env=env)
+                dt = time.perf_counter() - t
+                first, seen = None, False
+                for line in open(os.path.join(d, "out.txt")):
+                    if line.startswith("Energies"):
+                        seen = True
+                    elif seen and first is None and line.split():
+                        first = float(line.split()[0])
+            print(f"| {name} | {n_p} | {thr} | {dt:.2f} | {first} |", flush=True)
+
+
 def main():
+    if "--solves" in sys.argv:
+        threads = [int(x) for x in os.environ.get("EDG_SOLVE_THREADS", f"{os.cpu_count() or 1},1").split(",")]
+        solves(threads)
+        return
     if not os.path.exists(HARNESS):
         raise SystemExit("build the reference first: make -C oracle ref REF_SRC=<reference src/>")
     cores = os.cpu_count() or 1
