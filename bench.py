@@ -68,6 +68,18 @@ def profile_traffic(kernel_tag: str):
     return float(rec["dram_bytes_per_launch"]) if rec else None
 
 
+def roofline_record(B: float, B_base: float, ms: float, peak: float, peak_kind: str, traffic) -> dict:
+    """The line's roofline object: achieved GB/s and its fraction of the peak
+    by the kernel's algorithmic bytes B and by the problem's own bytes B_base,
+    with the DRAM traffic per launch (None when no capture is recorded)."""
+    achieved = B / (ms / 1e3) / 1e9
+    base = B_base / (ms / 1e3) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_kind": peak_kind, "traffic": traffic,
+            "traffic_over_algorithmic": None if traffic is None else traffic / B,
+            "base_bytes": B_base, "base_achieved": base, "base_frac": base / peak}
+
+
 def ingest_ncu(csv_path: str, tag: str, kernel: str, scale: float, note: str) -> dict:
     """Sum dram__bytes_read.sum + dram__bytes_write.sum per launch of `kernel`
     from an ncu --csv log (--metrics or --page raw layout), average over the
@@ -495,7 +507,6 @@ def run_device(args, world, rank, local_rank):
                                       "sHv on the same sectors")
 
     peak, peak_kind = measured_peak_hbm()
-    achieved = B / (ms_step / 1e3) / 1e9
     traffic = profile_traffic(f"hv_{mode}_{args.workload}_{args.dtype}")
     # the problem's own bytes (per row the representative, stabiliser byte,
     # v_i and w_i; per nonzero one v_j), whatever the kernel stores
@@ -516,11 +527,7 @@ def run_device(args, world, rank, local_rank):
                    "tune_ms_lpr_8_16_32": None if tune_ms is None else [round(float(x), 3) for x in tune_ms],
                    "matrix_free_GBps": B_mf / (mf_ms / 1e3) / 1e9,
                    "l2": "inputs larger than L2 (no flush needed)", "orbit_search": "torus" if sec.info["torus"] else "walk"},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_kind": peak_kind, "traffic": traffic,
-                     "traffic_over_algorithmic": None if traffic is None else traffic / B,
-                     "base_bytes": B_base, "base_achieved": B_base / (ms_step / 1e3) / 1e9,
-                     "base_frac": B_base / (ms_step / 1e3) / 1e9 / peak},
+        "roofline": roofline_record(B, B_base, ms_step, peak, peak_kind, traffic),
         "block_hv": block,
         "other_precision_hv": other,
         "cpu_baseline": cpu,

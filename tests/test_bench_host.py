@@ -73,3 +73,14 @@ def test_bad_arguments_are_rejected(argv, monkeypatch):
     monkeypatch.setattr(sys, "argv", ["bench.py"] + argv)
     with pytest.raises(SystemExit):
         bench.main()
+
+
+def test_roofline_record_by_both_byte_counts():
+    """frac by the kernel's bytes, base_frac by the problem's own bytes, and
+    traffic over the kernel's bytes, all against the same peak."""
+    r = bench.roofline_record(180.6e9, 118.3e9, 60.4, 6673.5, "measured", 272.6e9)
+    assert r["achieved"] == pytest.approx(180.6e9 / 0.0604 / 1e9)
+    assert r["frac"] == pytest.approx(r["achieved"] / 6673.5)
+    assert r["base_frac"] == pytest.approx(118.3e9 / 0.0604 / 1e9 / 6673.5)
+    assert r["traffic_over_algorithmic"] == pytest.approx(272.6 / 180.6)
+    assert bench.roofline_record(1e9, 1e9, 1.0, 1000.0, "fallback", None)["traffic_over_algorithmic"] is None
